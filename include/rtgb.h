@@ -1,0 +1,440 @@
+/*
+ * rtgb.h — C ABI of the GB300 wavefront path tracer.
+ *
+ * This is the drop-in boundary for the realtime per-pixel radiance path of
+ * elegracer/ray_tracing. The reference exposes that path only as C++ classes;
+ * every entry point below names the reference member it replaces (file:line,
+ * relative to the reference project root).
+ *
+ * Conventions
+ *   - Plain C: POD structs, raw pointers and sizes, status codes. No C++
+ *     exceptions cross this boundary; rtgb_last_error() returns the message
+ *     the reference would have thrown.
+ *   - One thread per handle. A handle owns its CUDA stream, its device scene,
+ *     all frame/history buffers and its CUDA graphs.
+ *   - Device views returned by rtgb_render_frame() stay valid until the next
+ *     rtgb_render_frame()/rtgb_prepare_scene()/rtgb_destroy() on that handle
+ *     (the reference states the same contract at
+ *     src/realtime/gpu/optix_renderer.h:84).
+ */
+#ifndef RTGB_H
+#define RTGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTGB_ABI_VERSION 1
+#define RTGB_MAX_CAMERAS 4          /* PackedCameraRig slots, src/realtime/camera_rig.h:27-30 */
+#define RTGB_EQUI_LUT_SIZE 1024     /* Equi62Lut1DParams::lut, src/realtime/camera_models.h:30-40 */
+
+typedef enum rtgb_status {
+    RTGB_OK = 0,
+    RTGB_INVALID_ARGUMENT = 1,   /* reference: std::invalid_argument / request validation */
+    RTGB_RUNTIME_ERROR = 2,      /* reference: std::runtime_error (CUDA failure, capacity) */
+    RTGB_NOT_PREPARED = 3,       /* render before rtgb_prepare_scene */
+    RTGB_DEVICE_FAULT_FLAG = 4,  /* a bounded device loop gave up and set the error word */
+    RTGB_UNSUPPORTED = 5
+} rtgb_status;
+
+/* ------------------------------------------------------------------------ */
+/* Scene: the packed (post prepare_gpu_scene) form of PackedScene.          */
+/* Mirrors src/realtime/gpu/launch_params.h:135-237 and                     */
+/* src/common/light_sampling.h:44-62, with Eigen members replaced by float. */
+/* ------------------------------------------------------------------------ */
+
+typedef enum rtgb_material_type {
+    RTGB_MATERIAL_LAMBERTIAN = 0,
+    RTGB_MATERIAL_METAL = 1,
+    RTGB_MATERIAL_DIELECTRIC = 2,
+    RTGB_MATERIAL_DIFFUSE_LIGHT = 3,
+    RTGB_MATERIAL_ISOTROPIC = 4,
+    RTGB_MATERIAL_OPENPBR = 5
+} rtgb_material_type;
+
+typedef enum rtgb_texture_type {
+    RTGB_TEXTURE_CONSTANT = 0,
+    RTGB_TEXTURE_CHECKER = 1,
+    RTGB_TEXTURE_IMAGE = 2,
+    RTGB_TEXTURE_NOISE = 3
+} rtgb_texture_type;
+
+typedef enum rtgb_analytic_light_type {
+    RTGB_ANALYTIC_SPHERE = 0,
+    RTGB_ANALYTIC_DISK = 1,
+    RTGB_ANALYTIC_RECT = 2,
+    RTGB_ANALYTIC_CYLINDER = 3,
+    RTGB_ANALYTIC_DISTANT = 4,
+    RTGB_ANALYTIC_DOME = 5
+} rtgb_analytic_light_type;
+
+/* PackedTexture, launch_params.h:226-237 */
+typedef struct rtgb_texture {
+    int32_t type;
+    int32_t even_texture;
+    int32_t odd_texture;
+    int32_t image_offset;   /* first texel in rtgb_scene::image_texels */
+    int32_t image_width;
+    int32_t image_height;
+    int32_t u_address_mode; /* 0 constant, 1 clamp, 2 periodic, 3 mirror */
+    int32_t v_address_mode;
+    int32_t filter_type;    /* 0 closest, 1 linear */
+    float scale;
+    float color[3];
+} rtgb_texture;
+
+/* MaterialSample, launch_params.h:216-223 */
+typedef struct rtgb_material {
+    int32_t albedo_texture;
+    int32_t emission_texture;
+    float ior;
+    float fuzz;
+    int32_t type;           /* rtgb_material_type */
+    int32_t openpbr_index;
+} rtgb_material;
+
+/* PackedSphere, launch_params.h:135-141 */
+typedef struct rtgb_sphere {
+    float center[3];
+    float radius;
+    int32_t material_index;
+} rtgb_sphere;
+
+/* PackedQuad, launch_params.h:143-152 */
+typedef struct rtgb_quad {
+    float origin[3];
+    float edge_u[3];
+    float edge_v[3];
+    int32_t material_index;
+} rtgb_quad;
+
+/* PackedTriangle, launch_params.h:154-175 */
+typedef struct rtgb_triangle {
+    float p0[3];
+    float p1[3];
+    float p2[3];
+    float n0[3];
+    float n1[3];
+    float n2[3];
+    float uv0[2];
+    float uv1[2];
+    float uv2[2];
+    int32_t material_index;
+    int32_t has_vertex_normals;
+    int32_t has_texcoords;
+} rtgb_triangle;
+
+/* PackedMedium, launch_params.h:201-214 (rotation rows are world->local) */
+typedef struct rtgb_medium {
+    float local_center_or_min[3];
+    float radius;
+    float local_max[3];
+    float density;
+    float rotation_row0[3];
+    float rotation_row1[3];
+    float rotation_row2[3];
+    float translation[3];
+    int32_t material_index;
+    int32_t boundary_type;  /* 0 sphere, 1 box */
+} rtgb_medium;
+
+/* PackedAnalyticLight, src/common/light_sampling.h:44-62 */
+typedef struct rtgb_analytic_light {
+    int32_t type;           /* rtgb_analytic_light_type */
+    float position[3];
+    float basis_x[3];
+    float basis_y[3];
+    float basis_z[3];
+    float radiance[3];
+    float radius;
+    float width;
+    float height;
+    float length;
+    float world_area;
+    float cos_theta_max;
+    float selection_pdf;
+    float cdf;
+    int32_t delta;
+    int32_t treat_as_point;
+    int32_t treat_as_line;
+} rtgb_analytic_light;
+
+/* PackedScene (src/realtime/scene_description.h:130-146) after
+ * prepare_gpu_scene (src/realtime/gpu/packed_scene_preparation.cpp:306-348).
+ * The emissive-geometry light CDF (build_light_distribution, :265-302) is
+ * computed by the library; the analytic-light CDF is the caller's (it comes
+ * from finalize_analytic_light_distribution, src/scene/analytic_light_compiler.cpp:15-39). */
+typedef struct rtgb_scene {
+    const rtgb_texture* textures;
+    int32_t texture_count;
+    const float* image_texels;          /* RGB float triplets */
+    int32_t image_texel_count;          /* number of triplets */
+    const rtgb_material* materials;
+    int32_t material_count;
+    const rtgb_sphere* spheres;
+    int32_t sphere_count;
+    const rtgb_quad* quads;
+    int32_t quad_count;
+    const rtgb_triangle* triangles;
+    int32_t triangle_count;
+    const rtgb_medium* media;
+    int32_t medium_count;
+    const rtgb_analytic_light* analytic_lights;
+    int32_t analytic_light_count;
+    float background[3];
+} rtgb_scene;
+
+/* ------------------------------------------------------------------------ */
+/* Cameras: PackedCamera / PackedCameraRig, src/realtime/camera_rig.h:15-30  */
+/* ------------------------------------------------------------------------ */
+
+typedef enum rtgb_camera_model {
+    RTGB_CAMERA_PINHOLE32 = 0,
+    RTGB_CAMERA_EQUI62_LUT1D = 1
+} rtgb_camera_model;
+
+/* Pinhole32Params, src/realtime/camera_models.h:14-24 */
+typedef struct rtgb_pinhole32 {
+    double fx, fy, cx, cy, k1, k2, k3, p1, p2;
+} rtgb_pinhole32;
+
+/* Equi62Lut1DParams, src/realtime/camera_models.h:26-37 */
+typedef struct rtgb_equi62_lut1d {
+    int32_t width;
+    int32_t height;
+    double fx, fy, cx, cy;
+    double radial[6];
+    double tangential[2];
+    double lut[RTGB_EQUI_LUT_SIZE];
+    double lut_step;
+} rtgb_equi62_lut1d;
+
+/* PackedCamera. T_rc maps camera coordinates (x right, y down, z forward)
+ * into renderer/world coordinates: rotation is row-major 3x3. */
+typedef struct rtgb_camera {
+    int32_t enabled;
+    int32_t width;
+    int32_t height;
+    int32_t model;          /* rtgb_camera_model */
+    double rotation[9];
+    double translation[3];
+    rtgb_pinhole32 pinhole;
+    rtgb_equi62_lut1d equi;
+} rtgb_camera;
+
+typedef struct rtgb_camera_rig {
+    int32_t active_count;
+    rtgb_camera cameras[RTGB_MAX_CAMERAS];
+} rtgb_camera_rig;
+
+/* RenderProfile, src/realtime/render_profile.h:10-25 */
+typedef struct rtgb_render_profile {
+    int32_t samples_per_pixel;
+    int32_t max_bounces;
+    int32_t enable_denoise;
+    int32_t rr_start_bounce;
+    double accumulation_reset_rotation_deg;
+    double accumulation_reset_translation;
+    int32_t enable_restir_di;
+    int32_t restir_initial_candidates;
+    int32_t restir_temporal_reuse;
+    int32_t restir_max_history_age;
+    int32_t restir_max_temporal_candidates;
+    int32_t restir_spatial_neighbors;
+    int32_t restir_max_spatial_candidates;
+    int32_t restir_bias_correction;   /* 0 off, 1 basic (src/common/restir_di.h:16-19) */
+    int32_t restir_min_analytic_lights;
+} rtgb_render_profile;
+
+/* ------------------------------------------------------------------------ */
+/* Renderer                                                                  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rtgb_renderer* rtgb_handle;
+
+typedef struct rtgb_create_info {
+    int32_t device;            /* CUDA ordinal (the reference hard-codes 0: optix_renderer.cpp:120) */
+    int32_t use_cuda_graph;    /* capture each frame's launch sequence as a CUDA graph */
+    int32_t debug_path_records;/* record per-path hit codes and radiance (parity tests) */
+} rtgb_create_info;
+
+/* DeviceRadianceFrameView (src/realtime/gpu/device_radiance_frame_view.h) plus
+ * the remaining DeviceFrameBuffers AOVs (launch_params.h:25-34) and
+ * RadianceTiming (optix_renderer.h:27-31). Pointers are device pointers. */
+typedef struct rtgb_camera_frame_view {
+    int32_t camera_index;
+    int32_t width;
+    int32_t height;
+    const void* beauty;           /* float4 per pixel */
+    const void* normal;           /* float4, [0,1]-encoded world normal */
+    const void* denoiser_normal;  /* float4, camera-space normal */
+    const void* albedo;           /* float4 */
+    const void* depth;            /* float */
+    const void* flow;             /* float2 */
+    const void* flow_trustworthiness; /* float */
+    float render_ms;
+    float denoise_ms;
+    float download_ms;
+} rtgb_camera_frame_view;
+
+typedef struct rtgb_frame_views {
+    int32_t camera_count;
+    rtgb_camera_frame_view cameras[RTGB_MAX_CAMERAS];
+    float frame_render_ms;        /* whole-frame CUDA-event time (all cameras, one launch sequence) */
+    uint32_t sample_stream;       /* stream used for this frame */
+    uint64_t rays_traced;         /* primary+extension+shadow+ReSTIR visibility rays */
+    uint64_t primary_rays;
+    uint64_t extension_rays;
+    uint64_t shadow_rays;
+    uint64_t restir_visibility_rays;
+} rtgb_frame_views;
+
+/* RestirDiagnostics, optix_renderer.h:43-51 */
+typedef struct rtgb_restir_stats {
+    int32_t pixel_count;
+    int32_t active_reservoir_count;
+    int32_t temporal_reuse_count;
+    int32_t spatial_reuse_count;
+    int32_t bias_corrected_count;
+    int32_t max_candidate_count;
+    int32_t max_age;
+} rtgb_restir_stats;
+
+/* AccelerationUpdateStats-like summary of the device LBVH. */
+typedef struct rtgb_acceleration_info {
+    int32_t primitive_count;      /* spheres + quads + triangles */
+    int32_t node_count;           /* internal BVH2 nodes */
+    int32_t analytic_light_node_count;
+    int32_t analytic_bvh_light_count; /* finite, non-point analytic lights in the light BVH */
+    float build_ms;               /* device build time (Morton, sort, hierarchy, bounds) */
+    int32_t traversal_stack_overflows; /* count since the last prepare; always reported, never silent */
+} rtgb_acceleration_info;
+
+/* Replaces OptixRenderer::OptixRenderer + RendererPool(int) (optix_renderer.cpp:104-109,
+ * renderer_pool.cpp:111-116): one handle serves every camera of a rig. */
+rtgb_status rtgb_create(const rtgb_create_info* info, rtgb_handle* out_handle);
+void rtgb_destroy(rtgb_handle handle);
+
+/* Last error message of this handle ("" if none). */
+const char* rtgb_last_error(rtgb_handle handle);
+
+/* Replaces OptixRenderer::prepare_scene / RendererPool::prepare_scene
+ * (optix_renderer.cpp:440-456, renderer_pool.cpp:120): packs the scene,
+ * builds the light CDF, uploads it and builds the device LBVH. Resets the
+ * sample stream to 0 and the temporal history, like use_prepared_scene. */
+rtgb_status rtgb_prepare_scene(rtgb_handle handle, const rtgb_scene* scene);
+
+/* OptixRenderer::reset_sequence (optix_renderer.cpp:178-181). */
+rtgb_status rtgb_reset_sequence(rtgb_handle handle, uint32_t sample_stream);
+
+/* OptixRenderer::reset_accumulation (optix_renderer.cpp:173-176). */
+rtgb_status rtgb_reset_accumulation(rtgb_handle handle);
+
+/* Replaces RendererPool::render_device_frame / render_frame
+ * (renderer_pool.cpp:160-185) and OptixRenderer::render_prepared_device
+ * (optix_renderer.cpp:434-457): all `active_cameras` leading slots of the rig
+ * render in ONE launch sequence on the handle's stream, then the frame's
+ * sample stream advances by one. Returns device views and timings. The call
+ * is asynchronous except for reading back the frame's ray counters. */
+rtgb_status rtgb_render_frame(rtgb_handle handle, const rtgb_camera_rig* rig,
+    const rtgb_render_profile* profile, int32_t active_cameras, rtgb_frame_views* out_views);
+
+/* Replaces download_radiance_frame_profiled (optix_renderer.cpp:283-326):
+ * copies the last frame's AOVs of one camera into caller-owned host memory.
+ * Any pointer may be NULL. Sizes are width*height*4 floats (rgba) and
+ * width*height floats (depth). Returns the copy time in *download_ms. */
+rtgb_status rtgb_download_frame(rtgb_handle handle, int32_t camera_index, float* beauty_rgba,
+    float* normal_rgba, float* albedo_rgba, float* depth, float* download_ms);
+
+/* Copies any device frame buffer of one camera (flow, trust, denoiser normal)
+ * to host: which = 0 beauty, 1 normal, 2 denoiser_normal, 3 albedo, 4 depth,
+ * 5 flow, 6 flow_trustworthiness. `bytes` must equal the buffer size. */
+rtgb_status rtgb_download_buffer(rtgb_handle handle, int32_t camera_index, int32_t which,
+    void* host, size_t bytes);
+
+/* OptixRenderer::restir_diagnostics (optix_renderer.cpp:183-215), per camera. */
+rtgb_status rtgb_restir_diagnostics(rtgb_handle handle, int32_t camera_index,
+    rtgb_restir_stats* out);
+
+/* Copies the last frame's reservoirs of one camera (84 bytes each, the
+ * RestirReservoir layout of src/common/restir_di.h:36-48). */
+rtgb_status rtgb_download_reservoirs(rtgb_handle handle, int32_t camera_index, void* host,
+    size_t bytes);
+
+/* OptixRenderer::render_direction_debug (optix_renderer.cpp:156-162 ->
+ * programs.cu:1807-1826): RGBA8 encoding of world ray directions. */
+rtgb_status rtgb_render_direction_debug(rtgb_handle handle, const rtgb_camera_rig* rig,
+    int32_t camera_index, uint8_t* host_rgba);
+
+/* Headless tone map of a camera's beauty into RGBA8 host memory, the
+ * arithmetic of src/realtime/viewer/cuda_gl_presenter.cu:23-38. */
+rtgb_status rtgb_tonemap_rgba8(rtgb_handle handle, int32_t camera_index, uint8_t* host_rgba);
+
+rtgb_status rtgb_acceleration_info_get(rtgb_handle handle, rtgb_acceleration_info* out);
+
+/* The CUDA stream (cudaStream_t) every launch of this handle is issued on. */
+void* rtgb_stream(rtgb_handle handle);
+
+/* Parity support (only with rtgb_create_info::debug_path_records).
+ * Per path (pixel-major, then sample) and bounce: hit code
+ *   -1 miss, (k << 28) | index with k = 0 sphere, 1 quad, 2 triangle,
+ *   4 medium, 5 analytic light; and the path's final radiance (float3).
+ * `paths` must equal the frame's total path count. */
+rtgb_status rtgb_download_path_records(rtgb_handle handle, int32_t camera_index,
+    int32_t* hit_codes, int32_t max_bounces, float* radiance_rgb, int64_t paths);
+
+/* LBVH parity: sorted Morton codes, the primitive order they induce and the
+ * Karras hierarchy (per internal node: left, right child; a negative child c
+ * is the leaf of sorted slot ~c). Arrays sized primitive_count and
+ * primitive_count-1 respectively. */
+rtgb_status rtgb_download_lbvh(rtgb_handle handle, uint32_t* sorted_morton,
+    int32_t* sorted_primitive, int32_t* node_children /* 2 per node */);
+
+/* ------------------------------------------------------------------------ */
+/* Host-side authoring helpers (C++23 host code in the same library).        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct rtgb_host_scene rtgb_host_scene;
+
+/* Builtin and procedural scenes. Names:
+ *   "cornell_box"        shared_scene_builders.cpp:101-139, :348-356
+ *   "smoke"              shared_scene_builders.cpp:475-487
+ *   "final_room"         shared_scene_builders.cpp:489-552
+ *   "bouncing_spheres"   shared_scene_builders.cpp:241-264
+ *   "restir_acceptance"  utils/render_restir_acceptance.cpp:41-93
+ *   "random_spheres"     seeded 22x22 sphere field + emissive rect lights
+ *   "triangle_terrain"   seeded displaced-grid terrain + icosphere instances
+ * `detail` scales the procedural scenes (light count / triangle budget);
+ * 0 selects the default size. */
+rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t detail,
+    rtgb_host_scene** out_scene);
+void rtgb_host_scene_destroy(rtgb_host_scene* scene);
+/* A view of the scene's arrays (owned by the host scene). */
+rtgb_status rtgb_host_scene_view(const rtgb_host_scene* scene, rtgb_scene* out_view);
+
+/* make_equi62_lut1d_params (src/realtime/camera_models.cpp:228-248). */
+rtgb_status rtgb_make_equi62_lut1d(int32_t width, int32_t height, double fx, double fy,
+    double cx, double cy, const double radial[6], const double tangential[2],
+    rtgb_equi62_lut1d* out);
+
+/* CameraRig::pack for a body pose T_bc (row-major rotation, translation):
+ * T_rc = (camera_to_renderer * R_bc, body_to_renderer * t_bc), camera_rig.cpp:73-97. */
+rtgb_status rtgb_pack_camera_pose(const double rotation_bc[9], const double translation_bc[3],
+    double rotation_rc[9], double translation_rc[3]);
+
+/* Default rig of a scene (the viewer's four yawed cameras, or the configured
+ * mixed pinhole/equi rig of the procedural scenes). */
+rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32_t width,
+    int32_t height, rtgb_camera_rig* out_rig);
+
+/* RenderProfile::quality/balanced/realtime (render_profile.h:27-63). */
+rtgb_status rtgb_profile_preset(const char* name, rtgb_render_profile* out_profile);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* RTGB_H */

@@ -1,0 +1,227 @@
+"""ctypes mirror of ``include/rtgb.h`` (the C ABI of the sm_103a path tracer).
+
+The structures below must match the header field for field; ``tests/``
+checks every exported symbol and the structure sizes against the library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+MAX_CAMERAS = 4
+EQUI_LUT_SIZE = 1024
+
+OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID_ARGUMENT", 2: "RUNTIME_ERROR", 3: "NOT_PREPARED",
+                4: "DEVICE_FAULT_FLAG", 5: "UNSUPPORTED"}
+
+f3 = C.c_float * 3
+
+
+class Texture(C.Structure):
+    _fields_ = [("type", C.c_int32), ("even_texture", C.c_int32), ("odd_texture", C.c_int32),
+                ("image_offset", C.c_int32), ("image_width", C.c_int32), ("image_height", C.c_int32),
+                ("u_address_mode", C.c_int32), ("v_address_mode", C.c_int32), ("filter_type", C.c_int32),
+                ("scale", C.c_float), ("color", f3)]
+
+
+class Material(C.Structure):
+    _fields_ = [("albedo_texture", C.c_int32), ("emission_texture", C.c_int32), ("ior", C.c_float),
+                ("fuzz", C.c_float), ("type", C.c_int32), ("openpbr_index", C.c_int32)]
+
+
+class Sphere(C.Structure):
+    _fields_ = [("center", f3), ("radius", C.c_float), ("material_index", C.c_int32)]
+
+
+class Quad(C.Structure):
+    _fields_ = [("origin", f3), ("edge_u", f3), ("edge_v", f3), ("material_index", C.c_int32)]
+
+
+class Triangle(C.Structure):
+    _fields_ = [("p0", f3), ("p1", f3), ("p2", f3), ("n0", f3), ("n1", f3), ("n2", f3),
+                ("uv0", C.c_float * 2), ("uv1", C.c_float * 2), ("uv2", C.c_float * 2),
+                ("material_index", C.c_int32), ("has_vertex_normals", C.c_int32), ("has_texcoords", C.c_int32)]
+
+
+class Medium(C.Structure):
+    _fields_ = [("local_center_or_min", f3), ("radius", C.c_float), ("local_max", f3), ("density", C.c_float),
+                ("rotation_row0", f3), ("rotation_row1", f3), ("rotation_row2", f3), ("translation", f3),
+                ("material_index", C.c_int32), ("boundary_type", C.c_int32)]
+
+
+class AnalyticLight(C.Structure):
+    _fields_ = [("type", C.c_int32), ("position", f3), ("basis_x", f3), ("basis_y", f3), ("basis_z", f3),
+                ("radiance", f3), ("radius", C.c_float), ("width", C.c_float), ("height", C.c_float),
+                ("length", C.c_float), ("world_area", C.c_float), ("cos_theta_max", C.c_float),
+                ("selection_pdf", C.c_float), ("cdf", C.c_float), ("delta", C.c_int32),
+                ("treat_as_point", C.c_int32), ("treat_as_line", C.c_int32)]
+
+
+class Scene(C.Structure):
+    _fields_ = [("textures", C.POINTER(Texture)), ("texture_count", C.c_int32),
+                ("image_texels", C.POINTER(C.c_float)), ("image_texel_count", C.c_int32),
+                ("materials", C.POINTER(Material)), ("material_count", C.c_int32),
+                ("spheres", C.POINTER(Sphere)), ("sphere_count", C.c_int32),
+                ("quads", C.POINTER(Quad)), ("quad_count", C.c_int32),
+                ("triangles", C.POINTER(Triangle)), ("triangle_count", C.c_int32),
+                ("media", C.POINTER(Medium)), ("medium_count", C.c_int32),
+                ("analytic_lights", C.POINTER(AnalyticLight)), ("analytic_light_count", C.c_int32),
+                ("background", f3)]
+
+
+class Pinhole32(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("fx", "fy", "cx", "cy", "k1", "k2", "k3", "p1", "p2")]
+
+
+class Equi62Lut1d(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("fx", C.c_double), ("fy", C.c_double),
+                ("cx", C.c_double), ("cy", C.c_double), ("radial", C.c_double * 6),
+                ("tangential", C.c_double * 2), ("lut", C.c_double * EQUI_LUT_SIZE), ("lut_step", C.c_double)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("width", C.c_int32), ("height", C.c_int32), ("model", C.c_int32),
+                ("rotation", C.c_double * 9), ("translation", C.c_double * 3),
+                ("pinhole", Pinhole32), ("equi", Equi62Lut1d)]
+
+
+class CameraRig(C.Structure):
+    _fields_ = [("active_count", C.c_int32), ("cameras", Camera * MAX_CAMERAS)]
+
+
+class RenderProfile(C.Structure):
+    _fields_ = [("samples_per_pixel", C.c_int32), ("max_bounces", C.c_int32), ("enable_denoise", C.c_int32),
+                ("rr_start_bounce", C.c_int32), ("accumulation_reset_rotation_deg", C.c_double),
+                ("accumulation_reset_translation", C.c_double), ("enable_restir_di", C.c_int32),
+                ("restir_initial_candidates", C.c_int32), ("restir_temporal_reuse", C.c_int32),
+                ("restir_max_history_age", C.c_int32), ("restir_max_temporal_candidates", C.c_int32),
+                ("restir_spatial_neighbors", C.c_int32), ("restir_max_spatial_candidates", C.c_int32),
+                ("restir_bias_correction", C.c_int32), ("restir_min_analytic_lights", C.c_int32)]
+
+
+class CreateInfo(C.Structure):
+    _fields_ = [("device", C.c_int32), ("use_cuda_graph", C.c_int32), ("debug_path_records", C.c_int32)]
+
+
+class CameraFrameView(C.Structure):
+    _fields_ = [("camera_index", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("beauty", C.c_void_p), ("normal", C.c_void_p), ("denoiser_normal", C.c_void_p),
+                ("albedo", C.c_void_p), ("depth", C.c_void_p), ("flow", C.c_void_p),
+                ("flow_trustworthiness", C.c_void_p), ("render_ms", C.c_float), ("denoise_ms", C.c_float),
+                ("download_ms", C.c_float)]
+
+
+class FrameViews(C.Structure):
+    _fields_ = [("camera_count", C.c_int32), ("cameras", CameraFrameView * MAX_CAMERAS),
+                ("frame_render_ms", C.c_float), ("sample_stream", C.c_uint32), ("rays_traced", C.c_uint64),
+                ("primary_rays", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("restir_visibility_rays", C.c_uint64)]
+
+
+class RestirDiagnostics(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("pixel_count", "active_reservoir_count", "temporal_reuse_count",
+                                         "spatial_reuse_count", "bias_corrected_count", "max_candidate_count",
+                                         "max_age")]
+
+
+class AccelerationInfo(C.Structure):
+    _fields_ = [("primitive_count", C.c_int32), ("node_count", C.c_int32),
+                ("analytic_light_node_count", C.c_int32), ("analytic_bvh_light_count", C.c_int32),
+                ("build_ms", C.c_float), ("traversal_stack_overflows", C.c_int32)]
+
+
+# 84-byte RestirReservoir (src/common/restir_di.h:36-48)
+RESERVOIR_DTYPE = np.dtype([
+    ("light_index", "<i4"), ("u0", "<f4"), ("u1", "<f4"),
+    ("position", "<f4", 3), ("normal", "<f4", 3), ("material_type", "<i4"), ("primitive_type", "<i4"),
+    ("primitive_index", "<i4"), ("weight_sum", "<f4"), ("selected_target", "<f4"), ("estimator_weight", "<f4"),
+    ("candidate_count", "<i4"), ("temporal_candidate_count", "<i4"), ("spatial_candidate_count", "<i4"),
+    ("bias_correction_source_count", "<i4"), ("age", "<i4"), ("valid", "<i4"),
+])
+assert RESERVOIR_DTYPE.itemsize == 84
+
+Handle = C.c_void_p
+P = C.POINTER
+
+# name -> (restype, argtypes); every rtgb_* symbol declared in include/rtgb.h
+SIGNATURES = {
+    "rtgb_create": (C.c_int, [P(CreateInfo), P(Handle)]),
+    "rtgb_destroy": (None, [Handle]),
+    "rtgb_last_error": (C.c_char_p, [Handle]),
+    "rtgb_prepare_scene": (C.c_int, [Handle, P(Scene)]),
+    "rtgb_reset_sequence": (C.c_int, [Handle, C.c_uint32]),
+    "rtgb_reset_accumulation": (C.c_int, [Handle]),
+    "rtgb_render_frame": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32, P(FrameViews)]),
+    "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      P(C.c_float)]),
+    "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),
+    "rtgb_restir_diagnostics": (C.c_int, [Handle, C.c_int32, P(RestirDiagnostics)]),
+    "rtgb_download_reservoirs": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_size_t]),
+    "rtgb_render_direction_debug": (C.c_int, [Handle, P(CameraRig), C.c_int32, C.c_void_p]),
+    "rtgb_tonemap_rgba8": (C.c_int, [Handle, C.c_int32, C.c_void_p]),
+    "rtgb_acceleration_info_get": (C.c_int, [Handle, P(AccelerationInfo)]),
+    "rtgb_stream": (C.c_void_p, [Handle]),
+    "rtgb_download_path_records": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                             C.c_int64]),
+    "rtgb_download_lbvh": (C.c_int, [Handle, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtgb_host_scene_create": (C.c_int, [C.c_char_p, C.c_uint32, C.c_int64, P(C.c_void_p)]),
+    "rtgb_host_scene_destroy": (None, [C.c_void_p]),
+    "rtgb_host_scene_view": (C.c_int, [C.c_void_p, P(Scene)]),
+    "rtgb_make_equi62_lut1d": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                         C.c_double, P(C.c_double), P(C.c_double), P(Equi62Lut1d)]),
+    "rtgb_pack_camera_pose": (C.c_int, [P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]),
+    "rtgb_default_rig": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, P(CameraRig)]),
+    "rtgb_profile_preset": (C.c_int, [C.c_char_p, P(RenderProfile)]),
+}
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load ``librtgb.so`` (building it in-tree when absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not path.exists():
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run __graft_entry__.build()")
+        _build.build_product()
+    lib = C.CDLL(str(path))
+    missing = []
+    for name, (res, args) in SIGNATURES.items():
+        try:
+            fn = getattr(lib, name)
+        except AttributeError:
+            missing.append(name)
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    lib.rtgb_missing_symbols = missing
+    _lib = lib
+    return lib
+
+
+class RtgbError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def check(status: int, handle=None, what: str = "") -> None:
+    if status != OK:
+        msg = what
+        if handle is not None:
+            raw = load().rtgb_last_error(handle)
+            if raw:
+                msg = f"{what}: {raw.decode()}"
+        raise RtgbError(status, msg)

@@ -1,0 +1,79 @@
+"""Host scenes, rigs and profiles through the C ABI's authoring helpers.
+
+Thin Python handles over ``rtgb_host_scene_*``, ``rtgb_default_rig`` and
+``rtgb_profile_preset`` (C++23 host code in ``librtgb.so``), so tests, the
+bench and the oracle all consume the exact arrays the library produces.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class HostScene:
+    """A builtin or procedural scene owned by the C++ host library."""
+
+    def __init__(self, name: str, seed: int = 0, detail: int = 0):
+        self.lib = abi.load()
+        self.name = name
+        self.ptr = C.c_void_p()
+        abi.check(self.lib.rtgb_host_scene_create(name.encode(), seed, detail, C.byref(self.ptr)),
+                  what=f"rtgb_host_scene_create({name})")
+        self.view = abi.Scene()
+        abi.check(self.lib.rtgb_host_scene_view(self.ptr, C.byref(self.view)), what="rtgb_host_scene_view")
+
+    def close(self):
+        if self.ptr:
+            self.lib.rtgb_host_scene_destroy(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def counts(self) -> dict[str, int]:
+        v = self.view
+        return {"spheres": v.sphere_count, "quads": v.quad_count, "triangles": v.triangle_count,
+                "media": v.medium_count, "analytic_lights": v.analytic_light_count,
+                "materials": v.material_count, "textures": v.texture_count}
+
+
+def default_rig(scene_name: str, camera_count: int, width: int = 0, height: int = 0) -> abi.CameraRig:
+    rig = abi.CameraRig()
+    abi.check(abi.load().rtgb_default_rig(scene_name.encode(), camera_count, width, height, C.byref(rig)),
+              what=f"rtgb_default_rig({scene_name})")
+    return rig
+
+
+def profile(name: str, **overrides) -> abi.RenderProfile:
+    p = abi.RenderProfile()
+    abi.check(abi.load().rtgb_profile_preset(name.encode(), C.byref(p)), what=f"rtgb_profile_preset({name})")
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def restir_acceptance_profile(spp: int, restir: bool, spatial_neighbors: int = 1) -> abi.RenderProfile:
+    """make_profile of utils/render_restir_acceptance.cpp:101-118."""
+    return profile("realtime", samples_per_pixel=spp, max_bounces=1, rr_start_bounce=2, enable_denoise=0,
+                   enable_restir_di=int(restir), restir_initial_candidates=8, restir_temporal_reuse=int(restir),
+                   restir_max_history_age=20, restir_max_temporal_candidates=64,
+                   restir_spatial_neighbors=spatial_neighbors if restir else 0, restir_max_spatial_candidates=8,
+                   restir_bias_correction=1, restir_min_analytic_lights=16)
+
+
+def display_u8(linear: np.ndarray) -> np.ndarray:
+    """display_channel of utils/render_restir_acceptance.cpp:149-153 (Reinhard, sqrt, lround)."""
+    x = np.maximum(linear.astype(np.float32), np.float32(0.0))
+    mapped = x / (np.float32(1.0) + x)
+    enc = np.sqrt(mapped)
+    v = np.float32(255.0) * np.minimum(enc, np.float32(1.0))
+    # lround of the float product: half away from zero (values are non-negative)
+    return np.floor(v.astype(np.float64) + 0.5).astype(np.uint8)
