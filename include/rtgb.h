@@ -342,6 +342,19 @@ rtgb_status rtgb_reset_accumulation(rtgb_handle handle);
 rtgb_status rtgb_render_frame(rtgb_handle handle, const rtgb_camera_rig* rig,
     const rtgb_render_profile* profile, int32_t active_cameras, rtgb_frame_views* out_views);
 
+/* rtgb_render_frame without the final wait: the frame is enqueued on the
+ * handle's stream and the call returns. Views and statistics of the last
+ * enqueued frame come from rtgb_frame_stats(). */
+rtgb_status rtgb_render_frame_async(rtgb_handle handle, const rtgb_camera_rig* rig,
+    const rtgb_render_profile* profile, int32_t active_cameras);
+
+/* Waits for the last enqueued frame and fills its views, timing and ray counts. */
+rtgb_status rtgb_frame_stats(rtgb_handle handle, rtgb_frame_views* out_views);
+
+/* Rays traced since the scene was prepared: primary, extension, shadow and
+ * ReSTIR visibility (waits for the stream). */
+rtgb_status rtgb_ray_totals(rtgb_handle handle, uint64_t totals[4]);
+
 /* Replaces download_radiance_frame_profiled (optix_renderer.cpp:283-326):
  * copies the last frame's AOVs of one camera into caller-owned host memory.
  * Any pointer may be NULL. Sizes are width*height*4 floats (rgba) and

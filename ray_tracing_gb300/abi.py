@@ -157,6 +157,9 @@ SIGNATURES = {
     "rtgb_reset_sequence": (C.c_int, [Handle, C.c_uint32]),
     "rtgb_reset_accumulation": (C.c_int, [Handle]),
     "rtgb_render_frame": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32, P(FrameViews)]),
+    "rtgb_render_frame_async": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32]),
+    "rtgb_frame_stats": (C.c_int, [Handle, P(FrameViews)]),
+    "rtgb_ray_totals": (C.c_int, [Handle, P(C.c_uint64)]),
     "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       P(C.c_float)]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),

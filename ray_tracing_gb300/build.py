@@ -32,7 +32,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: every a*b+c rounds twice, exactly like the -ffp-contract=off
 # oracle; the BVH box test uses explicit fmaf where contraction is wanted.
 NVCC_FLAGS = ARCH + [
-    "-O3", "-lineinfo", "--fmad=false", "-std=c++20", "-Xcompiler", "-fPIC",
+    "-O3", "-lineinfo", "--fmad=false", "-std=c++20", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
     "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills",
 ]
 CXX_FLAGS = ["-O2", "-std=c++23", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra"]

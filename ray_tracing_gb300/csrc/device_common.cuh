@@ -1,0 +1,713 @@
+// Device building blocks of the wavefront path tracer (sm_103a).
+//
+// Per-path arithmetic follows the reference's device functions operation for
+// operation (src/realtime/gpu/programs.cu, src/realtime/gpu/device_math.h,
+// src/common/light_sampling.h, src/common/restir_di.h) so that, compiled with
+// --fmad=false, one path reproduces the reference's radiance. The data layout
+// around it (SoA path streams, leaf-ordered primitive records, BVH2 nodes with
+// child boxes inline) is this project's own.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "rtgb.h"
+
+#define RTGB_HD __host__ __device__ __forceinline__
+#define RTGB_D __device__ __forceinline__
+
+namespace rtgb {
+
+constexpr float kRayEpsilon = 1e-3f;
+constexpr float kRayFar = 1e30f;
+constexpr float kPi = 3.14159265358979323846f;
+constexpr double kCameraEpsilon = 1e-12;
+constexpr int kTraversalStack = 64;
+
+// ---- float3 arithmetic (device_math.h:20-88) --------------------------------
+RTGB_HD float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+RTGB_HD float3 add(const float3& a, const float3& b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+RTGB_HD float3 sub(const float3& a, const float3& b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+RTGB_HD float3 mul(const float3& a, const float3& b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+RTGB_HD float3 mul(const float3& v, float s) { return f3(v.x * s, v.y * s, v.z * s); }
+RTGB_HD float3 divs(const float3& v, float s) {
+    const float inv = 1.0f / s;
+    return f3(v.x * inv, v.y * inv, v.z * inv);
+}
+RTGB_HD float dot(const float3& a, const float3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+RTGB_HD float3 cross(const float3& a, const float3& b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+RTGB_HD float len_sq(const float3& v) { return dot(v, v); }
+RTGB_HD float len(const float3& v) { return sqrtf(len_sq(v)); }
+RTGB_HD float3 normalize(const float3& v) {
+    const float l = len(v);
+    if (l <= 1e-8f) return f3(0.0f, 0.0f, 0.0f);
+    return divs(v, l);
+}
+RTGB_HD float3 reflect(const float3& i, const float3& n) { return sub(i, mul(n, 2.0f * dot(i, n))); }
+RTGB_HD float3 refract(const float3& i, const float3& n, float eta) {
+    const float ct = fminf(dot(mul(i, -1.0f), n), 1.0f);
+    const float3 perp = mul(add(i, mul(n, ct)), eta);
+    const float k = 1.0f - len_sq(perp);
+    return add(perp, mul(n, -sqrtf(fmaxf(k, 0.0f))));
+}
+RTGB_HD float max_comp(const float3& v) { return fmaxf(v.x, fmaxf(v.y, v.z)); }
+RTGB_HD float3 clamp3(const float3& v, float lo, float hi) {
+    return f3(fminf(fmaxf(v.x, lo), hi), fminf(fmaxf(v.y, lo), hi), fminf(fmaxf(v.z, lo), hi));
+}
+RTGB_HD bool near_zero(const float3& v) {
+    return fabsf(v.x) < 1e-7f && fabsf(v.y) < 1e-7f && fabsf(v.z) < 1e-7f;
+}
+RTGB_HD float3 ld3(const float* p) { return f3(p[0], p[1], p[2]); }
+RTGB_HD float3 xyz(const float4& v) { return f3(v.x, v.y, v.z); }
+RTGB_HD float4 f4(const float3& v, float w) { return make_float4(v.x, v.y, v.z, w); }
+
+// ---- per-path RNG (programs.cu:104-137) ---------------------------------------
+RTGB_HD uint32_t hash_u32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+RTGB_HD uint32_t rng_for(int pixel, int sample, uint32_t stream) {
+    return hash_u32(static_cast<uint32_t>(pixel) * 1973u ^ static_cast<uint32_t>(sample + 1) * 9277u
+                    ^ static_cast<uint32_t>(stream + 1) * 26699u ^ 0x9e3779b9u);
+}
+RTGB_HD float rnd(uint32_t& s) {
+    s = s * 1664525u + 1013904223u;
+    return static_cast<float>(s & 0x00ffffffu) * (1.0f / 16777216.0f);
+}
+// Draws are consumed left to right (x, y, z).
+RTGB_D float3 random_in_unit_sphere(uint32_t& rng) {
+    // The reference loops until acceptance; 1e6 rejections have probability
+    // (1 - pi/6)^1e6, so the bound never binds but keeps the loop finite.
+    for (int guard = 0; guard < 1000000; ++guard) {
+        const float a = rnd(rng) * 2.0f - 1.0f;
+        const float b = rnd(rng) * 2.0f - 1.0f;
+        const float c = rnd(rng) * 2.0f - 1.0f;
+        const float3 p = f3(a, b, c);
+        if (len_sq(p) < 1.0f) return p;
+    }
+    return f3(0.0f, 0.0f, 0.0f);
+}
+RTGB_D float3 random_unit_vector(uint32_t& rng) { return normalize(random_in_unit_sphere(rng)); }
+
+// ---- light pdfs (light_sampling.h:64-124) --------------------------------------
+RTGB_HD float uniform_sphere_pdf() { return 0.07957747154594767f; }
+RTGB_HD float uniform_cone_pdf(float ctm) {
+    const float sa = 6.28318530717958648f * (1.0f - ctm);
+    return sa > 1e-12f ? 1.0f / sa : 0.0f;
+}
+RTGB_HD float area_pdf(float area, float d2, float ac) {
+    if (area <= 1e-12f || d2 <= 0.0f || ac <= 1e-8f) return 0.0f;
+    return d2 / (area * ac);
+}
+RTGB_HD float power_heuristic(float a, float b) {
+    if (a <= 0.0f) return 0.0f;
+    const float a2 = a * a;
+    const float b2 = b * b;
+    return a2 / (a2 + b2);
+}
+// First i with u < cdf[i] (else count-1): an upper-bound binary search over the
+// non-decreasing CDF returns the same index as the reference's linear scan
+// (light_sampling.h:90-116) in O(log n).
+RTGB_D int sample_cdf(const float* __restrict__ cdf, int count, float u) {
+    if (count <= 0) return -1;
+    const float s = u < 0.0f ? 0.0f : (u < 1.0f ? u : 0.99999994f);
+    int lo = 0, hi = count;  // first index in [lo, hi) with s < cdf[i]
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s < __ldg(cdf + mid)) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo < count ? lo : count - 1;
+}
+RTGB_HD void sample_uniform_triangle(float u0, float u1, float& w0, float& w1, float& w2) {
+    const float su = sqrtf(u0 < 0.0f ? 0.0f : (u0 < 1.0f ? u0 : 1.0f));
+    w0 = 1.0f - su;
+    w1 = su * (1.0f - u1);
+    w2 = su * u1;
+}
+
+// ---- reservoirs (restir_di.h:21-199), the reference's 84-byte layout ----------
+struct Candidate {
+    int light_index;
+    float u0;
+    float u1;
+};
+struct Surface {
+    float position[3];
+    float normal[3];
+    int material_type;
+    int primitive_type;
+    int primitive_index;
+};
+struct Reservoir {
+    Candidate selected;
+    Surface surface;
+    float weight_sum;
+    float selected_target;
+    float estimator_weight;
+    int candidate_count;
+    int temporal_candidate_count;
+    int spatial_candidate_count;
+    int bias_correction_source_count;
+    int age;
+    int valid;
+};
+static_assert(sizeof(Reservoir) == 84, "RestirReservoir layout");
+
+RTGB_HD Reservoir empty_reservoir() {
+    Reservoir r;
+    r.selected = Candidate{-1, 0.0f, 0.0f};
+    for (int i = 0; i < 3; ++i) {
+        r.surface.position[i] = 0.0f;
+        r.surface.normal[i] = 0.0f;
+    }
+    r.surface.material_type = -1;
+    r.surface.primitive_type = -1;
+    r.surface.primitive_index = -1;
+    r.weight_sum = 0.0f;
+    r.selected_target = 0.0f;
+    r.estimator_weight = 0.0f;
+    r.candidate_count = 0;
+    r.temporal_candidate_count = 0;
+    r.spatial_candidate_count = 0;
+    r.bias_correction_source_count = 0;
+    r.age = 0;
+    r.valid = 0;
+    return r;
+}
+
+RTGB_HD float clamp_unit(float v) { return v < 0.0f ? 0.0f : (v < 1.0f ? v : 0.99999994f); }
+RTGB_HD bool finite_positive(float v) { return v > 0.0f && isfinite(v); }
+
+RTGB_HD bool reservoir_update(Reservoir& r, const Candidate& c, float target, float weight, int m, float u) {
+    if (c.light_index < 0 || m <= 0) return false;
+    r.candidate_count += m;
+    if (!finite_positive(target) || !finite_positive(weight)) return false;
+    const float next = r.weight_sum + weight;
+    if (!finite_positive(next)) return false;
+    const bool sel = clamp_unit(u) * next < weight;
+    if (sel) {
+        r.selected = c;
+        r.selected_target = target;
+        r.valid = 1;
+    }
+    r.weight_sum = next;
+    return sel;
+}
+
+RTGB_HD void reservoir_finalize(Reservoir& r) {
+    r.estimator_weight = 0.0f;
+    if (r.valid == 0 || r.candidate_count <= 0 || !finite_positive(r.selected_target)
+        || !finite_positive(r.weight_sum)) {
+        r.valid = 0;
+        return;
+    }
+    r.estimator_weight = r.weight_sum / (static_cast<float>(r.candidate_count) * r.selected_target);
+    if (!finite_positive(r.estimator_weight)) {
+        r.valid = 0;
+        r.estimator_weight = 0.0f;
+    }
+}
+
+RTGB_HD void reservoir_finalize_basic(Reservoir& r, float sel_t, float sum, int n) {
+    r.estimator_weight = 0.0f;
+    r.bias_correction_source_count = n > 0 ? n : 0;
+    if (r.valid == 0 || n <= 0 || !finite_positive(r.selected_target) || !finite_positive(r.weight_sum)
+        || !finite_positive(sel_t) || !finite_positive(sum)) {
+        r.valid = 0;
+        return;
+    }
+    r.estimator_weight = r.weight_sum * sel_t / (r.selected_target * sum);
+    if (!finite_positive(r.estimator_weight)) {
+        r.valid = 0;
+        r.estimator_weight = 0.0f;
+    }
+}
+
+RTGB_HD bool surface_valid(const Surface& cur, const Reservoir& prev, float max_dist, float min_dot, int max_age) {
+    if (prev.valid == 0 || prev.selected.light_index < 0 || prev.age < 0 || prev.age >= max_age
+        || cur.material_type != prev.surface.material_type || cur.primitive_type != prev.surface.primitive_type
+        || cur.primitive_index != prev.surface.primitive_index) {
+        return false;
+    }
+    const float limit = max_dist > 0.0f ? max_dist : 0.0f;
+    const float dx = cur.position[0] - prev.surface.position[0];
+    const float dy = cur.position[1] - prev.surface.position[1];
+    const float dz = cur.position[2] - prev.surface.position[2];
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float nd = cur.normal[0] * prev.surface.normal[0] + cur.normal[1] * prev.surface.normal[1]
+                     + cur.normal[2] * prev.surface.normal[2];
+    return d2 <= limit * limit && nd >= min_dot;
+}
+
+struct MergeResult {
+    int multiplicity;
+    int selected;
+};
+
+RTGB_HD MergeResult reservoir_merge(Reservoir& cur, const Reservoir& prev, float target, int max_c, float u,
+    bool temporal) {
+    if (prev.valid == 0 || prev.candidate_count <= 0 || !finite_positive(prev.estimator_weight)) {
+        return MergeResult{0, 0};
+    }
+    int m = prev.candidate_count;
+    if (max_c > 0 && m > max_c) m = max_c;
+    const float w = finite_positive(target) ? target * prev.estimator_weight * static_cast<float>(m) : 0.0f;
+    const bool sel = reservoir_update(cur, prev.selected, target, w, m, u);
+    if (temporal) {
+        cur.temporal_candidate_count += m;
+        cur.age = prev.age + 1;
+    } else {
+        cur.spatial_candidate_count += m;
+    }
+    return MergeResult{m, sel ? 1 : 0};
+}
+
+// ---- device scene ------------------------------------------------------------
+
+// Emissive-geometry light (PackedLight, light_sampling.h:22-27).
+struct PackedLight {
+    int type;  // 0 sphere, 1 quad, 2 triangle, 3 environment
+    int primitive_index;
+    float selection_pdf;
+    float cdf;
+};
+
+// One leaf-ordered primitive record, 64 bytes (four float4):
+//   sphere:   [0] center.xyz radius
+//   quad:     [0] origin.xyz n.x  [1] edge_u.xyz n.y  [2] edge_v.xyz n.z  [3] w.xyz
+//   triangle: [0] p0.xyz          [1] e1.xyz          [2] e2.xyz
+// [3].w always holds the primitive code (type << 28 | index) as int bits.
+// n = unit quad normal and w = n / |n|^2 are computed on the host with the
+// reference's float operations (programs.cu:1451-1476), e1/e2 = p1-p0, p2-p0.
+struct PrimRecord {
+    float4 q[4];
+};
+
+// BVH2 node with both children's boxes inline, 64 bytes:
+//   a = (c0.lo.xyz, c0 child) b = (c0.hi.xyz, c1 child) c = (c1.lo.xyz, -) d = (c1.hi.xyz, -)
+// A child >= 0 is an internal node; a child < 0 is the leaf of sorted slot ~child.
+struct BvhNode {
+    float4 a, b, c, d;
+};
+
+struct DeviceScene {
+    const PrimRecord* prims;      // leaf order
+    const BvhNode* nodes;
+    int prim_count;
+    int node_count;
+    const rtgb_sphere* spheres;
+    const rtgb_quad* quads;
+    const rtgb_triangle* triangles;
+    const rtgb_medium* media;
+    const rtgb_material* materials;
+    const rtgb_texture* textures;
+    const float* texels;           // RGB triplets
+    int sphere_count, quad_count, triangle_count, medium_count, material_count, texture_count, texel_count;
+    const PackedLight* lights;
+    const float* light_cdf;
+    int light_count;
+    int environment_light;        // index into lights or -1
+    const int* sphere_light;       // primitive -> light index or -1
+    const int* quad_light;
+    const int* triangle_light;
+    const rtgb_analytic_light* analytic;
+    const float* analytic_cdf;
+    int analytic_count;
+    const BvhNode* analytic_nodes;  // BVH over finite, non-point analytic lights
+    const int* analytic_leaf;       // sorted slot -> analytic light index
+    int analytic_bvh_count;
+    int analytic_node_count;
+    const int* infinite_analytic;   // distant/dome light indices, reference order
+    int infinite_analytic_count;
+    float background[3];
+};
+
+// ---- cameras: programs.cu:304-537 ------------------------------------------------
+
+struct CameraDev {
+    int width, height, model, lut_monotone;
+    long long pixel_offset;   // first pixel of this camera in frame-wide arrays
+    long long path_offset;    // pixel_offset * spp
+    float origin_f[3], bx_f[3], by_f[3], bz_f[3];  // static_cast<float> of the double pose
+    double origin[3], bx[3], by[3], bz[3];
+    double pin[9];                                  // fx fy cx cy k1 k2 k3 p1 p2
+    double eq_fx, eq_fy, eq_cx, eq_cy, eq_tan[2], lut_step;
+    const double* lut;                              // 1024 doubles (device)
+    const float4* dirs;                             // per-pixel camera-space direction
+};
+
+struct D2 {
+    double x, y;
+};
+
+RTGB_HD D2 distort_pinhole(const double* p, const D2& xy) {
+    const double x = xy.x, y = xy.y;
+    const double x2 = x * x, y2 = y * y, xyt = x * y;
+    const double r2 = x2 + y2, r4 = r2 * r2, r6 = r4 * r2;
+    const double radial = 1.0 + p[4] * r2 + p[5] * r4 + p[6] * r6;
+    return D2{x * radial + p[8] * (r2 + 2.0 * x2) + 2.0 * p[7] * xyt,
+        y * radial + p[7] * (r2 + 2.0 * y2) + 2.0 * p[8] * xyt};
+}
+
+RTGB_HD bool solve2(double a00, double a01, double a10, double a11, const D2& rhs, D2& d) {
+    const double det = a00 * a11 - a01 * a10;
+    if (fabs(det) < kCameraEpsilon) return false;
+    const double inv = 1.0 / det;
+    d.x = (a11 * rhs.x - a01 * rhs.y) * inv;
+    d.y = (-a10 * rhs.x + a00 * rhs.y) * inv;
+    return true;
+}
+
+RTGB_HD float3 unproject_pinhole(const double* p, double px, double py) {
+    const D2 xd{(px - p[2]) / p[0], (py - p[3]) / p[1]};
+    D2 xy = xd;
+    for (int it = 0; it < 24; ++it) {
+        const D2 dist = distort_pinhole(p, xy);
+        const D2 err{xd.x - dist.x, xd.y - dist.y};
+        if (err.x * err.x + err.y * err.y < 1e-20) break;
+        const double x = xy.x, y = xy.y;
+        const double r2 = x * x + y * y, r4 = r2 * r2, r6 = r4 * r2;
+        const double radial = 1.0 + p[4] * r2 + p[5] * r4 + p[6] * r6;
+        const double drdx = 2.0 * x * (p[4] + 2.0 * p[5] * r2 + 3.0 * p[6] * r4);
+        const double drdy = 2.0 * y * (p[4] + 2.0 * p[5] * r2 + 3.0 * p[6] * r4);
+        D2 d{0.0, 0.0};
+        if (!solve2(radial + x * drdx + 6.0 * p[8] * x + 2.0 * p[7] * y, x * drdy + 2.0 * p[7] * x + 2.0 * p[8] * y,
+                y * drdx + 2.0 * p[7] * x + 2.0 * p[8] * y, radial + y * drdy + 6.0 * p[7] * y + 2.0 * p[8] * x, err,
+                d)) {
+            break;
+        }
+        xy.x += d.x;
+        xy.y += d.y;
+    }
+    return normalize(f3(static_cast<float>(xy.x), static_cast<float>(xy.y), 1.0f));
+}
+
+RTGB_HD float2 project_pinhole(const double* p, const float3& dir) {
+    if (fabsf(dir.z) < 1e-7f) return make_float2(-1.0f, -1.0f);
+    const double inv_z = 1.0 / static_cast<double>(dir.z);
+    const D2 xu{static_cast<double>(dir.x) * inv_z, static_cast<double>(dir.y) * inv_z};
+    const D2 xd = distort_pinhole(p, xu);
+    return make_float2(static_cast<float>(xd.x * p[0] + p[2]), static_cast<float>(xd.y * p[1] + p[3]));
+}
+
+RTGB_HD D2 equi_tangential(const D2& xy, const double* t) {
+    const double xr = xy.x, yr = xy.y;
+    const double xr2 = xr * xr, yr2 = yr * yr, xryr = xr * yr;
+    return D2{xr + 2.0 * t[0] * xryr + t[1] * (xr2 + yr2 + 2.0 * xr2), yr + t[0] * (xr2 + yr2 + 2.0 * yr2) + 2.0 * t[1] * xryr};
+}
+
+RTGB_HD D2 remove_equi_tangential(const D2& xy, const double* t) {
+    const D2 dist = equi_tangential(xy, t);
+    D2 d{0.0, 0.0};
+    if (!solve2(1.0 + 2.0 * t[0] * xy.y + 6.0 * t[1] * xy.x, 2.0 * t[0] * xy.x + 2.0 * t[1] * xy.y,
+            2.0 * t[0] * xy.x + 2.0 * t[1] * xy.y, 1.0 + 6.0 * t[0] * xy.y + 2.0 * t[1] * xy.x,
+            D2{xy.x - dist.x, xy.y - dist.y}, d)) {
+        return xy;
+    }
+    return D2{xy.x + d.x, xy.y + d.y};
+}
+
+// Unprojection of one pixel centre for a camera (FP64, computed once per
+// intrinsics change into the camera's direction table).
+RTGB_HD float3 unproject_equi(const double fx, const double fy, const double cx, const double cy, const double* tan2,
+    const double* lut, double lut_step, double px, double py) {
+    const D2 xy{(px - cx) / fx, (py - cy) / fy};
+    if (xy.x * xy.x + xy.y * xy.y < kCameraEpsilon * kCameraEpsilon) return f3(0.0f, 0.0f, 1.0f);
+    const D2 xr = remove_equi_tangential(xy, tan2);
+    const double rd = sqrt(xr.x * xr.x + xr.y * xr.y);
+    if (rd < kCameraEpsilon) return f3(0.0f, 0.0f, 1.0f);
+    double theta = 0.0;
+    bool ok = true;
+    if (rd <= 0.0 || lut_step <= 0.0) {
+        theta = 0.0;
+    } else {
+        const double pos = rd / lut_step;
+        if (pos > 1023.0) {
+            ok = false;
+        } else if (pos >= 1023.0) {
+            theta = lut[1023];
+        } else {
+            const int i = static_cast<int>(pos);
+            const double a = pos - static_cast<double>(i);
+            theta = (1.0 - a) * lut[i] + a * lut[i + 1];
+        }
+    }
+    if (!ok) return normalize(f3(static_cast<float>(xy.x), static_cast<float>(xy.y), 1.0f));
+    const double scale = tan(theta) / rd;
+    return normalize(f3(static_cast<float>(xr.x * scale), static_cast<float>(xr.y * scale), 1.0f));
+}
+
+// invert_lut_theta (programs.cu:435-450): first i with lut[i] <= theta <= lut[i+1].
+// On a non-decreasing LUT that is lower_bound(theta) - 1, found by bisection.
+RTGB_D double invert_lut_theta(const CameraDev& c, double theta) {
+    if (theta <= 0.0 || c.lut_step <= 0.0) return 0.0;
+    if (theta >= c.lut[1023]) return 1023.0 * c.lut_step;
+    if (c.lut_monotone) {
+        int lo = 0, hi = 1024;  // first j with lut[j] >= theta
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (c.lut[mid] < theta) lo = mid + 1;
+            else hi = mid;
+        }
+        const int i = lo - 1;
+        if (i >= 0 && i < 1023) {
+            const double den = c.lut[i + 1] - c.lut[i];
+            const double a = den > 0.0 ? (theta - c.lut[i]) / den : 0.0;
+            return (static_cast<double>(i) + a) * c.lut_step;
+        }
+    }
+    for (int i = 0; i < 1023; ++i) {
+        if (c.lut[i] <= theta && theta <= c.lut[i + 1]) {
+            const double den = c.lut[i + 1] - c.lut[i];
+            const double a = den > 0.0 ? (theta - c.lut[i]) / den : 0.0;
+            return (static_cast<double>(i) + a) * c.lut_step;
+        }
+    }
+    return 1023.0 * c.lut_step;
+}
+
+RTGB_D float2 project_camera(const CameraDev& c, const float3& dir) {
+    if (c.model != RTGB_CAMERA_EQUI62_LUT1D) return project_pinhole(c.pin, dir);
+    const double dx = dir.x, dy = dir.y, dz = dir.z;
+    const double r = sqrt(dx * dx + dy * dy);
+    if (r < kCameraEpsilon) return make_float2(static_cast<float>(c.eq_cx), static_cast<float>(c.eq_cy));
+    const double theta = atan2(r, dz);
+    const double rd = invert_lut_theta(c, theta);
+    const D2 xr{dx / r * rd, dy / r * rd};
+    const D2 xd = equi_tangential(xr, c.eq_tan);
+    return make_float2(static_cast<float>(xd.x * c.eq_fx + c.eq_cx), static_cast<float>(xd.y * c.eq_fy + c.eq_cy));
+}
+
+RTGB_D float3 cam_to_world(const CameraDev& c, const float3& d) {
+    return normalize(add(add(mul(ld3(c.bx_f), d.x), mul(ld3(c.by_f), d.y)), mul(ld3(c.bz_f), d.z)));
+}
+
+// ---- primitive tests (programs.cu:1421-1547) on leaf records -------------------
+
+RTGB_D int prim_code(const PrimRecord& p) { return __float_as_int(p.q[3].w); }
+
+// Sphere: returns the accepted root or -1 (no hit) for (tmin, tmax).
+RTGB_D bool sphere_t(const float3& center, float radius, const float3& o, const float3& d, float tmin, float tmax,
+    float& t) {
+    const float3 oc = sub(o, center);
+    const float a = len_sq(d);
+    const float hb = dot(oc, d);
+    const float c = len_sq(oc) - radius * radius;
+    const float disc = hb * hb - a * c;
+    if (disc <= 0.0f) return false;
+    const float sd = sqrtf(disc);
+    float root = (-hb - sd) / a;
+    if (root <= tmin || root >= tmax) {
+        root = (-hb + sd) / a;
+        if (root <= tmin || root >= tmax) return false;
+    }
+    t = root;
+    return true;
+}
+
+RTGB_D bool quad_t(const float3& origin, const float3& normal, const float3& w, const float3& eu, const float3& ev,
+    const float3& o, const float3& d, float tmin, float tmax, float& t, float& u, float& v) {
+    const float denom = dot(normal, d);
+    if (fabsf(denom) < 1e-6f) return false;
+    const float tt = dot(sub(origin, o), normal) / denom;
+    if (tt <= tmin || tt >= tmax) return false;
+    const float3 p = add(o, mul(d, tt));
+    const float3 rel = sub(p, origin);
+    const float uu = dot(w, cross(rel, ev));
+    const float vv = dot(w, cross(eu, rel));
+    if (uu < 0.0f || uu > 1.0f || vv < 0.0f || vv > 1.0f) return false;
+    t = tt;
+    u = uu;
+    v = vv;
+    return true;
+}
+
+RTGB_D bool triangle_t(const float3& p0, const float3& e1, const float3& e2, const float3& o, const float3& d,
+    float tmin, float tmax, float& t, float& u, float& v) {
+    const float3 pvec = cross(d, e2);
+    const float det = dot(e1, pvec);
+    if (fabsf(det) <= 1e-8f) return false;
+    const float inv = 1.0f / det;
+    const float3 tvec = sub(o, p0);
+    const float uu = dot(tvec, pvec) * inv;
+    if (uu < 0.0f || uu > 1.0f) return false;
+    const float3 qvec = cross(tvec, e1);
+    const float vv = dot(d, qvec) * inv;
+    if (vv < 0.0f || (uu + vv) > 1.0f) return false;
+    const float tt = dot(e2, qvec) * inv;
+    if (tt <= tmin || tt >= tmax) return false;
+    t = tt;
+    u = uu;
+    v = vv;
+    return true;
+}
+
+// Tests one leaf record; on a hit inside (tmin, tmax) returns t.
+RTGB_D bool prim_hit(const PrimRecord& p, const float3& o, const float3& d, float tmin, float tmax, float& t) {
+    const int type = static_cast<unsigned>(prim_code(p)) >> 28;
+    float u, v;
+    if (type == 2) return triangle_t(xyz(p.q[0]), xyz(p.q[1]), xyz(p.q[2]), o, d, tmin, tmax, t, u, v);
+    if (type == 0) return sphere_t(xyz(p.q[0]), p.q[0].w, o, d, tmin, tmax, t);
+    return quad_t(xyz(p.q[0]), f3(p.q[0].w, p.q[1].w, p.q[2].w), xyz(p.q[3]), xyz(p.q[1]), xyz(p.q[2]), o, d, tmin,
+        tmax, t, u, v);
+}
+
+RTGB_D PrimRecord load_prim(const PrimRecord* __restrict__ prims, int slot) {
+    PrimRecord r;
+    const float4* src = reinterpret_cast<const float4*>(prims + slot);
+    r.q[0] = __ldg(src + 0);
+    r.q[1] = __ldg(src + 1);
+    r.q[2] = __ldg(src + 2);
+    r.q[3] = __ldg(src + 3);
+    return r;
+}
+
+// Slab test of one child box; boxes were widened at build time, so the fused
+// form below never rejects a box the exact test accepts.
+RTGB_D bool box_hit(const float3& lo, const float3& hi, const float3& inv, const float3& oinv, float tmin, float tmax,
+    float& tnear) {
+    const float tx0 = __fmaf_rn(lo.x, inv.x, -oinv.x), tx1 = __fmaf_rn(hi.x, inv.x, -oinv.x);
+    const float ty0 = __fmaf_rn(lo.y, inv.y, -oinv.y), ty1 = __fmaf_rn(hi.y, inv.y, -oinv.y);
+    const float tz0 = __fmaf_rn(lo.z, inv.z, -oinv.z), tz1 = __fmaf_rn(hi.z, inv.z, -oinv.z);
+    const float n = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    const float f = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    tnear = n;
+    return n <= f;
+}
+
+struct RayInv {
+    float3 inv, oinv;
+};
+
+RTGB_D RayInv ray_inv(const float3& o, const float3& d) {
+    // Zero direction components get a huge finite reciprocal so slabs stay ordered.
+    auto rcp = [](float x) { return fabsf(x) > 1e-20f ? 1.0f / x : copysignf(1e20f, x); };
+    RayInv r;
+    r.inv = f3(rcp(d.x), rcp(d.y), rcp(d.z));
+    r.oinv = f3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+    return r;
+}
+
+// Closest hit over the scene BVH: strict t < closest like the reference, so
+// equal-t primitives keep the first one traversed. Returns the code or -1.
+// `overflow` counts subtrees dropped by a full stack (never silently).
+RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3& d, float tmin, float& closest,
+    int& overflow) {
+    int best = -1;
+    if (s.prim_count <= 0) return -1;
+    if (s.prim_count == 1) {
+        const PrimRecord p = load_prim(s.prims, 0);
+        float t;
+        if (prim_hit(p, o, d, tmin, closest, t)) {
+            closest = t;
+            best = prim_code(p);
+        }
+        return best;
+    }
+    const RayInv ri = ray_inv(o, d);
+    int stack[kTraversalStack];
+    int sp = 0;
+    int node = 0;
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        const float4* np = reinterpret_cast<const float4*>(s.nodes + node);
+        const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
+        const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
+        float t0, t1;
+        bool h0 = box_hit(xyz(a), xyz(b), ri.inv, ri.oinv, tmin, closest, t0);
+        bool h1 = box_hit(xyz(c), xyz(e), ri.inv, ri.oinv, tmin, closest, t1);
+        if (h0 && c0 < 0) {
+            const PrimRecord p = load_prim(s.prims, ~c0);
+            float t;
+            if (prim_hit(p, o, d, tmin, closest, t)) {
+                closest = t;
+                best = prim_code(p);
+            }
+            h0 = false;
+        }
+        if (h1 && c1 < 0) {
+            const PrimRecord p = load_prim(s.prims, ~c1);
+            float t;
+            if (prim_hit(p, o, d, tmin, closest, t)) {
+                closest = t;
+                best = prim_code(p);
+            }
+            h1 = false;
+        }
+        if (h0 && h1) {
+            const bool first0 = t0 <= t1;
+            if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
+            else ++overflow;
+            node = first0 ? c0 : c1;
+            continue;
+        }
+        if (h0) {
+            node = c0;
+            continue;
+        }
+        if (h1) {
+            node = c1;
+            continue;
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return best;
+}
+
+// Any hit in (tmin, tmax): the reference's occlusion test is a closest-hit
+// query whose `hit` flag alone is used (programs.cu:1759-1762), so the first
+// hit found gives the same answer.
+RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d, float tmin, float tmax, int& overflow) {
+    if (s.prim_count <= 0) return false;
+    if (s.prim_count == 1) {
+        float t;
+        return prim_hit(load_prim(s.prims, 0), o, d, tmin, tmax, t);
+    }
+    const RayInv ri = ray_inv(o, d);
+    int stack[kTraversalStack];
+    int sp = 0;
+    int node = 0;
+    for (int guard = 0; guard < (1 << 24); ++guard) {
+        const float4* np = reinterpret_cast<const float4*>(s.nodes + node);
+        const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
+        const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
+        float t0, t1, t;
+        bool h0 = box_hit(xyz(a), xyz(b), ri.inv, ri.oinv, tmin, tmax, t0);
+        bool h1 = box_hit(xyz(c), xyz(e), ri.inv, ri.oinv, tmin, tmax, t1);
+        if (h0 && c0 < 0) {
+            if (prim_hit(load_prim(s.prims, ~c0), o, d, tmin, tmax, t)) return true;
+            h0 = false;
+        }
+        if (h1 && c1 < 0) {
+            if (prim_hit(load_prim(s.prims, ~c1), o, d, tmin, tmax, t)) return true;
+            h1 = false;
+        }
+        if (h0 && h1) {
+            const bool first0 = t0 <= t1;
+            if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
+            else ++overflow;
+            node = first0 ? c0 : c1;
+            continue;
+        }
+        if (h0) {
+            node = c0;
+            continue;
+        }
+        if (h1) {
+            node = c1;
+            continue;
+        }
+        if (sp == 0) break;
+        node = stack[--sp];
+    }
+    return false;
+}
+
+}  // namespace rtgb

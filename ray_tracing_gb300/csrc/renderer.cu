@@ -1,0 +1,1159 @@
+// Renderer: the C ABI of include/rtgb.h over the wavefront kernels.
+//
+// One handle replaces the reference's RendererPool + one OptixRenderer per
+// camera (src/realtime/gpu/renderer_pool.cpp, optix_renderer.cpp): the scene
+// is uploaded once, every active camera renders in one launch sequence on one
+// stream, frame and history buffers ping-pong instead of being copied
+// (device_frame_buffers.cpp:153-164), and the per-frame sequence is captured
+// once as a CUDA graph and replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lbvh.cuh"
+#include "wavefront.cuh"
+
+namespace rtgb {
+
+// scene_prep: leaf records and padded boxes for every surface primitive
+// (spheres, then quads, then triangles).
+__global__ void k_prim_records(DeviceScene s, PrimRecord* records, float4* aabb_lo, float4* aabb_hi, float pad) {
+    const int n = s.sphere_count + s.quad_count + s.triangle_count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        PrimRecord r;
+        float3 lo, hi;
+        int code;
+        if (i < s.sphere_count) {
+            const rtgb_sphere sp = s.spheres[i];
+            const float3 c = ld3(sp.center);
+            const float rr = fabsf(sp.radius);
+            r.q[0] = make_float4(c.x, c.y, c.z, sp.radius);
+            r.q[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            r.q[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            lo = f3(c.x - rr, c.y - rr, c.z - rr);
+            hi = f3(c.x + rr, c.y + rr, c.z + rr);
+            code = (0 << 28) | i;
+            r.q[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else if (i < s.sphere_count + s.quad_count) {
+            const int k = i - s.sphere_count;
+            const rtgb_quad q = s.quads[k];
+            const float3 o = ld3(q.origin), eu = ld3(q.edge_u), ev = ld3(q.edge_v);
+            const float3 n3 = cross(eu, ev);
+            const float nls = len_sq(n3);
+            float3 normal = f3(0.0f, 0.0f, 0.0f), w = f3(0.0f, 0.0f, 0.0f);
+            if (nls > 1e-12f) {  // degenerate quads keep a zero normal and never hit
+                normal = divs(n3, sqrtf(nls));
+                w = divs(n3, nls);
+            }
+            r.q[0] = make_float4(o.x, o.y, o.z, normal.x);
+            r.q[1] = make_float4(eu.x, eu.y, eu.z, normal.y);
+            r.q[2] = make_float4(ev.x, ev.y, ev.z, normal.z);
+            r.q[3] = make_float4(w.x, w.y, w.z, 0.0f);
+            const float3 p1 = add(o, eu), p2 = add(o, ev), p3 = add(add(o, eu), ev);
+            lo = f3(fminf(fminf(o.x, p1.x), fminf(p2.x, p3.x)), fminf(fminf(o.y, p1.y), fminf(p2.y, p3.y)),
+                fminf(fminf(o.z, p1.z), fminf(p2.z, p3.z)));
+            hi = f3(fmaxf(fmaxf(o.x, p1.x), fmaxf(p2.x, p3.x)), fmaxf(fmaxf(o.y, p1.y), fmaxf(p2.y, p3.y)),
+                fmaxf(fmaxf(o.z, p1.z), fmaxf(p2.z, p3.z)));
+            code = (1 << 28) | k;
+        } else {
+            const int k = i - s.sphere_count - s.quad_count;
+            const rtgb_triangle t = s.triangles[k];
+            const float3 p0 = ld3(t.p0), p1 = ld3(t.p1), p2 = ld3(t.p2);
+            const float3 e1 = sub(p1, p0), e2 = sub(p2, p0);
+            r.q[0] = make_float4(p0.x, p0.y, p0.z, 0.0f);
+            r.q[1] = make_float4(e1.x, e1.y, e1.z, 0.0f);
+            r.q[2] = make_float4(e2.x, e2.y, e2.z, 0.0f);
+            r.q[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            lo = f3(fminf(fminf(p0.x, p1.x), p2.x), fminf(fminf(p0.y, p1.y), p2.y), fminf(fminf(p0.z, p1.z), p2.z));
+            hi = f3(fmaxf(fmaxf(p0.x, p1.x), p2.x), fmaxf(fmaxf(p0.y, p1.y), p2.y), fmaxf(fmaxf(p0.z, p1.z), p2.z));
+            code = (2 << 28) | k;
+        }
+        r.q[3].w = __int_as_float(code);
+        records[i] = r;
+        aabb_lo[i] = make_float4(lo.x - pad, lo.y - pad, lo.z - pad, 0.0f);
+        aabb_hi[i] = make_float4(hi.x + pad, hi.y + pad, hi.z + pad, 0.0f);
+    }
+}
+
+__global__ void k_gather_records(const PrimRecord* __restrict__ in, const int* __restrict__ order, PrimRecord* out,
+    int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = in[order[i]];
+}
+
+void launch_prim_records(const DeviceScene& scene, PrimRecord* records, float4* aabb_lo, float4* aabb_hi, float pad,
+    cudaStream_t stream) {
+    const int n = scene.sphere_count + scene.quad_count + scene.triangle_count;
+    k_prim_records<<<std::min((n + 255) / 256, 8192), 256, 0, stream>>>(scene, records, aabb_lo, aabb_hi, pad);
+}
+
+void launch_gather_records(const PrimRecord* in, const int* order, PrimRecord* out, int n, cudaStream_t stream) {
+    k_gather_records<<<std::min((n + 255) / 256, 8192), 256, 0, stream>>>(in, order, out, n);
+}
+
+namespace {
+
+struct CudaFailure {
+    cudaError_t err;
+    const char* expr;
+};
+
+#define RTGB_CHECK(expr)                                      \
+    do {                                                      \
+        const cudaError_t rtgb_err_ = (expr);                 \
+        if (rtgb_err_ != cudaSuccess) throw CudaFailure{rtgb_err_, #expr}; \
+    } while (0)
+
+struct Invalid {
+    std::string message;
+};
+
+// A device allocation that grows on demand.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void* ensure(size_t need) {
+        if (need <= bytes && p) return p;
+        release();
+        if (need == 0) need = 256;
+        RTGB_CHECK(cudaMalloc(&p, need));
+        bytes = need;
+        return p;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+template <typename T>
+T* upload(DevBuf& buf, const T* host, size_t count, cudaStream_t stream) {
+    buf.ensure(std::max<size_t>(count, 1) * sizeof(T));
+    if (count > 0) RTGB_CHECK(cudaMemcpyAsync(buf.p, host, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return buf.as<T>();
+}
+
+// Per camera slot: device LUT and per-pixel direction table for one set of
+// intrinsics. Two per slot, so the previous frame's camera stays valid while
+// the current one changes.
+struct CameraRes {
+    DevBuf lut;
+    DevBuf dirs;
+    bool valid = false;
+    int width = 0, height = 0, model = 0;
+    rtgb_pinhole32 pinhole{};
+    rtgb_equi62_lut1d equi{};
+    int monotone = 1;
+};
+
+bool same_intrinsics(const CameraRes& r, const rtgb_camera& c) {
+    if (!r.valid || r.width != c.width || r.height != c.height || r.model != c.model) return false;
+    if (c.model == RTGB_CAMERA_PINHOLE32) return std::memcmp(&r.pinhole, &c.pinhole, sizeof(rtgb_pinhole32)) == 0;
+    return std::memcmp(&r.equi, &c.equi, sizeof(rtgb_equi62_lut1d)) == 0;
+}
+
+float luminance(float r, float g, float b) { return std::max(0.0f, 0.2126f * r + 0.7152f * g + 0.0722f * b); }
+
+}  // namespace
+}  // namespace rtgb
+
+using namespace rtgb;
+
+struct rtgb_renderer {
+    int device = 0;
+    bool use_graph = true;
+    bool record = false;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    LaunchShape shapes[6]{};
+    std::string error;
+
+    // scene
+    bool prepared = false;
+    DeviceScene scene{};
+    DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
+        triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
+        sorted_keys, sorted_vals;
+    int prim_count = 0;
+    int analytic_bvh_count = 0;
+    float build_ms = 0.0f;
+
+    // frame state
+    uint32_t sample_stream = 0;
+    CameraRes cam_res[RTGB_MAX_CAMERAS][2];
+    int cam_cur[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    CameraDev prev[RTGB_MAX_CAMERAS]{};
+    int prev_valid[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int history_length[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int layout_w[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int layout_h[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int layout_count = 0;
+    long long total_pixels = 0;
+    long long total_paths = 0;
+    DevBuf frame_mem[2];
+    FrameBufs frames[2]{};
+    int cur = 0;
+    int last = -1;  // frame index holding the last rendered frame
+    long long last_pixel_offset[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int last_w[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int last_h[RTGB_MAX_CAMERAS] = {0, 0, 0, 0};
+    int last_count = 0;
+    int last_spp = 1;
+    int last_bounces = 1;
+    DevBuf path_mem;
+    long long path_capacity = 0;
+    int path_record_bounces = 0;
+    Paths paths{};
+    DevBuf counters_mem, fp_mem, debug_rgba;
+    Counters* d_counters = nullptr;
+    Counters* h_counters = nullptr;  // pinned
+    FrameParams* d_fp = nullptr;
+    FrameParams h_fp{};
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    // graph
+    cudaGraphExec_t graph_exec = nullptr;
+    long long graph_key[4] = {-1, -1, -1, -1};
+
+    void fail_cuda(const CudaFailure& f) {
+        error = std::string("CUDA failure at ") + f.expr + ": " + cudaGetErrorString(f.err);
+    }
+
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+        graph_key[0] = -1;
+    }
+
+    ~rtgb_renderer() {
+        if (stream) cudaStreamSynchronize(stream);
+        drop_graph();
+        DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
+            &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
+            &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
+            &counters_mem, &fp_mem, &debug_rgba};
+        for (DevBuf* b : bufs) b->release();
+        for (auto& slot : cam_res) {
+            for (auto& r : slot) {
+                r.lut.release();
+                r.dirs.release();
+            }
+        }
+        if (h_counters) cudaFreeHost(h_counters);
+        if (ev_start) cudaEventDestroy(ev_start);
+        if (ev_stop) cudaEventDestroy(ev_stop);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void init(const rtgb_create_info& info) {
+        device = info.device;
+        use_graph = info.use_cuda_graph != 0;
+        record = info.debug_path_records != 0;
+        RTGB_CHECK(cudaSetDevice(device));
+        RTGB_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        RTGB_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+        query_launch_shapes(sm_count, shapes);
+        RTGB_CHECK(cudaGetLastError());
+        d_counters = static_cast<Counters*>(counters_mem.ensure(sizeof(Counters)));
+        RTGB_CHECK(cudaMemsetAsync(d_counters, 0, sizeof(Counters), stream));
+        d_fp = static_cast<FrameParams*>(fp_mem.ensure(sizeof(FrameParams)));
+        RTGB_CHECK(cudaMallocHost(reinterpret_cast<void**>(&h_counters), sizeof(Counters)));
+        std::memset(h_counters, 0, sizeof(Counters));
+        RTGB_CHECK(cudaEventCreate(&ev_start));
+        RTGB_CHECK(cudaEventCreate(&ev_stop));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    // ---- scene: packed_scene_preparation.cpp:191-348 + device LBVH --------------
+
+    std::vector<float> scene_texels_;
+
+    float average_texture_lum_r(const rtgb_scene& s, int index, int depth, float out[3]) const {
+        out[0] = out[1] = out[2] = 0.0f;
+        if (index < 0 || index >= s.texture_count || depth >= 8) return 0.0f;
+        const rtgb_texture& t = s.textures[index];
+        if (t.type == 0) {
+            for (int k = 0; k < 3; ++k) out[k] = std::max(t.color[k], 0.0f);
+        } else if (t.type == 1) {
+            float e[3], o[3];
+            average_texture_lum_r(s, t.even_texture, depth + 1, e);
+            average_texture_lum_r(s, t.odd_texture, depth + 1, o);
+            for (int k = 0; k < 3; ++k) out[k] = 0.5f * (e[k] + o[k]);
+        } else if (t.type == 2 && t.image_width > 0 && t.image_height > 0) {
+            const int count = t.image_width * t.image_height;
+            if (t.image_offset < 0 || t.image_offset + count > s.image_texel_count) return 0.0f;
+            float sum[3] = {0.0f, 0.0f, 0.0f};
+            for (int i = 0; i < count; ++i)
+                for (int k = 0; k < 3; ++k) sum[k] += s.image_texels[3 * static_cast<size_t>(t.image_offset + i) + k];
+            for (int k = 0; k < 3; ++k) out[k] = std::max(sum[k] / static_cast<float>(count), 0.0f);
+        } else if (t.type == 3) {
+            out[0] = out[1] = out[2] = 0.5f;
+        }
+        return 0.0f;
+    }
+
+    float emission_lum(const rtgb_scene& s, int mi) const {
+        if (mi < 0 || mi >= s.material_count) return 0.0f;
+        const rtgb_material& m = s.materials[mi];
+        if (m.type != 3) return 0.0f;
+        float c[3];
+        average_texture_lum_r(s, m.emission_texture, 0, c);
+        return luminance(c[0], c[1], c[2]);
+    }
+
+    void validate_scene(const rtgb_scene& s) {
+        auto check = [&](const void* p, int n, const char* what) {
+            if (n < 0 || (n > 0 && p == nullptr)) throw Invalid{std::string("scene ") + what + " array is invalid"};
+        };
+        check(s.textures, s.texture_count, "texture");
+        check(s.image_texels, s.image_texel_count, "image texel");
+        check(s.materials, s.material_count, "material");
+        check(s.spheres, s.sphere_count, "sphere");
+        check(s.quads, s.quad_count, "quad");
+        check(s.triangles, s.triangle_count, "triangle");
+        check(s.media, s.medium_count, "medium");
+        check(s.analytic_lights, s.analytic_light_count, "analytic light");
+        const long long surfaces = static_cast<long long>(s.sphere_count) + s.quad_count + s.triangle_count;
+        if (surfaces == 0) throw Invalid{"render_radiance requires at least one surface primitive"};
+        if (surfaces >= (1ll << 28)) throw Invalid{"scene exceeds 2^28 surface primitives"};
+    }
+
+    void prepare(const rtgb_scene& s) {
+        validate_scene(s);
+        RTGB_CHECK(cudaSetDevice(device));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        drop_graph();
+        prepared = false;
+        DeviceScene d{};
+        d.spheres = upload(spheres, s.spheres, static_cast<size_t>(s.sphere_count), stream);
+        d.quads = upload(quads, s.quads, static_cast<size_t>(s.quad_count), stream);
+        d.triangles = upload(triangles, s.triangles, static_cast<size_t>(s.triangle_count), stream);
+        d.media = upload(media, s.media, static_cast<size_t>(s.medium_count), stream);
+        d.materials = upload(materials, s.materials, static_cast<size_t>(s.material_count), stream);
+        d.textures = upload(textures, s.textures, static_cast<size_t>(s.texture_count), stream);
+        d.texels = s.image_texel_count > 0 ? upload(texels, s.image_texels, 3 * static_cast<size_t>(s.image_texel_count), stream) : nullptr;
+        d.sphere_count = s.sphere_count;
+        d.quad_count = s.quad_count;
+        d.triangle_count = s.triangle_count;
+        d.medium_count = s.medium_count;
+        d.material_count = s.material_count;
+        d.texture_count = s.texture_count;
+        d.texel_count = s.image_texel_count;
+        std::memcpy(d.background, s.background, sizeof d.background);
+
+        // build_light_distribution (packed_scene_preparation.cpp:265-302)
+        std::vector<PackedLight> L;
+        std::vector<int> sl(static_cast<size_t>(s.sphere_count), -1), ql(static_cast<size_t>(s.quad_count), -1),
+            tl(static_cast<size_t>(s.triangle_count), -1);
+        auto append = [&](int type, int index, float w) {
+            if (!std::isfinite(w) || w <= 1e-12f) return;
+            L.push_back(PackedLight{type, index, w, 0.0f});
+        };
+        constexpr float kPiF = 3.14159265358979323846f;
+        for (int i = 0; i < s.sphere_count; ++i) {
+            const rtgb_sphere& sp = s.spheres[i];
+            append(0, i, 4.0f * kPiF * sp.radius * sp.radius * emission_lum(s, sp.material_index));
+        }
+        for (int i = 0; i < s.quad_count; ++i) {
+            const rtgb_quad& q = s.quads[i];
+            const float cx = q.edge_u[1] * q.edge_v[2] - q.edge_u[2] * q.edge_v[1];
+            const float cy = q.edge_u[2] * q.edge_v[0] - q.edge_u[0] * q.edge_v[2];
+            const float cz = q.edge_u[0] * q.edge_v[1] - q.edge_u[1] * q.edge_v[0];
+            append(1, i, std::sqrt(cx * cx + cy * cy + cz * cz) * emission_lum(s, q.material_index));
+        }
+        for (int i = 0; i < s.triangle_count; ++i) {
+            const rtgb_triangle& t = s.triangles[i];
+            const float ax = t.p1[0] - t.p0[0], ay = t.p1[1] - t.p0[1], az = t.p1[2] - t.p0[2];
+            const float bx = t.p2[0] - t.p0[0], by = t.p2[1] - t.p0[1], bz = t.p2[2] - t.p0[2];
+            const float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
+            append(2, i, 0.5f * std::sqrt(cx * cx + cy * cy + cz * cz) * emission_lum(s, t.material_index));
+        }
+        append(3, -1, 4.0f * kPiF * luminance(s.background[0], s.background[1], s.background[2]));
+        float total = 0.0f;
+        for (const PackedLight& l : L) total += l.selection_pdf;
+        float cdf = 0.0f;
+        for (PackedLight& l : L) {
+            l.selection_pdf /= total;
+            cdf += l.selection_pdf;
+            l.cdf = cdf;
+        }
+        if (!L.empty()) L.back().cdf = 1.0f;
+        std::vector<float> lcdf(L.size());
+        d.environment_light = -1;
+        for (size_t i = 0; i < L.size(); ++i) {
+            lcdf[i] = L[i].cdf;
+            const int idx = L[i].primitive_index;
+            // find_packed_light returns the first match; a primitive appears once.
+            if (L[i].type == 0) sl[static_cast<size_t>(idx)] = static_cast<int>(i);
+            else if (L[i].type == 1) ql[static_cast<size_t>(idx)] = static_cast<int>(i);
+            else if (L[i].type == 2) tl[static_cast<size_t>(idx)] = static_cast<int>(i);
+            else if (d.environment_light < 0) d.environment_light = static_cast<int>(i);
+        }
+        d.lights = upload(lights, L.data(), L.size(), stream);
+        d.light_cdf = upload(light_cdf, lcdf.data(), lcdf.size(), stream);
+        d.light_count = static_cast<int>(L.size());
+        d.sphere_light = upload(sphere_light, sl.data(), sl.size(), stream);
+        d.quad_light = upload(quad_light, ql.data(), ql.size(), stream);
+        d.triangle_light = upload(triangle_light, tl.data(), tl.size(), stream);
+
+        // analytic lights: CDF array, infinite list and a BVH over finite ones
+        const int na = s.analytic_light_count;
+        d.analytic = upload(analytic, s.analytic_lights, static_cast<size_t>(na), stream);
+        d.analytic_count = na;
+        std::vector<float> acdf(static_cast<size_t>(na));
+        std::vector<int> inf, finite;
+        for (int i = 0; i < na; ++i) {
+            const rtgb_analytic_light& l = s.analytic_lights[i];
+            acdf[static_cast<size_t>(i)] = l.cdf;
+            if (l.type == 4 || l.type == 5) inf.push_back(i);
+            if ((l.type >= 0 && l.type <= 3) && l.treat_as_point == 0) finite.push_back(i);
+        }
+        d.analytic_cdf = upload(analytic_cdf, acdf.data(), acdf.size(), stream);
+        d.infinite_analytic = upload(infinite_analytic, inf.data(), inf.size(), stream);
+        d.infinite_analytic_count = static_cast<int>(inf.size());
+
+        cudaEvent_t b0, b1;
+        RTGB_CHECK(cudaEventCreate(&b0));
+        RTGB_CHECK(cudaEventCreate(&b1));
+        RTGB_CHECK(cudaEventRecord(b0, stream));
+
+        // scene LBVH
+        const int n = s.sphere_count + s.quad_count + s.triangle_count;
+        float scale = 0.0f;
+        for (int i = 0; i < s.sphere_count; ++i)
+            for (int k = 0; k < 3; ++k) scale = std::max(scale, std::fabs(s.spheres[i].center[k]) + std::fabs(s.spheres[i].radius));
+        for (int i = 0; i < s.quad_count; ++i)
+            for (int k = 0; k < 3; ++k)
+                scale = std::max(scale, std::fabs(s.quads[i].origin[k]) + std::fabs(s.quads[i].edge_u[k]) + std::fabs(s.quads[i].edge_v[k]));
+        for (int i = 0; i < s.triangle_count; ++i)
+            for (int k = 0; k < 3; ++k)
+                scale = std::max({scale, std::fabs(s.triangles[i].p0[k]), std::fabs(s.triangles[i].p1[k]), std::fabs(s.triangles[i].p2[k])});
+        const float pad = 1e-5f + 1e-5f * scale;
+        d.prim_count = n;
+        prim_count = n;
+        DevBuf scratch, unsorted;
+        unsorted.ensure(static_cast<size_t>(n) * sizeof(PrimRecord));
+        scratch.ensure(lbvh_scratch_bytes(n));
+        LbvhScratch ls = lbvh_carve(scratch.p, n);
+        PrimRecord* recs = static_cast<PrimRecord*>(prims.ensure(static_cast<size_t>(n) * sizeof(PrimRecord)));
+        launch_prim_records(d, unsorted.as<PrimRecord>(), ls.aabb_lo, ls.aabb_hi, pad, stream);
+        RTGB_CHECK(cudaGetLastError());
+        if (n >= 2) {
+            BvhNode* nd = static_cast<BvhNode*>(nodes.ensure(static_cast<size_t>(n - 1) * sizeof(BvhNode)));
+            int* svals = nullptr;
+            uint32_t* skeys = nullptr;
+            RTGB_CHECK(lbvh_build(ls, n, nd, &svals, &skeys, stream));
+            launch_gather_records(unsorted.as<PrimRecord>(), svals, recs, n, stream);
+            RTGB_CHECK(cudaGetLastError());
+            sorted_keys.ensure(static_cast<size_t>(n) * sizeof(uint32_t));
+            sorted_vals.ensure(static_cast<size_t>(n) * sizeof(int));
+            RTGB_CHECK(cudaMemcpyAsync(sorted_keys.p, skeys, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToDevice, stream));
+            RTGB_CHECK(cudaMemcpyAsync(sorted_vals.p, svals, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToDevice, stream));
+            d.nodes = nd;
+            d.node_count = n - 1;
+        } else {
+            RTGB_CHECK(cudaMemcpyAsync(recs, unsorted.p, sizeof(PrimRecord), cudaMemcpyDeviceToDevice, stream));
+            d.nodes = nullptr;
+            d.node_count = 0;
+        }
+        d.prims = recs;
+
+        // analytic-light BVH (host boxes, device build)
+        const int nf = static_cast<int>(finite.size());
+        d.analytic_bvh_count = nf;
+        analytic_bvh_count = nf;
+        d.analytic_nodes = nullptr;
+        d.analytic_node_count = 0;
+        if (nf > 0) {
+            std::vector<float4> lo(static_cast<size_t>(nf)), hi(static_cast<size_t>(nf));
+            float lscale = 0.0f;
+            for (int k = 0; k < nf; ++k) {
+                const rtgb_analytic_light& l = s.analytic_lights[finite[static_cast<size_t>(k)]];
+                float e[3];
+                const float bxl = std::sqrt(l.basis_x[0] * l.basis_x[0] + l.basis_x[1] * l.basis_x[1] + l.basis_x[2] * l.basis_x[2]);
+                for (int a = 0; a < 3; ++a) {
+                    const float bx = std::fabs(l.basis_x[a]), by = std::fabs(l.basis_y[a]), bz = std::fabs(l.basis_z[a]);
+                    if (l.type == 0) e[a] = std::fabs(l.radius) * bxl;
+                    else if (l.type == 1) e[a] = std::fabs(l.radius) * (bx + by);
+                    else if (l.type == 2) e[a] = 0.5f * (std::fabs(l.width) * bx + std::fabs(l.height) * by);
+                    else e[a] = std::fabs(l.radius) * (bx + by) + 0.5f * std::fabs(l.length) * bz;
+                    lscale = std::max(lscale, std::fabs(l.position[a]) + e[a]);
+                }
+                lo[static_cast<size_t>(k)] = make_float4(l.position[0] - e[0], l.position[1] - e[1], l.position[2] - e[2], 0.0f);
+                hi[static_cast<size_t>(k)] = make_float4(l.position[0] + e[0], l.position[1] + e[1], l.position[2] + e[2], 0.0f);
+            }
+            const float lpad = 1e-5f + 1e-5f * lscale;
+            for (int k = 0; k < nf; ++k) {
+                lo[static_cast<size_t>(k)].x -= lpad; lo[static_cast<size_t>(k)].y -= lpad; lo[static_cast<size_t>(k)].z -= lpad;
+                hi[static_cast<size_t>(k)].x += lpad; hi[static_cast<size_t>(k)].y += lpad; hi[static_cast<size_t>(k)].z += lpad;
+            }
+            std::vector<int> leaf(static_cast<size_t>(nf));
+            if (nf >= 2) {
+                DevBuf ascratch;
+                ascratch.ensure(lbvh_scratch_bytes(nf));
+                LbvhScratch as = lbvh_carve(ascratch.p, nf);
+                RTGB_CHECK(cudaMemcpyAsync(as.aabb_lo, lo.data(), lo.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
+                RTGB_CHECK(cudaMemcpyAsync(as.aabb_hi, hi.data(), hi.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
+                BvhNode* an = static_cast<BvhNode*>(analytic_nodes.ensure(static_cast<size_t>(nf - 1) * sizeof(BvhNode)));
+                int* svals = nullptr;
+                uint32_t* skeys = nullptr;
+                RTGB_CHECK(lbvh_build(as, nf, an, &svals, &skeys, stream));
+                std::vector<int> order(static_cast<size_t>(nf));
+                RTGB_CHECK(cudaMemcpyAsync(order.data(), svals, order.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
+                RTGB_CHECK(cudaStreamSynchronize(stream));
+                ascratch.release();
+                for (int k = 0; k < nf; ++k) leaf[static_cast<size_t>(k)] = finite[static_cast<size_t>(order[static_cast<size_t>(k)])];
+                d.analytic_nodes = an;
+                d.analytic_node_count = nf - 1;
+            } else {
+                leaf[0] = finite[0];
+            }
+            d.analytic_leaf = upload(analytic_leaf, leaf.data(), leaf.size(), stream);
+        } else {
+            d.analytic_leaf = nullptr;
+        }
+        RTGB_CHECK(cudaEventRecord(b1, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        RTGB_CHECK(cudaGetLastError());
+        RTGB_CHECK(cudaEventElapsedTime(&build_ms, b0, b1));
+        cudaEventDestroy(b0);
+        cudaEventDestroy(b1);
+        scratch.release();
+        unsorted.release();
+        scene = d;
+        prepared = true;
+        // use_prepared_scene: the sample stream restarts and history is dropped
+        sample_stream = 0;
+        reset_accumulation();
+        std::memset(h_counters, 0, sizeof(Counters));
+        RTGB_CHECK(cudaMemsetAsync(d_counters, 0, sizeof(Counters), stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    void reset_accumulation() {
+        for (int c = 0; c < RTGB_MAX_CAMERAS; ++c) {
+            history_length[c] = 0;
+            prev_valid[c] = 0;
+        }
+    }
+
+    // ---- frames -------------------------------------------------------------
+
+    void validate_request(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active) {
+        // validate_render_pool_request (render_request_validation.cpp)
+        if (rig.active_count < 1 || rig.active_count > RTGB_MAX_CAMERAS) throw Invalid{"render_frame rig.active_count out of range"};
+        if (active < 1 || active > RTGB_MAX_CAMERAS) throw Invalid{"render_frame active_cameras out of range"};
+        if (active > rig.active_count) throw Invalid{"render_frame active_cameras exceeds rig.active_count"};
+        for (int c = 0; c < active; ++c) {
+            const rtgb_camera& cam = rig.cameras[c];
+            if (cam.enabled == 0) throw Invalid{"render_frame leading camera slot disabled at index " + std::to_string(c)};
+            if (cam.width <= 0 || cam.height <= 0) throw Invalid{"render_frame leading camera slot has invalid resolution at index " + std::to_string(c)};
+            if (cam.model != RTGB_CAMERA_PINHOLE32 && cam.model != RTGB_CAMERA_EQUI62_LUT1D) throw Invalid{"render_frame unknown camera model"};
+            if (cam.model == RTGB_CAMERA_PINHOLE32 && (cam.pinhole.fx == 0.0 || cam.pinhole.fy == 0.0)) throw Invalid{"pinhole32 focal length is zero"};
+            if (cam.model == RTGB_CAMERA_EQUI62_LUT1D && (cam.equi.fx == 0.0 || cam.equi.fy == 0.0)) throw Invalid{"equi62_lut1d focal length is zero"};
+        }
+        if (profile.samples_per_pixel > 4096 || profile.max_bounces > 64) throw Invalid{"render profile exceeds spp 4096 / 64 bounces"};
+    }
+
+    void ensure_frames(long long pixels) {
+        // beauty, normal, dnormal, albedo float4; depth, trust float; flow float2; reservoir 84 B
+        const size_t per = 4 * 16 + 4 + 4 + 8 + sizeof(Reservoir);
+        for (int f = 0; f < 2; ++f) {
+            if (frame_mem[f].bytes >= static_cast<size_t>(pixels) * per + 2048 && frame_mem[f].p) continue;
+            drop_graph();
+            char* p = static_cast<char*>(frame_mem[f].ensure(static_cast<size_t>(pixels) * per + 2048));
+            auto take = [&](size_t bytes) {
+                char* r = p;
+                p += (bytes + 255) & ~size_t(255);
+                return r;
+            };
+            FrameBufs& b = frames[f];
+            b.beauty = reinterpret_cast<float4*>(take(pixels * 16));
+            b.normal = reinterpret_cast<float4*>(take(pixels * 16));
+            b.dnormal = reinterpret_cast<float4*>(take(pixels * 16));
+            b.albedo = reinterpret_cast<float4*>(take(pixels * 16));
+            b.depth = reinterpret_cast<float*>(take(pixels * 4));
+            b.flow = reinterpret_cast<float2*>(take(pixels * 8));
+            b.trust = reinterpret_cast<float*>(take(pixels * 4));
+            b.reservoirs = reinterpret_cast<Reservoir*>(take(pixels * sizeof(Reservoir)));
+        }
+    }
+
+    void ensure_paths(long long n, int spp, int bounces) {
+        const bool need_records = record;
+        if (n <= path_capacity && (!need_records || path_record_bounces >= bounces) && path_mem.p) return;
+        drop_graph();
+        const size_t align = 256;
+        auto sz = [&](size_t b) { return (b + align - 1) & ~(align - 1); };
+        const size_t f4 = sz(static_cast<size_t>(n) * 16), i1 = sz(static_cast<size_t>(n) * 4), i2 = sz(static_cast<size_t>(n) * 8);
+        size_t total = f4 * 15 + i2 + i1 * 5;
+        const bool scratch = true;
+        if (scratch) total += sz(static_cast<size_t>(n) * sizeof(Reservoir));
+        if (need_records) total += sz(static_cast<size_t>(n) * 4 * bounces);
+        char* p = static_cast<char*>(path_mem.ensure(total));
+        auto take = [&](size_t b) {
+            char* r = p;
+            p += b;
+            return r;
+        };
+        Paths P{};
+        P.ray_o = reinterpret_cast<float4*>(take(f4));
+        P.ray_d = reinterpret_cast<float4*>(take(f4));
+        P.thr = reinterpret_cast<float4*>(take(f4));
+        P.rad = reinterpret_cast<float4*>(take(f4));
+        P.prev_pos = reinterpret_cast<float4*>(take(f4));
+        P.prev_nrm = reinterpret_cast<float4*>(take(f4));
+        P.aux_n = reinterpret_cast<float4*>(take(f4));
+        P.aux_a = reinterpret_cast<float4*>(take(f4));
+        P.hit = reinterpret_cast<float4*>(take(f4));
+        for (int k = 0; k < 2; ++k) {
+            P.sh_o[k] = reinterpret_cast<float4*>(take(f4));
+            P.sh_d[k] = reinterpret_cast<float4*>(take(f4));
+            P.sh_c[k] = reinterpret_cast<float4*>(take(f4));
+        }
+        P.prev_prim = reinterpret_cast<int2*>(take(i2));
+        P.rng = reinterpret_cast<uint32_t*>(take(i1));
+        P.queue[0] = reinterpret_cast<int*>(take(i1));
+        P.queue[1] = reinterpret_cast<int*>(take(i1));
+        P.shadow_queue = reinterpret_cast<int*>(take(i1));
+        P.res_written = reinterpret_cast<int*>(take(i1));
+        P.res_scratch = reinterpret_cast<Reservoir*>(take(sz(static_cast<size_t>(n) * sizeof(Reservoir))));
+        P.codes = need_records ? reinterpret_cast<int*>(take(sz(static_cast<size_t>(n) * 4 * bounces))) : nullptr;
+        paths = P;
+        path_capacity = n;
+        path_record_bounces = need_records ? bounces : 0;
+        (void)spp;
+    }
+
+    // Binds a slot's device LUT and direction table for these intrinsics;
+    // returns true when the table has to be (re)computed.
+    bool bind_camera(int slot, const rtgb_camera& c, CameraDev& d) {
+        CameraRes* res = &cam_res[slot][cam_cur[slot]];
+        bool fresh = false;
+        if (!same_intrinsics(*res, c)) {
+            cam_cur[slot] ^= 1;
+            res = &cam_res[slot][cam_cur[slot]];
+            res->valid = true;
+            res->width = c.width;
+            res->height = c.height;
+            res->model = c.model;
+            res->pinhole = c.pinhole;
+            res->equi = c.equi;
+            res->monotone = 1;
+            for (int i = 0; i + 1 < RTGB_EQUI_LUT_SIZE; ++i) {
+                if (!(c.equi.lut[i] <= c.equi.lut[i + 1])) res->monotone = 0;
+            }
+            upload(res->lut, c.equi.lut, RTGB_EQUI_LUT_SIZE, stream);
+            res->dirs.ensure(static_cast<size_t>(c.width) * c.height * sizeof(float4));
+            fresh = true;
+        }
+        d.lut_monotone = res->monotone;
+        d.lut = res->lut.as<double>();
+        d.dirs = res->dirs.as<float4>();
+        return fresh;
+    }
+
+    // make_device_active_camera (radiance_launch_setup.cpp:19-64)
+    static CameraDev camera_dev(const rtgb_camera& c, long long pixel_offset, long long path_offset) {
+        CameraDev d{};
+        d.width = c.width;
+        d.height = c.height;
+        d.model = c.model;
+        d.pixel_offset = pixel_offset;
+        d.path_offset = path_offset;
+        for (int r = 0; r < 3; ++r) {
+            d.origin[r] = c.translation[r];
+            d.bx[r] = c.rotation[r * 3 + 0];
+            d.by[r] = c.rotation[r * 3 + 1];
+            d.bz[r] = c.rotation[r * 3 + 2];
+            d.origin_f[r] = static_cast<float>(d.origin[r]);
+            d.bx_f[r] = static_cast<float>(d.bx[r]);
+            d.by_f[r] = static_cast<float>(d.by[r]);
+            d.bz_f[r] = static_cast<float>(d.bz[r]);
+        }
+        const rtgb_pinhole32& ph = c.pinhole;
+        const double pin[9] = {ph.fx, ph.fy, ph.cx, ph.cy, ph.k1, ph.k2, ph.k3, ph.p1, ph.p2};
+        std::memcpy(d.pin, pin, sizeof pin);
+        d.eq_fx = c.equi.fx;
+        d.eq_fy = c.equi.fy;
+        d.eq_cx = c.equi.cx;
+        d.eq_cy = c.equi.cy;
+        d.eq_tan[0] = c.equi.tangential[0];
+        d.eq_tan[1] = c.equi.tangential[1];
+        d.lut_step = c.equi.lut_step;
+        d.lut_monotone = 1;
+        return d;
+    }
+
+    void enqueue_frame_kernels() {
+        launch_raygen(d_fp, paths, d_counters, shapes[0], stream);
+        for (int b = 0; b < h_fp.max_bounces; ++b) {
+            launch_trace(d_fp, scene, paths, d_counters, b, shapes[1], stream);
+            launch_reset_counters(d_counters, b, stream);
+            launch_shade(d_fp, scene, paths, d_counters, b, shapes[2], stream);
+            launch_shadow(scene, paths, d_counters, shapes[3], stream);
+        }
+        launch_finalize(d_fp, paths, d_counters, shapes[4], stream);
+        launch_resolve(d_fp, shapes[5], stream);
+    }
+
+    int render(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active, bool sync,
+        rtgb_frame_views* out) {
+        if (!prepared) {
+            error = "render_frame requires prepare_scene() first";
+            return RTGB_NOT_PREPARED;
+        }
+        validate_request(rig, profile, active);
+        RTGB_CHECK(cudaSetDevice(device));
+        const int spp = profile.samples_per_pixel > 0 ? profile.samples_per_pixel : 1;
+        const int mb = profile.max_bounces > 0 ? profile.max_bounces : 1;
+        // layout: cameras back to back; a change of any resolution drops history
+        bool layout_changed = active != layout_count;
+        for (int c = 0; c < active; ++c) layout_changed |= rig.cameras[c].width != layout_w[c] || rig.cameras[c].height != layout_h[c];
+        long long pixels = 0;
+        long long offsets[RTGB_MAX_CAMERAS];
+        for (int c = 0; c < active; ++c) {
+            offsets[c] = pixels;
+            pixels += static_cast<long long>(rig.cameras[c].width) * rig.cameras[c].height;
+        }
+        if (pixels * spp >= (1ll << 31)) throw Invalid{"frame exceeds 2^31 paths"};
+        if (layout_changed) {
+            // resize_history -> reset_history (device_frame_buffers.cpp:80-98)
+            for (int c = 0; c < RTGB_MAX_CAMERAS; ++c) {
+                history_length[c] = 0;
+                prev_valid[c] = 0;
+                layout_w[c] = c < active ? rig.cameras[c].width : 0;
+                layout_h[c] = c < active ? rig.cameras[c].height : 0;
+            }
+            layout_count = active;
+        }
+        total_pixels = pixels;
+        total_paths = pixels * spp;
+        ensure_frames(pixels);
+        ensure_paths(total_paths, spp, mb);
+
+        FrameParams& fp = h_fp;
+        std::memset(&fp, 0, sizeof fp);
+        for (int c = 0; c < active; ++c) {
+            fp.cam[c] = camera_dev(rig.cameras[c], offsets[c], offsets[c] * spp);
+            if (bind_camera(c, rig.cameras[c], fp.cam[c])) {
+                launch_camera_dirs(fp.cam[c], const_cast<float4*>(fp.cam[c].dirs), stream);
+            }
+            fp.prev[c] = prev[c];
+            fp.prev_valid[c] = prev_valid[c];
+            fp.history_length[c] = history_length[c];
+        }
+        RTGB_CHECK(cudaGetLastError());
+        fp.cam_count = active;
+        fp.spp = spp;
+        fp.max_bounces = mb;
+        fp.rr_start = profile.rr_start_bounce;
+        fp.total_pixels = total_pixels;
+        fp.total_paths = total_paths;
+        fp.stream = sample_stream;
+        const int min_lights = profile.restir_min_analytic_lights > 0 ? profile.restir_min_analytic_lights : 1;
+        fp.restir_enabled = profile.enable_restir_di != 0 && scene.analytic_count >= min_lights ? 1 : 0;
+        fp.restir_candidates = profile.restir_initial_candidates;
+        fp.restir_temporal = profile.restir_temporal_reuse;
+        fp.restir_max_age = profile.restir_max_history_age;
+        fp.restir_max_temporal = profile.restir_max_temporal_candidates;
+        fp.restir_spatial = profile.restir_spatial_neighbors;
+        fp.restir_max_spatial = profile.restir_max_spatial_candidates;
+        fp.restir_bias = profile.restir_bias_correction;
+        fp.record_paths = record ? 1 : 0;
+        fp.cur = frames[cur];
+        fp.hist = frames[cur ^ 1];
+        // Pageable source: the copy is staged before the call returns, so the
+        // host struct can be rewritten for the next frame immediately.
+        RTGB_CHECK(cudaMemcpyAsync(d_fp, &fp, sizeof fp, cudaMemcpyHostToDevice, stream));
+
+        RTGB_CHECK(cudaEventRecord(ev_start, stream));
+        const long long key[4] = {total_paths, mb, static_cast<long long>(paths.ray_o != nullptr), reinterpret_cast<long long>(scene.prims)};
+        if (use_graph) {
+            if (!graph_exec || std::memcmp(key, graph_key, sizeof key) != 0) {
+                drop_graph();
+                cudaGraph_t graph;
+                RTGB_CHECK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_frame_kernels();
+                RTGB_CHECK(cudaStreamEndCapture(stream, &graph));
+                const cudaError_t inst = cudaGraphInstantiate(&graph_exec, graph, 0);
+                cudaGraphDestroy(graph);
+                RTGB_CHECK(inst);
+                std::memcpy(graph_key, key, sizeof key);
+            }
+            RTGB_CHECK(cudaGraphLaunch(graph_exec, stream));
+        } else {
+            enqueue_frame_kernels();
+        }
+        RTGB_CHECK(cudaGetLastError());
+        RTGB_CHECK(cudaEventRecord(ev_stop, stream));
+        RTGB_CHECK(cudaMemcpyAsync(h_counters, d_counters, sizeof(Counters), cudaMemcpyDeviceToHost, stream));
+
+        // capture_launch_history (radiance_launch_setup.cpp:122-136); the
+        // frame buffers swap instead of copying into history.
+        for (int c = 0; c < active; ++c) {
+            prev[c] = fp.cam[c];
+            prev_valid[c] = 1;
+            history_length[c] = history_length[c] == 0 ? 1 : history_length[c] + 1;
+            last_pixel_offset[c] = offsets[c];
+            last_w[c] = rig.cameras[c].width;
+            last_h[c] = rig.cameras[c].height;
+        }
+        last_count = active;
+        last_spp = spp;
+        last_bounces = mb;
+        last = cur;
+        cur ^= 1;
+        const uint32_t used_stream = sample_stream++;
+        if (out) {
+            std::memset(out, 0, sizeof *out);
+            out->camera_count = active;
+            out->sample_stream = used_stream;
+            for (int c = 0; c < active; ++c) fill_view(c, out->cameras[c]);
+        }
+        if (sync) {
+            RTGB_CHECK(cudaStreamSynchronize(stream));
+            if (out) fill_stats(out);
+            if (h_counters->error != 0) {
+                error = "device reported " + std::to_string(h_counters->error) + " inconsistent hit records";
+                return RTGB_DEVICE_FAULT_FLAG;
+            }
+        }
+        return RTGB_OK;
+    }
+
+    void fill_view(int c, rtgb_camera_frame_view& v) const {
+        const FrameBufs& f = frames[last];
+        const long long o = last_pixel_offset[c];
+        v.camera_index = c;
+        v.width = last_w[c];
+        v.height = last_h[c];
+        v.beauty = f.beauty + o;
+        v.normal = f.normal + o;
+        v.denoiser_normal = f.dnormal + o;
+        v.albedo = f.albedo + o;
+        v.depth = f.depth + o;
+        v.flow = f.flow + o;
+        v.flow_trustworthiness = f.trust + o;
+    }
+
+    void fill_stats(rtgb_frame_views* out) {
+        float ms = 0.0f;
+        RTGB_CHECK(cudaEventElapsedTime(&ms, ev_start, ev_stop));
+        out->frame_render_ms = ms;
+        for (int c = 0; c < out->camera_count; ++c) out->cameras[c].render_ms = ms;
+        const Counters& k = *h_counters;
+        out->primary_rays = k.rays[0];
+        out->extension_rays = k.rays[1];
+        out->shadow_rays = k.rays[2];
+        out->restir_visibility_rays = k.rays[3];
+        out->rays_traced = k.rays[0] + k.rays[1] + k.rays[2] + k.rays[3];
+    }
+
+    void check_camera(int c) const {
+        if (last < 0) throw Invalid{"no frame has been rendered"};
+        if (c < 0 || c >= last_count) throw Invalid{"camera_index out of range: camera_index=" + std::to_string(c) + ", active_count=" + std::to_string(last_count)};
+    }
+
+    void download(int c, float* beauty, float* normal, float* albedo, float* depth, float* ms) {
+        check_camera(c);
+        const size_t n = static_cast<size_t>(last_w[c]) * last_h[c];
+        const FrameBufs& f = frames[last];
+        const long long o = last_pixel_offset[c];
+        RTGB_CHECK(cudaEventRecord(ev_start, stream));
+        if (beauty) RTGB_CHECK(cudaMemcpyAsync(beauty, f.beauty + o, n * 16, cudaMemcpyDeviceToHost, stream));
+        if (normal) RTGB_CHECK(cudaMemcpyAsync(normal, f.normal + o, n * 16, cudaMemcpyDeviceToHost, stream));
+        if (albedo) RTGB_CHECK(cudaMemcpyAsync(albedo, f.albedo + o, n * 16, cudaMemcpyDeviceToHost, stream));
+        if (depth) RTGB_CHECK(cudaMemcpyAsync(depth, f.depth + o, n * 4, cudaMemcpyDeviceToHost, stream));
+        RTGB_CHECK(cudaEventRecord(ev_stop, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        if (ms) RTGB_CHECK(cudaEventElapsedTime(ms, ev_start, ev_stop));
+    }
+
+    void download_buffer(int c, int which, void* host, size_t bytes) {
+        check_camera(c);
+        const size_t n = static_cast<size_t>(last_w[c]) * last_h[c];
+        const FrameBufs& f = frames[last];
+        const long long o = last_pixel_offset[c];
+        const void* src = nullptr;
+        size_t need = 0;
+        switch (which) {
+            case 0: src = f.beauty + o; need = n * 16; break;
+            case 1: src = f.normal + o; need = n * 16; break;
+            case 2: src = f.dnormal + o; need = n * 16; break;
+            case 3: src = f.albedo + o; need = n * 16; break;
+            case 4: src = f.depth + o; need = n * 4; break;
+            case 5: src = f.flow + o; need = n * 8; break;
+            case 6: src = f.trust + o; need = n * 4; break;
+            case 7: src = f.reservoirs + o; need = n * sizeof(Reservoir); break;
+            default: throw Invalid{"unknown frame buffer"};
+        }
+        if (bytes != need) throw Invalid{"buffer size mismatch: expected " + std::to_string(need) + " bytes"};
+        RTGB_CHECK(cudaMemcpyAsync(host, src, need, cudaMemcpyDeviceToHost, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+    }
+};
+
+namespace {
+
+template <typename F>
+rtgb_status guarded(rtgb_handle h, F&& fn) {
+    try {
+        if (h) h->error.clear();
+        return static_cast<rtgb_status>(fn());
+    } catch (const Invalid& e) {
+        if (h) h->error = e.message;
+        return RTGB_INVALID_ARGUMENT;
+    } catch (const CudaFailure& f) {
+        if (h) h->fail_cuda(f);
+        return RTGB_RUNTIME_ERROR;
+    } catch (const std::bad_alloc&) {
+        if (h) h->error = "host allocation failed";
+        return RTGB_RUNTIME_ERROR;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+rtgb_status rtgb_create(const rtgb_create_info* info, rtgb_handle* out) {
+    if (out == nullptr) return RTGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    rtgb_create_info defaults{0, 1, 0};
+    auto* h = new (std::nothrow) rtgb_renderer();
+    if (!h) return RTGB_RUNTIME_ERROR;
+    try {
+        h->init(info ? *info : defaults);
+    } catch (const CudaFailure&) {
+        delete h;
+        return RTGB_RUNTIME_ERROR;
+    }
+    *out = h;
+    return RTGB_OK;
+}
+
+void rtgb_destroy(rtgb_handle h) { delete h; }
+
+const char* rtgb_last_error(rtgb_handle h) { return h ? h->error.c_str() : "null handle"; }
+
+rtgb_status rtgb_prepare_scene(rtgb_handle h, const rtgb_scene* scene) {
+    if (!h || !scene) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->prepare(*scene);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_reset_sequence(rtgb_handle h, uint32_t s) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    h->sample_stream = s;
+    h->reset_accumulation();
+    return RTGB_OK;
+}
+
+rtgb_status rtgb_reset_accumulation(rtgb_handle h) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    h->reset_accumulation();
+    return RTGB_OK;
+}
+
+rtgb_status rtgb_render_frame(rtgb_handle h, const rtgb_camera_rig* rig, const rtgb_render_profile* profile,
+    int32_t active, rtgb_frame_views* out) {
+    if (!h || !rig || !profile) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] { return h->render(*rig, *profile, active, true, out); });
+}
+
+rtgb_status rtgb_render_frame_async(rtgb_handle h, const rtgb_camera_rig* rig, const rtgb_render_profile* profile,
+    int32_t active) {
+    if (!h || !rig || !profile) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] { return h->render(*rig, *profile, active, false, nullptr); });
+}
+
+rtgb_status rtgb_frame_stats(rtgb_handle h, rtgb_frame_views* out) {
+    if (!h || !out) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (h->last < 0) throw Invalid{"no frame has been rendered"};
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        std::memset(out, 0, sizeof *out);
+        out->camera_count = h->last_count;
+        out->sample_stream = h->sample_stream - 1;
+        for (int c = 0; c < h->last_count; ++c) h->fill_view(c, out->cameras[c]);
+        h->fill_stats(out);
+        return h->h_counters->error != 0 ? RTGB_DEVICE_FAULT_FLAG : RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_ray_totals(rtgb_handle h, uint64_t totals[4]) {
+    if (!h || !totals) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        Counters k;
+        RTGB_CHECK(cudaMemcpy(&k, h->d_counters, sizeof k, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < 4; ++i) totals[i] = k.cum_rays[i];
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_frame(rtgb_handle h, int32_t c, float* beauty, float* normal, float* albedo, float* depth,
+    float* ms) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->download(c, beauty, normal, albedo, depth, ms);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_buffer(rtgb_handle h, int32_t c, int32_t which, void* host, size_t bytes) {
+    if (!h || !host) return RTGB_INVALID_ARGUMENT;
+    if (which < 0 || which > 6) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->download_buffer(c, which, host, bytes);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_reservoirs(rtgb_handle h, int32_t c, void* host, size_t bytes) {
+    if (!h || !host) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->download_buffer(c, 7, host, bytes);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_restir_diagnostics(rtgb_handle h, int32_t c, rtgb_restir_stats* out) {
+    if (!h || !out) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->check_camera(c);
+        const size_t n = static_cast<size_t>(h->last_w[c]) * h->last_h[c];
+        std::vector<Reservoir> r(n);
+        h->download_buffer(c, 7, r.data(), n * sizeof(Reservoir));
+        rtgb_restir_stats d{};
+        d.pixel_count = static_cast<int32_t>(n);
+        for (const Reservoir& x : r) {
+            if (x.valid == 0) continue;
+            ++d.active_reservoir_count;
+            if (x.temporal_candidate_count > 0) ++d.temporal_reuse_count;
+            if (x.spatial_candidate_count > 0) ++d.spatial_reuse_count;
+            if (x.bias_correction_source_count > 0) ++d.bias_corrected_count;
+            d.max_candidate_count = std::max(d.max_candidate_count, x.candidate_count);
+            d.max_age = std::max(d.max_age, x.age);
+        }
+        *out = d;
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_render_direction_debug(rtgb_handle h, const rtgb_camera_rig* rig, int32_t c, uint8_t* host) {
+    if (!h || !rig || !host) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (rig->active_count < 1 || rig->active_count > RTGB_MAX_CAMERAS) throw Invalid{"render_radiance requires rig.active_count in [1, 4]"};
+        if (c < 0 || c >= rig->active_count) throw Invalid{"render_radiance camera_index out of range"};
+        const rtgb_camera& cam = rig->cameras[c];
+        if (cam.enabled == 0 || cam.width <= 0 || cam.height <= 0) throw Invalid{"render_radiance camera slot is disabled or invalid"};
+        RTGB_CHECK(cudaSetDevice(h->device));
+        CameraRes tmp;
+        tmp.valid = false;
+        // a private camera resource so the frame's camera tables stay untouched
+        upload(tmp.lut, cam.equi.lut, RTGB_EQUI_LUT_SIZE, h->stream);
+        tmp.dirs.ensure(static_cast<size_t>(cam.width) * cam.height * sizeof(float4));
+        CameraDev d = rtgb_renderer::camera_dev(cam, 0, 0);
+        d.lut = tmp.lut.as<double>();
+        d.dirs = tmp.dirs.as<float4>();
+        launch_camera_dirs(d, tmp.dirs.as<float4>(), h->stream);
+        const size_t n = static_cast<size_t>(cam.width) * cam.height;
+        h->debug_rgba.ensure(n * 4);
+        launch_direction_debug(d, h->debug_rgba.as<uint8_t>(), h->stream);
+        RTGB_CHECK(cudaGetLastError());
+        RTGB_CHECK(cudaMemcpyAsync(host, h->debug_rgba.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        tmp.lut.release();
+        tmp.dirs.release();
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_tonemap_rgba8(rtgb_handle h, int32_t c, uint8_t* host) {
+    if (!h || !host) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->check_camera(c);
+        const size_t n = static_cast<size_t>(h->last_w[c]) * h->last_h[c];
+        h->debug_rgba.ensure(n * 4);
+        launch_tonemap(h->frames[h->last].beauty + h->last_pixel_offset[c], h->debug_rgba.as<uint8_t>(),
+            static_cast<long long>(n), h->stream);
+        RTGB_CHECK(cudaGetLastError());
+        RTGB_CHECK(cudaMemcpyAsync(host, h->debug_rgba.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_acceleration_info_get(rtgb_handle h, rtgb_acceleration_info* out) {
+    if (!h || !out) return RTGB_INVALID_ARGUMENT;
+    rtgb_acceleration_info a{};
+    a.primitive_count = h->prim_count;
+    a.node_count = h->scene.node_count;
+    a.analytic_light_node_count = h->scene.analytic_node_count;
+    a.analytic_bvh_light_count = h->analytic_bvh_count;
+    a.build_ms = h->build_ms;
+    a.traversal_stack_overflows = h->h_counters ? h->h_counters->overflow : 0;
+    *out = a;
+    return RTGB_OK;
+}
+
+void* rtgb_stream(rtgb_handle h) { return h ? static_cast<void*>(h->stream) : nullptr; }
+
+rtgb_status rtgb_download_path_records(rtgb_handle h, int32_t c, int32_t* codes, int32_t max_bounces, float* radiance,
+    int64_t paths) {
+    if (!h || !codes || !radiance) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->record || h->paths.codes == nullptr) throw Invalid{"path records need rtgb_create_info::debug_path_records"};
+        h->check_camera(c);
+        const long long n = static_cast<long long>(h->last_w[c]) * h->last_h[c] * h->last_spp;
+        if (paths != n || max_bounces != h->last_bounces) throw Invalid{"path record shape mismatch"};
+        const long long first = h->last_pixel_offset[c] * h->last_spp;
+        RTGB_CHECK(cudaMemcpyAsync(codes, h->paths.codes + first * max_bounces, static_cast<size_t>(n) * max_bounces * 4,
+            cudaMemcpyDeviceToHost, h->stream));
+        std::vector<float4> rad(static_cast<size_t>(n));
+        RTGB_CHECK(cudaMemcpyAsync(rad.data(), h->paths.rad + first, static_cast<size_t>(n) * 16, cudaMemcpyDeviceToHost, h->stream));
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        for (long long i = 0; i < n; ++i) {
+            radiance[3 * i] = rad[static_cast<size_t>(i)].x;
+            radiance[3 * i + 1] = rad[static_cast<size_t>(i)].y;
+            radiance[3 * i + 2] = rad[static_cast<size_t>(i)].z;
+        }
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_lbvh(rtgb_handle h, uint32_t* sorted_morton, int32_t* sorted_primitive, int32_t* children) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->prepared) throw Invalid{"no scene prepared"};
+        const int n = h->prim_count;
+        if (n < 2) throw Invalid{"the scene has fewer than two primitives and no hierarchy"};
+        if (sorted_morton) RTGB_CHECK(cudaMemcpy(sorted_morton, h->sorted_keys.p, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost));
+        if (sorted_primitive) RTGB_CHECK(cudaMemcpy(sorted_primitive, h->sorted_vals.p, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToHost));
+        if (children) {
+            std::vector<BvhNode> nodes(static_cast<size_t>(n - 1));
+            RTGB_CHECK(cudaMemcpy(nodes.data(), h->nodes.p, nodes.size() * sizeof(BvhNode), cudaMemcpyDeviceToHost));
+            for (int i = 0; i < n - 1; ++i) {
+                int c0, c1;
+                std::memcpy(&c0, &nodes[static_cast<size_t>(i)].a.w, 4);
+                std::memcpy(&c1, &nodes[static_cast<size_t>(i)].b.w, 4);
+                children[2 * i] = c0;
+                children[2 * i + 1] = c1;
+            }
+        }
+        return RTGB_OK;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,107 @@
+// Wavefront state, frame buffers and launch entry points.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace rtgb {
+
+// Frame-wide AOV buffers: every active camera's pixels back to back
+// (camera c starts at CameraDev::pixel_offset). DeviceFrameBuffers of
+// src/realtime/gpu/launch_params.h:25-34.
+struct FrameBufs {
+    float4* beauty;
+    float4* normal;
+    float4* dnormal;
+    float4* albedo;
+    float* depth;
+    float2* flow;
+    float* trust;
+    Reservoir* reservoirs;
+};
+
+// Structure-of-arrays path streams, one slot per path (pixel-major, sample-minor).
+struct Paths {
+    float4* ray_o;      // origin.xyz
+    float4* ray_d;      // direction.xyz
+    float4* thr;        // throughput.xyz, w = previous BSDF pdf
+    float4* rad;        // radiance.xyz
+    float4* prev_pos;   // previous scatter position.xyz, w = flags (1 valid, 2 delta) as int bits
+    float4* prev_nrm;   // previous scatter normal.xyz, w = previous material type as int bits
+    int2* prev_prim;    // previous primitive type, index
+    uint32_t* rng;
+    float4* aux_n;      // bounce-0 shading normal.xyz, w = depth
+    float4* aux_a;      // bounce-0 albedo.xyz, w = 1 when captured
+    float4* hit;        // x = t, y = surface/medium code bits (-1 miss), z = analytic light index bits
+    float4* sh_o[2];    // shadow ray origin.xyz, w = tmax
+    float4* sh_d[2];    // shadow ray direction.xyz
+    float4* sh_c[2];    // contribution (throughput * direct).xyz, w = 1 when pending
+    Reservoir* res_scratch;  // per path reservoir when spp > 1 (ReSTIR)
+    int* res_written;        // per path: 1 when the path wrote res_scratch
+    int* queue[2];
+    int* shadow_queue;
+    int* codes;              // optional parity record [path][max_bounces]
+};
+
+struct Counters {
+    int active[2];
+    int shadow;
+    int error;
+    unsigned long long rays[4];  // primary, extension, shadow, restir visibility
+    int overflow;
+    int pad[3];
+    unsigned long long cum_rays[4];  // running totals since the counters were last cleared
+};
+
+struct FrameParams {
+    CameraDev cam[RTGB_MAX_CAMERAS];
+    CameraDev prev[RTGB_MAX_CAMERAS];
+    int prev_valid[RTGB_MAX_CAMERAS];
+    int history_length[RTGB_MAX_CAMERAS];
+    int cam_count;
+    int spp;
+    int max_bounces;
+    int rr_start;
+    long long total_pixels;
+    long long total_paths;
+    uint32_t stream;
+    int restir_enabled;
+    int restir_candidates;
+    int restir_temporal;
+    int restir_max_age;
+    int restir_max_temporal;
+    int restir_spatial;
+    int restir_max_spatial;
+    int restir_bias;
+    int record_paths;
+    FrameBufs cur;      // this frame's buffers
+    FrameBufs hist;     // the previous frame's (ping-pong)
+};
+
+struct LaunchShape {
+    int grid;
+    int block;
+};
+
+// Kernel launchers (wavefront.cu). All are asynchronous on `stream`.
+void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream);
+void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
+void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
+    LaunchShape shape, cudaStream_t stream);
+void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
+    LaunchShape shape, cudaStream_t stream);
+void launch_shadow(DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
+void launch_finalize(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
+void launch_resolve(const FrameParams* fp, LaunchShape shape, cudaStream_t stream);
+void launch_direction_debug(const CameraDev& cam, uint8_t* rgba, cudaStream_t stream);
+void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
+// Persistent grid sizes: SM count x resident blocks per SM for raygen, trace,
+// shade, shadow, finalize and resolve.
+void query_launch_shapes(int sm_count, LaunchShape* shapes);
+void launch_tonemap(const float4* beauty, uint8_t* rgba, long long pixels, cudaStream_t stream);
+
+// Scene preparation kernels (scene_prep.cu).
+void launch_prim_records(const DeviceScene& scene, PrimRecord* records, float4* aabb_lo, float4* aabb_hi, float pad,
+    cudaStream_t stream);
+void launch_gather_records(const PrimRecord* in, const int* order, PrimRecord* out, int n, cudaStream_t stream);
+
+}  // namespace rtgb

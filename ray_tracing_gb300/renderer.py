@@ -1,0 +1,176 @@
+"""Python mirror of the reference's renderer surface over the C ABI.
+
+``Renderer`` follows ``RendererPool`` / ``OptixRenderer``
+(src/realtime/gpu/renderer_pool.h:30-53, optix_renderer.h:69-128):
+``prepare_scene``, ``reset_sequence``, ``reset_accumulation``,
+``render_frame`` (all active cameras, one launch sequence), per-camera
+downloads, ``restir_diagnostics`` and ``render_direction_debug``. Errors come
+back as :class:`abi.RtgbError` carrying the library's message — the
+exceptions the reference throws.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+
+
+@dataclass
+class CameraFrame:
+    """RadianceFrame of src/realtime/gpu/frame_types.h:14-22 (host arrays)."""
+    camera_index: int
+    width: int
+    height: int
+    beauty_rgba: np.ndarray
+    normal_rgba: np.ndarray
+    albedo_rgba: np.ndarray
+    depth: np.ndarray
+    render_ms: float
+    download_ms: float
+
+    @property
+    def average_luminance(self) -> float:
+        b = self.beauty_rgba.astype(np.float64)
+        return float(np.mean(0.2126 * b[..., 0] + 0.7152 * b[..., 1] + 0.0722 * b[..., 2]))
+
+
+class Renderer:
+    def __init__(self, device: int = 0, use_cuda_graph: bool = True, debug_path_records: bool = False):
+        self.lib = abi.load()
+        missing = getattr(self.lib, "rtgb_missing_symbols", [])
+        if missing:
+            raise RuntimeError(f"librtgb.so lacks {missing}: rebuild with __graft_entry__.build()")
+        self.h = C.c_void_p()
+        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records))
+        st = self.lib.rtgb_create(C.byref(info), C.byref(self.h))
+        if st != abi.OK:
+            raise abi.RtgbError(st, "rtgb_create failed (no CUDA device?)")
+        self.last_views: abi.FrameViews | None = None
+        self._scene_ref = None
+
+    def close(self):
+        if self.h:
+            self.lib.rtgb_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st, what):
+        abi.check(st, self.h, what)
+
+    def prepare_scene(self, scene: abi.Scene) -> None:
+        self._check(self.lib.rtgb_prepare_scene(self.h, C.byref(scene)), "prepare_scene")
+        self._scene_ref = scene
+
+    def reset_sequence(self, sample_stream: int) -> None:
+        self._check(self.lib.rtgb_reset_sequence(self.h, sample_stream), "reset_sequence")
+
+    def reset_accumulation(self) -> None:
+        self._check(self.lib.rtgb_reset_accumulation(self.h), "reset_accumulation")
+
+    def render_frame(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int) -> abi.FrameViews:
+        views = abi.FrameViews()
+        self._check(self.lib.rtgb_render_frame(self.h, C.byref(rig), C.byref(profile), active, C.byref(views)),
+                    "render_frame")
+        self.last_views = views
+        return views
+
+    def render_frame_async(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int) -> None:
+        self._check(self.lib.rtgb_render_frame_async(self.h, C.byref(rig), C.byref(profile), active),
+                    "render_frame_async")
+
+    def frame_stats(self) -> abi.FrameViews:
+        views = abi.FrameViews()
+        self._check(self.lib.rtgb_frame_stats(self.h, C.byref(views)), "frame_stats")
+        self.last_views = views
+        return views
+
+    def ray_totals(self) -> np.ndarray:
+        out = (C.c_uint64 * 4)()
+        self._check(self.lib.rtgb_ray_totals(self.h, out), "ray_totals")
+        return np.array(list(out), dtype=np.uint64)
+
+    def stream_ptr(self) -> int:
+        return int(self.lib.rtgb_stream(self.h) or 0)
+
+    def _size(self, cam: int) -> tuple[int, int]:
+        v = self.last_views
+        if v is None or cam >= v.camera_count:
+            raise abi.RtgbError(1, f"camera_index out of range: {cam}")
+        return v.cameras[cam].width, v.cameras[cam].height
+
+    def download(self, cam: int) -> CameraFrame:
+        w, h = self._size(cam)
+        beauty = np.empty((h, w, 4), np.float32)
+        normal = np.empty((h, w, 4), np.float32)
+        albedo = np.empty((h, w, 4), np.float32)
+        depth = np.empty((h, w), np.float32)
+        ms = C.c_float()
+        self._check(self.lib.rtgb_download_frame(self.h, cam, beauty.ctypes.data, normal.ctypes.data,
+                                                 albedo.ctypes.data, depth.ctypes.data, C.byref(ms)), "download")
+        return CameraFrame(cam, w, h, beauty, normal, albedo, depth, self.last_views.cameras[cam].render_ms,
+                           ms.value)
+
+    BUFFERS = {"beauty": (0, 4), "normal": (1, 4), "denoiser_normal": (2, 4), "albedo": (3, 4), "depth": (4, 1),
+               "flow": (5, 2), "flow_trustworthiness": (6, 1)}
+
+    def buffer(self, cam: int, name: str) -> np.ndarray:
+        which, ch = self.BUFFERS[name]
+        w, h = self._size(cam)
+        out = np.empty((h, w, ch) if ch > 1 else (h, w), np.float32)
+        self._check(self.lib.rtgb_download_buffer(self.h, cam, which, out.ctypes.data, out.nbytes), "download_buffer")
+        return out
+
+    def reservoirs(self, cam: int) -> np.ndarray:
+        w, h = self._size(cam)
+        out = np.zeros(w * h, dtype=abi.RESERVOIR_DTYPE)
+        self._check(self.lib.rtgb_download_reservoirs(self.h, cam, out.ctypes.data, out.nbytes), "reservoirs")
+        return out
+
+    def restir_diagnostics(self, cam: int) -> abi.RestirDiagnostics:
+        d = abi.RestirDiagnostics()
+        self._check(self.lib.rtgb_restir_diagnostics(self.h, cam, C.byref(d)), "restir_diagnostics")
+        return d
+
+    def path_records(self, cam: int, spp: int, max_bounces: int):
+        w, h = self._size(cam)
+        paths = w * h * spp
+        codes = np.empty((paths, max_bounces), np.int32)
+        rad = np.empty((paths, 3), np.float32)
+        self._check(self.lib.rtgb_download_path_records(self.h, cam, codes.ctypes.data, max_bounces,
+                                                        rad.ctypes.data, paths), "path_records")
+        return codes, rad
+
+    def render_direction_debug(self, rig: abi.CameraRig, cam: int) -> np.ndarray:
+        c = rig.cameras[cam]
+        out = np.empty((c.height, c.width, 4), np.uint8)
+        self._check(self.lib.rtgb_render_direction_debug(self.h, C.byref(rig), cam, out.ctypes.data),
+                    "render_direction_debug")
+        return out
+
+    def tonemap_rgba8(self, cam: int) -> np.ndarray:
+        w, h = self._size(cam)
+        out = np.empty((h, w, 4), np.uint8)
+        self._check(self.lib.rtgb_tonemap_rgba8(self.h, cam, out.ctypes.data), "tonemap")
+        return out
+
+    def acceleration_info(self) -> abi.AccelerationInfo:
+        a = abi.AccelerationInfo()
+        self._check(self.lib.rtgb_acceleration_info_get(self.h, C.byref(a)), "acceleration_info")
+        return a
+
+    def lbvh(self):
+        n = self.acceleration_info().primitive_count
+        keys = np.empty(n, np.uint32)
+        order = np.empty(n, np.int32)
+        children = np.empty((max(n - 1, 0), 2), np.int32)
+        self._check(self.lib.rtgb_download_lbvh(self.h, keys.ctypes.data, order.ctypes.data, children.ctypes.data),
+                    "download_lbvh")
+        return keys, order, children

@@ -1,0 +1,71 @@
+"""The C ABI library: loads without a GPU, exports every declared entry point,
+and its structure layouts match the header as a C compiler sees them."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from ray_tracing_gb300 import abi
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "rtgb.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"\b(rtgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function():
+    lib = abi.load()
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) == set(abi.SIGNATURES), "abi.SIGNATURES must mirror include/rtgb.h"
+
+
+STRUCTS = {
+    "rtgb_texture": abi.Texture, "rtgb_material": abi.Material, "rtgb_sphere": abi.Sphere,
+    "rtgb_quad": abi.Quad, "rtgb_triangle": abi.Triangle, "rtgb_medium": abi.Medium,
+    "rtgb_analytic_light": abi.AnalyticLight, "rtgb_scene": abi.Scene, "rtgb_pinhole32": abi.Pinhole32,
+    "rtgb_equi62_lut1d": abi.Equi62Lut1d, "rtgb_camera": abi.Camera, "rtgb_camera_rig": abi.CameraRig,
+    "rtgb_render_profile": abi.RenderProfile, "rtgb_create_info": abi.CreateInfo,
+    "rtgb_camera_frame_view": abi.CameraFrameView, "rtgb_frame_views": abi.FrameViews,
+    "rtgb_restir_stats": abi.RestirDiagnostics, "rtgb_acceleration_info": abi.AccelerationInfo,
+}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    src = tmp_path / "sizes.c"
+    lines = ['#include <stdio.h>', '#include "rtgb.h"', "int main(void) {"]
+    for name in STRUCTS:
+        lines.append(f'  printf("{name} %zu\\n", sizeof({name}));')
+    lines.append("  return 0; }")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    for line in out.splitlines():
+        name, size = line.split()
+        assert C.sizeof(STRUCTS[name]) == int(size), name
+
+
+def test_create_without_gpu_reports_an_error_instead_of_crashing():
+    pytest.importorskip("torch")
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert abi.load().rtgb_create(None, C.byref(h)) == 2
+    assert not h.value
+
+
+def test_null_arguments_are_invalid():
+    lib = abi.load()
+    assert lib.rtgb_prepare_scene(None, None) == 1
+    assert lib.rtgb_render_frame(None, None, None, 1, None) == 1
+    assert lib.rtgb_reset_sequence(None, 0) == 1
+    assert lib.rtgb_download_frame(None, 0, None, None, None, None, None) == 1
