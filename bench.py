@@ -1,0 +1,385 @@
+#!/usr/bin/env python3
+"""Benchmark of the realtime radiance path on GB300.
+
+Workload (one step = one frame of every camera):
+  seeded random-sphere field (ground r=1000 + 22x22 r=0.2 spheres: 80% Lambertian,
+  15% metal, 5% dielectric) with 1024 emissive rect lights as analytic lights;
+  4 pinhole32 cameras 640x480, 1 spp, depth 4, ReSTIR DI with 32 initial
+  candidates, temporal reuse and 1 spatial neighbour, BASIC bias correction.
+
+value   = rays traced (primary + extension + shadow + ReSTIR visibility) per
+          second of device time, inputs resident (Mrays/s); each frame is timed
+          with CUDA events on the renderer's stream, an L2 flush runs between
+          frames outside the events.
+e2e     = the same metric through the C ABI with host buffers: rtgb_render_frame
+          and the download of every camera's beauty/normal/albedo/depth into
+          pinned host memory, wall-clock timed per step.
+roofline: the launch with the largest share of the frame, SURVEY per-unit
+          algorithmic bytes over its CUDA-event durations, against the measured
+          HBM copy bandwidth.
+cpu_baseline / --impl reference: the CPU oracle (restatement of the reference's
+          radiance kernel, with the reference's median-split BVH) on all host
+          threads, over a band of rows of the same workload.
+
+Launch: python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+(under torchrun for N > 1: one process per GPU, independent replicas).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "4-cam ms/frame at equal relMSE to 4096spp ref, denoised vs plain; Mrays/s"
+UNIT = "Mrays/s"
+SEED = 20260718          # the reference protocol's default sequence seed
+WIDTH, HEIGHT, CAMERAS = 640, 480, 4
+LIGHTS = 1024
+L2_FLUSH_BYTES = 256 << 20
+
+# SURVEY 8(d) algorithmic bytes per unit (SoA stream bytes, BVH traffic excluded)
+BYTES_RAYGEN = 32 + 48          # per path: ray + path state
+BYTES_TRACE = 32 + 16           # per ray: read ray, write hit
+BYTES_SHADE = 16 + 48 + 48 + 32 + 32 + 16   # per path segment
+BYTES_RESTIR_PER_SPATIAL = 84   # per reuse neighbour, added to 84 + 84 (history) + 84 (write)
+BYTES_SHADOW = 32 + 4           # per shadow ray
+BYTES_RESOLVE = 68 + 36 + 68 + 12  # per pixel (accumulate + resolve)
+
+
+def workload_config(spatial=1):
+    return {
+        "workload": "random_spheres_4x640x480_1spp_d4_restir32",
+        "scene": f"ground + 22x22 spheres, {LIGHTS} analytic rect lights",
+        "cameras": f"{CAMERAS}x pinhole32 {WIDTH}x{HEIGHT}",
+        "spp": 1, "max_bounces": 4, "restir_candidates": 32, "temporal_reuse": 1, "spatial_neighbors": spatial,
+        "denoise": "off (no learned denoiser in this build)",
+        "seed": SEED, "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed frames",
+    }
+
+
+def make_inputs():
+    from ray_tracing_gb300 import scenes
+    sc = scenes.HostScene("random_spheres", seed=0, detail=LIGHTS)
+    rig = scenes.default_rig("random_spheres", CAMERAS, WIDTH, HEIGHT)
+    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1,
+                          restir_initial_candidates=32, restir_temporal_reuse=1, restir_spatial_neighbors=1)
+    return sc, rig, prof
+
+
+# ---- clocks -------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "200"], stdout=self.out,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for _, _, flags in rows:
+            for n, f in zip(names, flags):
+                if f.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---- CPU oracle (baseline / reference arm) ----------------------------------------
+
+def oracle_frames(sc, rig, prof, stride, frames, threads=0):
+    """Renders `frames` frames of every `stride`-th row on the CPU oracle;
+    returns (rays traced in the last frame, seconds of the last frame)."""
+    from oracle.binding import OracleRenderer
+    orc = OracleRenderer(sc.view, use_reference_bvh=True, threads=threads)
+    orc.reset_sequence(SEED)
+    rays = secs = 0.0
+    for _ in range(frames):
+        t0 = time.perf_counter()
+        orc.render_frame(rig, prof, CAMERAS, row_stride=stride)
+        secs = time.perf_counter() - t0
+        rays = sum(orc.rays(c) for c in range(CAMERAS))
+    orc.close()
+    return rays, secs
+
+
+def cpu_baseline(sc, rig, prof):
+    cores = os.cpu_count() or 1
+    stride = 2
+    rays, secs = oracle_frames(sc, rig, prof, stride, frames=2, threads=cores)
+    return {"value": rays / secs / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"CPU oracle (reference BVH, {cores} threads): every {stride}th row of each of the "
+                      f"{CAMERAS} cameras, 2nd of 2 frames timed ({secs:.2f} s, {int(rays)} rays)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    sc, rig, prof = make_inputs()
+    cores = os.cpu_count() or 1
+    stride = 20
+    from oracle.binding import OracleRenderer
+    orc = OracleRenderer(sc.view, use_reference_bvh=True, threads=cores)
+    orc.reset_sequence(SEED)
+    for _ in range(args.warmup):
+        orc.render_frame(rig, prof, CAMERAS, row_stride=stride)
+    rays = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.render_frame(rig, prof, CAMERAS, row_stride=stride)
+        rays += sum(orc.rays(c) for c in range(CAMERAS))
+    secs = time.perf_counter() - t0
+    value = rays / secs / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"every {stride}th row of each camera per step; the reference's renderer "
+                                   "needs CUDA/OptiX/Eigen and does not build here, so its radiance kernel runs as "
+                                   "the C++ oracle restatement"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---- GPU arm --------------------------------------------------------------------------
+
+def roofline(stage_ms, frames_stats, spatial):
+    """Picks the launch kind with the largest summed time; returns its roofline record."""
+    peaks = {}
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        peaks = json.loads(p.read_text())
+    peak = peaks.get("hbm_gbs")
+    peak_note = "of measured" if peak else "of fallback"
+    peak = peak or 6800.0
+    kinds = {"raygen": [0.0, 0.0, 0], "trace": [0.0, 0.0, 0], "shade": [0.0, 0.0, 0], "shadow": [0.0, 0.0, 0],
+             "resolve": [0.0, 0.0, 0]}
+    for times, st in zip(stage_ms, frames_stats):
+        mb = (len(times) - 3) // 3
+        paths = st["paths"]
+        active = st["active"]
+        kinds["raygen"][0] += times[0]
+        kinds["raygen"][1] += paths * BYTES_RAYGEN
+        kinds["raygen"][2] += 1
+        for b in range(mb):
+            t_tr, t_sh, t_sd = times[1 + 3 * b], times[2 + 3 * b], times[3 + 3 * b]
+            kinds["trace"][0] += t_tr
+            kinds["trace"][1] += active[b] * BYTES_TRACE
+            kinds["trace"][2] += 1
+            restir = st["restir_pixels"] * (84 + 84 * (1 + spatial) + 84) if b == 0 else 0
+            kinds["shade"][0] += t_sh
+            kinds["shade"][1] += active[b] * BYTES_SHADE + restir
+            kinds["shade"][2] += 1
+            kinds["shadow"][0] += t_sd
+            kinds["shadow"][2] += 1
+        kinds["shadow"][1] += st["shadow_rays"] * BYTES_SHADOW
+        kinds["resolve"][0] += times[-2] + times[-1]
+        kinds["resolve"][1] += st["pixels"] * BYTES_RESOLVE
+        kinds["resolve"][2] += 1
+    name = max(kinds, key=lambda k: kinds[k][0])
+    ms, nbytes, launches = kinds[name]
+    achieved = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    traffic = None
+    tpath = ROOT / "profiles" / "roofline_traffic.json"
+    if tpath.exists():
+        traffic = json.loads(tpath.read_text()).get(f"k_{name}")
+    total = sum(v[0] for v in kinds.values())
+    return {"kernel": f"k_{name}", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": peak_note,
+            "avg_launch_ms": ms / max(launches, 1), "algorithmic_bytes_per_launch": nbytes / max(launches, 1),
+            "share_of_frame": ms / total if total > 0 else None,
+            "stage_ms_per_frame": {k: v[0] / max(len(stage_ms), 1) for k, v in kinds.items()}}
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from ray_tracing_gb300.renderer import Renderer
+
+    torch.cuda.set_device(local_rank)
+    sc, rig, prof = make_inputs()
+    r = Renderer(device=local_rank, stage_timing=True)
+    r.prepare_scene(sc.view)
+    r.reset_sequence(SEED)
+    stream = torch.cuda.ExternalStream(r.stream_ptr())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
+    for _ in range(args.warmup):
+        r.render_frame(rig, prof, CAMERAS)
+    launches_per_frame = 3 + 4 * prof.max_bounces  # raygen + (trace, reset, shade, shadow) per bounce + finalize + resolve
+
+    sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
+                           if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
+    sampler.start()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    rays0 = r.ray_totals()
+    frame_ms, stage_ms, frame_stats = [], [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ev0.record(stream)
+        r.render_frame_async(rig, prof, CAMERAS)
+        ev1.record(stream)
+        v = r.frame_stats()
+        frame_ms.append(ev0.elapsed_time(ev1))
+        stage_ms.append(r.stage_times())
+        frame_stats.append({"paths": WIDTH * HEIGHT * CAMERAS, "pixels": WIDTH * HEIGHT * CAMERAS,
+                            "active": [int(v.active_paths[b]) for b in range(prof.max_bounces)],
+                            "restir_pixels": int(v.restir_pixels), "shadow_rays": int(v.shadow_rays)})
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    rays = float(np.sum(r.ray_totals() - rays0))
+    total_ms = float(sum(frame_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        rt = torch.tensor([rays], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(rt, op=dist.ReduceOp.SUM)
+        rays = float(rt.item())
+    value = rays / (total_ms * 1e-3) / 1e6
+
+    # e2e: public API with host buffers (pinned), wall clock per step
+    e2e_steps = max(3, min(args.steps, 10))
+    pixels = WIDTH * HEIGHT
+    host = [[torch.empty(pixels * 4, dtype=torch.float32, pin_memory=True) for _ in range(3)]
+            + [torch.empty(pixels, dtype=torch.float32, pin_memory=True)] for _ in range(CAMERAS)]
+    import ctypes as C
+    lib = r.lib
+    e2e_rays = 0
+    h2d = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        views = r.render_frame(rig, prof, CAMERAS)
+        e2e_rays += views.rays_traced
+        h2d += views.h2d_bytes
+        for c in range(CAMERAS):
+            b, n, a, d = host[c]
+            st = lib.rtgb_download_frame(r.h, c, b.data_ptr(), n.data_ptr(), a.data_ptr(), d.data_ptr(), None)
+            if st != 0:
+                raise RuntimeError("rtgb_download_frame failed")
+    e2e_secs = time.perf_counter() - t0
+    e2e = {"value": e2e_rays / e2e_secs / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d // e2e_steps),
+           "d2h_bytes_per_step": CAMERAS * pixels * (16 * 3 + 4), "steps": e2e_steps,
+           "ms_per_step": 1000.0 * e2e_secs / e2e_steps}
+    if world > 1:
+        t = torch.tensor([e2e["value"]], dtype=torch.float64, device=f"cuda:{local_rank}")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e["value"] = float(t.item())
+
+    if rank != 0:
+        return 0
+    roof = roofline(stage_ms, frame_stats, spatial=1)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single"),
+        "rays_per_frame": rays / args.steps / world,
+        "roofline": roof,
+        "e2e": e2e,
+        "clocks": clocks,
+        "gpu_launches": launches_per_frame * args.steps,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(sc, rig, prof)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        if args.impl == "reference":
+            dist.init_process_group("gloo")
+        else:
+            import torch
+            torch.cuda.set_device(local_rank)
+            dist.init_process_group("nccl")
+    from ray_tracing_gb300 import build
+    if rank == 0:
+        build.build_all()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+    else:
+        rc = run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

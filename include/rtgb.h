@@ -259,6 +259,7 @@ typedef struct rtgb_create_info {
     int32_t device;            /* CUDA ordinal (the reference hard-codes 0: optix_renderer.cpp:120) */
     int32_t use_cuda_graph;    /* capture each frame's launch sequence as a CUDA graph */
     int32_t debug_path_records;/* record per-path hit codes and radiance (parity tests) */
+    int32_t stage_timing;      /* record CUDA events between the frame's launches (rtgb_stage_times) */
 } rtgb_create_info;
 
 /* DeviceRadianceFrameView (src/realtime/gpu/device_radiance_frame_view.h) plus
@@ -290,6 +291,9 @@ typedef struct rtgb_frame_views {
     uint64_t extension_rays;
     uint64_t shadow_rays;
     uint64_t restir_visibility_rays;
+    uint64_t h2d_bytes;           /* bytes this frame copied host -> device (frame parameters, camera tables) */
+    uint64_t active_paths[64];    /* paths entering each bounce (wavefront queue lengths) */
+    uint64_t restir_pixels;       /* bounce-0 paths that ran ReSTIR DI */
 } rtgb_frame_views;
 
 /* RestirDiagnostics, optix_renderer.h:43-51 */
@@ -350,6 +354,11 @@ rtgb_status rtgb_render_frame_async(rtgb_handle handle, const rtgb_camera_rig* r
 
 /* Waits for the last enqueued frame and fills its views, timing and ray counts. */
 rtgb_status rtgb_frame_stats(rtgb_handle handle, rtgb_frame_views* out_views);
+
+/* Per-launch device times (ms) of the last frame, in launch order:
+ * raygen, then per bounce trace / shade / shadow, then finalize and resolve
+ * (3 * max_bounces + 3 entries). Needs rtgb_create_info::stage_timing. */
+rtgb_status rtgb_stage_times(rtgb_handle handle, float* out_ms, int32_t capacity, int32_t* out_count);
 
 /* Rays traced since the scene was prepared: primary, extension, shadow and
  * ReSTIR visibility (waits for the stream). */

@@ -24,7 +24,8 @@ _SIGS = {
     "orc_reset_accumulation": (None, [C.c_void_p]),
     "orc_set_path_records": (None, [C.c_void_p, C.c_int]),
     "orc_sample_stream": (C.c_uint32, [C.c_void_p]),
-    "orc_render_frame": (C.c_int, [C.c_void_p, P(abi.CameraRig), P(abi.RenderProfile), C.c_int, C.c_int, C.c_int]),
+    "orc_render_frame": (C.c_int, [C.c_void_p, P(abi.CameraRig), P(abi.RenderProfile), C.c_int, C.c_int, C.c_int,
+                                   C.c_int]),
     "orc_get_buffer": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
     "orc_get_path_records": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int64]),
     "orc_last_rays": (C.c_uint64, [C.c_void_p, C.c_int]),
@@ -93,9 +94,12 @@ class OracleRenderer:
     def set_path_records(self, on: bool):
         self.lib.orc_set_path_records(self.h, int(on))
 
-    def render_frame(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int, rows=None):
+    def render_frame(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int, rows=None, row_stride=1):
+        """Renders every active camera; `rows` = (first, end) restricts to a band, `row_stride` samples it."""
         y0, y1 = rows if rows else (0, 0)
-        st = self.lib.orc_render_frame(self.h, C.byref(rig), C.byref(profile), active, y0, y1)
+        if row_stride > 1 and not rows:
+            y0, y1 = 0, 1 << 30
+        st = self.lib.orc_render_frame(self.h, C.byref(rig), C.byref(profile), active, y0, y1, row_stride)
         if st != 0:
             raise RuntimeError(f"orc_render_frame status {st}")
         for i in range(active):

@@ -1405,7 +1405,8 @@ public:
 
     // launch_radiance_pipeline for every active camera; rows [y0, y1) only
     // when y1 > y0 (a bounded sample for timing).
-    int render_frame(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active, int y0, int y1) {
+    int render_frame(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active, int y0, int y1,
+        int stride) {
         if (active < 1 || active > RTGB_MAX_CAMERAS || active > rig.active_count) return RTGB_INVALID_ARGUMENT;
         if (cams_.size() < static_cast<size_t>(active)) cams_.resize(static_cast<size_t>(active));
         const uint32_t stream = stream_++;
@@ -1450,12 +1451,16 @@ public:
             const int ry0 = y1 > y0 ? std::max(0, y0) : 0;
             const int ry1 = y1 > y0 ? std::min(pc.height, y1) : pc.height;
             std::atomic<uint64_t> rays{0};
-            parallel_rows(ry0, ry1, [&](int y) {
+            const int step = stride > 1 ? stride : 1;
+            const int nrows = (ry1 - ry0 + step - 1) / step;
+            parallel_rows(0, nrows, [&](int r) {
+                const int y = ry0 + r * step;
                 uint64_t local = 0;
                 for (int x = 0; x < pc.width; ++x) local += radiance_pixel(p, x, y);
                 rays.fetch_add(local, std::memory_order_relaxed);
             });
-            parallel_rows(ry0, ry1, [&](int y) {
+            parallel_rows(0, nrows, [&](int r) {
+                const int y = ry0 + r * step;
                 for (int x = 0; x < pc.width; ++x) resolve_pixel(p, x, y);
             });
             cs.rays = rays.load();
@@ -1975,9 +1980,9 @@ void orc_set_path_records(orc_renderer* h, int on) { h->r->set_record(on != 0); 
 uint32_t orc_sample_stream(orc_renderer* h) { return h->r->stream(); }
 
 int orc_render_frame(orc_renderer* h, const rtgb_camera_rig* rig, const rtgb_render_profile* profile,
-    int active, int row_begin, int row_end) {
+    int active, int row_begin, int row_end, int row_stride) {
     if (!h || !rig || !profile) return RTGB_INVALID_ARGUMENT;
-    return h->r->render_frame(*rig, *profile, active, row_begin, row_end);
+    return h->r->render_frame(*rig, *profile, active, row_begin, row_end, row_stride);
 }
 
 // which: 0 beauty, 1 normal, 2 denoiser_normal, 3 albedo, 4 depth, 5 flow, 6 trust, 7 reservoirs

@@ -105,7 +105,8 @@ class RenderProfile(C.Structure):
 
 
 class CreateInfo(C.Structure):
-    _fields_ = [("device", C.c_int32), ("use_cuda_graph", C.c_int32), ("debug_path_records", C.c_int32)]
+    _fields_ = [("device", C.c_int32), ("use_cuda_graph", C.c_int32), ("debug_path_records", C.c_int32),
+                ("stage_timing", C.c_int32)]
 
 
 class CameraFrameView(C.Structure):
@@ -120,7 +121,8 @@ class FrameViews(C.Structure):
     _fields_ = [("camera_count", C.c_int32), ("cameras", CameraFrameView * MAX_CAMERAS),
                 ("frame_render_ms", C.c_float), ("sample_stream", C.c_uint32), ("rays_traced", C.c_uint64),
                 ("primary_rays", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("restir_visibility_rays", C.c_uint64)]
+                ("restir_visibility_rays", C.c_uint64), ("h2d_bytes", C.c_uint64),
+                ("active_paths", C.c_uint64 * 64), ("restir_pixels", C.c_uint64)]
 
 
 class RestirDiagnostics(C.Structure):
@@ -160,6 +162,7 @@ SIGNATURES = {
     "rtgb_render_frame_async": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32]),
     "rtgb_frame_stats": (C.c_int, [Handle, P(FrameViews)]),
     "rtgb_ray_totals": (C.c_int, [Handle, P(C.c_uint64)]),
+    "rtgb_stage_times": (C.c_int, [Handle, P(C.c_float), C.c_int32, P(C.c_int32)]),
     "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       P(C.c_float)]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),

@@ -218,6 +218,10 @@ struct rtgb_renderer {
     FrameParams* d_fp = nullptr;
     FrameParams h_fp{};
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    bool stage_timing = false;
+    std::vector<cudaEvent_t> stage_events;
+    int stage_count = 0;
+    uint64_t frame_h2d = 0;
     // graph
     cudaGraphExec_t graph_exec = nullptr;
     long long graph_key[4] = {-1, -1, -1, -1};
@@ -247,6 +251,7 @@ struct rtgb_renderer {
             }
         }
         if (h_counters) cudaFreeHost(h_counters);
+        for (cudaEvent_t e : stage_events) cudaEventDestroy(e);
         if (ev_start) cudaEventDestroy(ev_start);
         if (ev_stop) cudaEventDestroy(ev_stop);
         if (stream) cudaStreamDestroy(stream);
@@ -256,6 +261,7 @@ struct rtgb_renderer {
         device = info.device;
         use_graph = info.use_cuda_graph != 0;
         record = info.debug_path_records != 0;
+        stage_timing = info.stage_timing != 0;
         RTGB_CHECK(cudaSetDevice(device));
         RTGB_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         RTGB_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
@@ -692,16 +698,42 @@ struct rtgb_renderer {
         return d;
     }
 
+    // Stage events are recorded as external event nodes, so they also time
+    // each launch inside the replayed graph.
+    void mark(int& k) {
+        if (!stage_timing) return;
+        RTGB_CHECK(cudaEventRecordWithFlags(stage_events[static_cast<size_t>(k)], stream, cudaEventRecordExternal));
+        ++k;
+    }
+
     void enqueue_frame_kernels() {
+        const int mb = h_fp.max_bounces;
+        if (stage_timing) {
+            const size_t need = static_cast<size_t>(3 * mb + 4);
+            while (stage_events.size() < need) {
+                cudaEvent_t e;
+                RTGB_CHECK(cudaEventCreate(&e));
+                stage_events.push_back(e);
+            }
+        }
+        int k = 0;
+        mark(k);
         launch_raygen(d_fp, paths, d_counters, shapes[0], stream);
-        for (int b = 0; b < h_fp.max_bounces; ++b) {
+        mark(k);
+        for (int b = 0; b < mb; ++b) {
             launch_trace(d_fp, scene, paths, d_counters, b, shapes[1], stream);
+            mark(k);
             launch_reset_counters(d_counters, b, stream);
             launch_shade(d_fp, scene, paths, d_counters, b, shapes[2], stream);
+            mark(k);
             launch_shadow(scene, paths, d_counters, shapes[3], stream);
+            mark(k);
         }
         launch_finalize(d_fp, paths, d_counters, shapes[4], stream);
+        mark(k);
         launch_resolve(d_fp, shapes[5], stream);
+        mark(k);
+        stage_count = stage_timing ? k - 1 : 0;
     }
 
     int render(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active, bool sync,
@@ -741,10 +773,12 @@ struct rtgb_renderer {
 
         FrameParams& fp = h_fp;
         std::memset(&fp, 0, sizeof fp);
+        frame_h2d = sizeof(FrameParams);
         for (int c = 0; c < active; ++c) {
             fp.cam[c] = camera_dev(rig.cameras[c], offsets[c], offsets[c] * spp);
             if (bind_camera(c, rig.cameras[c], fp.cam[c])) {
                 launch_camera_dirs(fp.cam[c], const_cast<float4*>(fp.cam[c].dirs), stream);
+                frame_h2d += RTGB_EQUI_LUT_SIZE * sizeof(double);
             }
             fp.prev[c] = prev[c];
             fp.prev_valid[c] = prev_valid[c];
@@ -855,6 +889,9 @@ struct rtgb_renderer {
         out->shadow_rays = k.rays[2];
         out->restir_visibility_rays = k.rays[3];
         out->rays_traced = k.rays[0] + k.rays[1] + k.rays[2] + k.rays[3];
+        out->h2d_bytes = frame_h2d;
+        out->restir_pixels = k.restir_pixels;
+        for (int b = 0; b < last_bounces && b < 64; ++b) out->active_paths[b] = static_cast<uint64_t>(k.bounce_active[b]);
     }
 
     void check_camera(int c) const {
@@ -927,7 +964,7 @@ extern "C" {
 rtgb_status rtgb_create(const rtgb_create_info* info, rtgb_handle* out) {
     if (out == nullptr) return RTGB_INVALID_ARGUMENT;
     *out = nullptr;
-    rtgb_create_info defaults{0, 1, 0};
+    rtgb_create_info defaults{0, 1, 0, 0};
     auto* h = new (std::nothrow) rtgb_renderer();
     if (!h) return RTGB_RUNTIME_ERROR;
     try {
@@ -988,6 +1025,22 @@ rtgb_status rtgb_frame_stats(rtgb_handle h, rtgb_frame_views* out) {
         for (int c = 0; c < h->last_count; ++c) h->fill_view(c, out->cameras[c]);
         h->fill_stats(out);
         return h->h_counters->error != 0 ? RTGB_DEVICE_FAULT_FLAG : RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_stage_times(rtgb_handle h, float* out, int32_t capacity, int32_t* count) {
+    if (!h || !out || !count) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->stage_timing) throw Invalid{"stage times need rtgb_create_info::stage_timing"};
+        if (h->last < 0) throw Invalid{"no frame has been rendered"};
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        const int n = std::min(h->stage_count, capacity);
+        for (int i = 0; i < n; ++i) {
+            RTGB_CHECK(cudaEventElapsedTime(out + i, h->stage_events[static_cast<size_t>(i)],
+                h->stage_events[static_cast<size_t>(i + 1)]));
+        }
+        *count = h->stage_count;
+        return RTGB_OK;
     });
 }
 

@@ -104,6 +104,7 @@ __global__ void __launch_bounds__(256) k_raygen(const FrameParams* __restrict__ 
         counters->rays[1] = 0;
         counters->rays[2] = 0;
         counters->rays[3] = 0;
+        counters->restir_pixels = 0;
     }
 }
 
@@ -112,6 +113,7 @@ __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ f
     Counters* counters, int bounce) {
     const int in = bounce & 1;
     const int count = counters->active[in];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && bounce < 64) counters->bounce_active[bounce] = count;
     int overflow = 0;
     unsigned long long traced = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
@@ -156,6 +158,7 @@ struct ShadeCtx {
     const DeviceScene& s;
     int overflow;
     unsigned long long vis_rays;
+    unsigned long long restir_runs;
 };
 
 RTGB_D float restir_lum(const float3& v) { return fmaxf(0.0f, 0.2126f * v.x + 0.7152f * v.y + 0.0722f * v.z); }
@@ -239,6 +242,7 @@ RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const F
     const FrameParams& fp = ctx.fp;
     const DeviceScene& s = ctx.s;
     if (h.mtype == 3 || s.analytic_count <= 0) return;
+    ++ctx.restir_runs;
     const CameraDev& cam = fp.cam[c];
     Reservoir r = empty_reservoir();
     const int req = fp.restir_candidates > 0 ? fp.restir_candidates : 1;
@@ -349,7 +353,7 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
     const int in = bounce & 1;
     const int out = in ^ 1;
     const int count = counters->active[in];
-    ShadeCtx ctx{fp, s, 0, 0ull};
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const int path = P.queue[in][i];
         const float4 hr = P.hit[path];
@@ -546,6 +550,7 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
         queue_push(P.shadow_queue, &counters->shadow, path, any_shadow);
     }
     count_add(&counters->rays[3], ctx.vis_rays);
+    count_add(&counters->restir_pixels, ctx.restir_runs);
     if (ctx.overflow) atomicAdd(&counters->overflow, ctx.overflow);
 }
 

@@ -50,6 +50,8 @@ struct Counters {
     int overflow;
     int pad[3];
     unsigned long long cum_rays[4];  // running totals since the counters were last cleared
+    int bounce_active[64];           // paths entering each bounce of the last frame
+    unsigned long long restir_pixels; // paths that ran ReSTIR DI in the last frame
 };
 
 struct FrameParams {

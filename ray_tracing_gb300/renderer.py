@@ -38,13 +38,14 @@ class CameraFrame:
 
 
 class Renderer:
-    def __init__(self, device: int = 0, use_cuda_graph: bool = True, debug_path_records: bool = False):
+    def __init__(self, device: int = 0, use_cuda_graph: bool = True, debug_path_records: bool = False,
+                 stage_timing: bool = False):
         self.lib = abi.load()
         missing = getattr(self.lib, "rtgb_missing_symbols", [])
         if missing:
             raise RuntimeError(f"librtgb.so lacks {missing}: rebuild with __graft_entry__.build()")
         self.h = C.c_void_p()
-        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records))
+        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records), int(stage_timing))
         st = self.lib.rtgb_create(C.byref(info), C.byref(self.h))
         if st != abi.OK:
             raise abi.RtgbError(st, "rtgb_create failed (no CUDA device?)")
@@ -96,6 +97,13 @@ class Renderer:
         out = (C.c_uint64 * 4)()
         self._check(self.lib.rtgb_ray_totals(self.h, out), "ray_totals")
         return np.array(list(out), dtype=np.uint64)
+
+    def stage_times(self) -> np.ndarray:
+        """Per-launch device ms of the last frame: raygen, (trace, shade, shadow) per bounce, finalize, resolve."""
+        buf = (C.c_float * 256)()
+        n = C.c_int32()
+        self._check(self.lib.rtgb_stage_times(self.h, buf, 256, C.byref(n)), "stage_times")
+        return np.array(buf[: n.value], dtype=np.float64)
 
     def stream_ptr(self) -> int:
         return int(self.lib.rtgb_stream(self.h) or 0)
