@@ -195,7 +195,9 @@ def run_reference(args, rank, world):
 # ---- GPU arm --------------------------------------------------------------------------
 
 def roofline(stage_ms, frames_stats, spatial):
-    """Picks the launch kind with the largest summed time; returns its roofline record."""
+    """Roofline record of the launch slot (kernel at a bounce) with the largest
+    average time per frame; SURVEY per-unit algorithmic bytes over its
+    CUDA-event durations, against the measured HBM copy bandwidth."""
     peaks = {}
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -203,43 +205,41 @@ def roofline(stage_ms, frames_stats, spatial):
     peak = peaks.get("hbm_gbs")
     peak_note = "of measured" if peak else "of fallback"
     peak = peak or 6800.0
-    kinds = {"raygen": [0.0, 0.0, 0], "trace": [0.0, 0.0, 0], "shade": [0.0, 0.0, 0], "shadow": [0.0, 0.0, 0],
-             "resolve": [0.0, 0.0, 0]}
+    slots = {}
+
+    def add(name, ms, nbytes):
+        v = slots.setdefault(name, [0.0, 0.0, 0])
+        v[0] += ms
+        v[1] += nbytes
+        v[2] += 1
+
     for times, st in zip(stage_ms, frames_stats):
         mb = (len(times) - 3) // 3
-        paths = st["paths"]
-        active = st["active"]
-        kinds["raygen"][0] += times[0]
-        kinds["raygen"][1] += paths * BYTES_RAYGEN
-        kinds["raygen"][2] += 1
+        add("k_raygen", times[0], st["paths"] * BYTES_RAYGEN)
         for b in range(mb):
-            t_tr, t_sh, t_sd = times[1 + 3 * b], times[2 + 3 * b], times[3 + 3 * b]
-            kinds["trace"][0] += t_tr
-            kinds["trace"][1] += active[b] * BYTES_TRACE
-            kinds["trace"][2] += 1
+            act = st["active"][b]
             restir = st["restir_pixels"] * (84 + 84 * (1 + spatial) + 84) if b == 0 else 0
-            kinds["shade"][0] += t_sh
-            kinds["shade"][1] += active[b] * BYTES_SHADE + restir
-            kinds["shade"][2] += 1
-            kinds["shadow"][0] += t_sd
-            kinds["shadow"][2] += 1
-        kinds["shadow"][1] += st["shadow_rays"] * BYTES_SHADOW
-        kinds["resolve"][0] += times[-2] + times[-1]
-        kinds["resolve"][1] += st["pixels"] * BYTES_RESOLVE
-        kinds["resolve"][2] += 1
-    name = max(kinds, key=lambda k: kinds[k][0])
-    ms, nbytes, launches = kinds[name]
+            add(f"k_trace@{b}", times[1 + 3 * b], act * BYTES_TRACE)
+            add(f"k_shade@{b}", times[2 + 3 * b], act * BYTES_SHADE + restir)
+            add(f"k_shadow@{b}", times[3 + 3 * b], st["shadow_rays_per_bounce"][b] * BYTES_SHADOW)
+        add("k_finalize+k_resolve", times[-2] + times[-1], st["pixels"] * BYTES_RESOLVE)
+    name = max(slots, key=lambda k: slots[k][0])
+    ms, nbytes, launches = slots[name]
     achieved = nbytes / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
     traffic = None
     tpath = ROOT / "profiles" / "roofline_traffic.json"
     if tpath.exists():
-        traffic = json.loads(tpath.read_text()).get(f"k_{name}")
-    total = sum(v[0] for v in kinds.values())
-    return {"kernel": f"k_{name}", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        rec = json.loads(tpath.read_text()).get(name)
+        traffic = rec["dram_bytes"] if rec else None
+    frame_ms = sum(v[0] for v in slots.values())
+    by_kernel = {}
+    for k, v in slots.items():
+        by_kernel[k.split("@")[0]] = by_kernel.get(k.split("@")[0], 0.0) + v[0] / max(len(stage_ms), 1)
+    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": traffic, "peak_source": peak_note,
             "avg_launch_ms": ms / max(launches, 1), "algorithmic_bytes_per_launch": nbytes / max(launches, 1),
-            "share_of_frame": ms / total if total > 0 else None,
-            "stage_ms_per_frame": {k: v[0] / max(len(stage_ms), 1) for k, v in kinds.items()}}
+            "share_of_frame": ms / frame_ms if frame_ms > 0 else None,
+            "stage_ms_per_frame": by_kernel}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -279,7 +279,8 @@ def run_ours(args, rank, world, local_rank):
         stage_ms.append(r.stage_times())
         frame_stats.append({"paths": WIDTH * HEIGHT * CAMERAS, "pixels": WIDTH * HEIGHT * CAMERAS,
                             "active": [int(v.active_paths[b]) for b in range(prof.max_bounces)],
-                            "restir_pixels": int(v.restir_pixels), "shadow_rays": int(v.shadow_rays)})
+                            "restir_pixels": int(v.restir_pixels),
+                            "shadow_rays_per_bounce": [int(v.shadow_per_bounce[b]) for b in range(prof.max_bounces)]})
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()

@@ -294,6 +294,7 @@ typedef struct rtgb_frame_views {
     uint64_t h2d_bytes;           /* bytes this frame copied host -> device (frame parameters, camera tables) */
     uint64_t active_paths[64];    /* paths entering each bounce (wavefront queue lengths) */
     uint64_t restir_pixels;       /* bounce-0 paths that ran ReSTIR DI */
+    uint64_t shadow_per_bounce[64]; /* shadow rays traced at each bounce */
 } rtgb_frame_views;
 
 /* RestirDiagnostics, optix_renderer.h:43-51 */
@@ -356,8 +357,9 @@ rtgb_status rtgb_render_frame_async(rtgb_handle handle, const rtgb_camera_rig* r
 rtgb_status rtgb_frame_stats(rtgb_handle handle, rtgb_frame_views* out_views);
 
 /* Per-launch device times (ms) of the last frame, in launch order:
- * raygen, then per bounce trace / shade / shadow, then finalize and resolve
- * (3 * max_bounces + 3 entries). Needs rtgb_create_info::stage_timing. */
+ * raygen, then per bounce trace / shade (+ ReSTIR DI at bounce 0) / shadow,
+ * then finalize and resolve (3 * max_bounces + 3 entries). Needs
+ * rtgb_create_info::stage_timing. */
 rtgb_status rtgb_stage_times(rtgb_handle handle, float* out_ms, int32_t capacity, int32_t* out_count);
 
 /* Rays traced since the scene was prepared: primary, extension, shadow and

@@ -1338,7 +1338,9 @@ struct FrameBuffers {
         depth.assign(n, 0.0f);
         flow.assign(n * 2, 0.0f);
         trust.assign(n, 0.0f);
-        reservoirs.assign(n, Reservoir{});
+        Reservoir zero{};
+        std::memset(&zero, 0, sizeof zero);  // the reference memsets the buffer every launch
+        reservoirs.assign(n, zero);
     }
 };
 

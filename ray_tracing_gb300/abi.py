@@ -122,7 +122,8 @@ class FrameViews(C.Structure):
                 ("frame_render_ms", C.c_float), ("sample_stream", C.c_uint32), ("rays_traced", C.c_uint64),
                 ("primary_rays", C.c_uint64), ("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("restir_visibility_rays", C.c_uint64), ("h2d_bytes", C.c_uint64),
-                ("active_paths", C.c_uint64 * 64), ("restir_pixels", C.c_uint64)]
+                ("active_paths", C.c_uint64 * 64), ("restir_pixels", C.c_uint64),
+                ("shadow_per_bounce", C.c_uint64 * 64)]
 
 
 class RestirDiagnostics(C.Structure):

@@ -114,13 +114,13 @@ RTGB_HD float power_heuristic(float a, float b) {
 // First i with u < cdf[i] (else count-1): an upper-bound binary search over the
 // non-decreasing CDF returns the same index as the reference's linear scan
 // (light_sampling.h:90-116) in O(log n).
-RTGB_D int sample_cdf(const float* __restrict__ cdf, int count, float u) {
+RTGB_D int sample_cdf(const float* cdf, int count, float u) {
     if (count <= 0) return -1;
     const float s = u < 0.0f ? 0.0f : (u < 1.0f ? u : 0.99999994f);
     int lo = 0, hi = count;  // first index in [lo, hi) with s < cdf[i]
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (s < __ldg(cdf + mid)) hi = mid;
+        if (s < cdf[mid]) hi = mid;  // cdf may live in shared or global memory
         else lo = mid + 1;
     }
     return lo < count ? lo : count - 1;
@@ -179,6 +179,17 @@ RTGB_HD Reservoir empty_reservoir() {
     r.bias_correction_source_count = 0;
     r.age = 0;
     r.valid = 0;
+    return r;
+}
+
+// The per-launch cudaMemsetAsync of the reservoir buffer (optix_renderer.cpp:
+// 253-254): every field zero, which is what pixels without ReSTIR keep.
+RTGB_HD Reservoir zero_reservoir() {
+    Reservoir r = empty_reservoir();
+    r.selected.light_index = 0;
+    r.surface.material_type = 0;
+    r.surface.primitive_type = 0;
+    r.surface.primitive_index = 0;
     return r;
 }
 

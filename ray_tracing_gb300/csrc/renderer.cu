@@ -173,7 +173,7 @@ struct rtgb_renderer {
     bool record = false;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
-    LaunchShape shapes[6]{};
+    LaunchShape shapes[7]{};
     std::string error;
 
     // scene
@@ -599,7 +599,7 @@ struct rtgb_renderer {
         const size_t align = 256;
         auto sz = [&](size_t b) { return (b + align - 1) & ~(align - 1); };
         const size_t f4 = sz(static_cast<size_t>(n) * 16), i1 = sz(static_cast<size_t>(n) * 4), i2 = sz(static_cast<size_t>(n) * 8);
-        size_t total = f4 * 15 + i2 + i1 * 5;
+        size_t total = f4 * 15 + i2 + i1 * 6;
         const bool scratch = true;
         if (scratch) total += sz(static_cast<size_t>(n) * sizeof(Reservoir));
         if (need_records) total += sz(static_cast<size_t>(n) * 4 * bounces);
@@ -629,6 +629,7 @@ struct rtgb_renderer {
         P.queue[0] = reinterpret_cast<int*>(take(i1));
         P.queue[1] = reinterpret_cast<int*>(take(i1));
         P.shadow_queue = reinterpret_cast<int*>(take(i1));
+        P.restir_queue = reinterpret_cast<int*>(take(i1));
         P.res_written = reinterpret_cast<int*>(take(i1));
         P.res_scratch = reinterpret_cast<Reservoir*>(take(sz(static_cast<size_t>(n) * sizeof(Reservoir))));
         P.codes = need_records ? reinterpret_cast<int*>(take(sz(static_cast<size_t>(n) * 4 * bounces))) : nullptr;
@@ -725,8 +726,9 @@ struct rtgb_renderer {
             mark(k);
             launch_reset_counters(d_counters, b, stream);
             launch_shade(d_fp, scene, paths, d_counters, b, shapes[2], stream);
+            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes[6], stream);
             mark(k);
-            launch_shadow(scene, paths, d_counters, shapes[3], stream);
+            launch_shadow(scene, paths, d_counters, b, shapes[3], stream);
             mark(k);
         }
         launch_finalize(d_fp, paths, d_counters, shapes[4], stream);
@@ -891,6 +893,7 @@ struct rtgb_renderer {
         out->rays_traced = k.rays[0] + k.rays[1] + k.rays[2] + k.rays[3];
         out->h2d_bytes = frame_h2d;
         out->restir_pixels = k.restir_pixels;
+        for (int b = 0; b < last_bounces && b < 64; ++b) out->shadow_per_bounce[b] = k.shadow_bounce[b];
         for (int b = 0; b < last_bounces && b < 64; ++b) out->active_paths[b] = static_cast<uint64_t>(k.bounce_active[b]);
     }
 

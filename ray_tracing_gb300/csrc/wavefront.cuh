@@ -39,6 +39,7 @@ struct Paths {
     int* res_written;        // per path: 1 when the path wrote res_scratch
     int* queue[2];
     int* shadow_queue;
+    int* restir_queue;       // bounce-0 surfaces waiting for ReSTIR DI
     int* codes;              // optional parity record [path][max_bounces]
 };
 
@@ -52,6 +53,9 @@ struct Counters {
     unsigned long long cum_rays[4];  // running totals since the counters were last cleared
     int bounce_active[64];           // paths entering each bounce of the last frame
     unsigned long long restir_pixels; // paths that ran ReSTIR DI in the last frame
+    int restir;                       // ReSTIR queue length
+    int pad2;
+    unsigned long long shadow_bounce[64];  // shadow rays traced per bounce
 };
 
 struct FrameParams {
@@ -91,13 +95,16 @@ void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
     LaunchShape shape, cudaStream_t stream);
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream);
-void launch_shadow(DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
+void launch_shadow(DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
+    cudaStream_t stream);
+void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
+    cudaStream_t stream);
 void launch_finalize(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
 void launch_resolve(const FrameParams* fp, LaunchShape shape, cudaStream_t stream);
 void launch_direction_debug(const CameraDev& cam, uint8_t* rgba, cudaStream_t stream);
 void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
 // Persistent grid sizes: SM count x resident blocks per SM for raygen, trace,
-// shade, shadow, finalize and resolve.
+// shade, shadow, finalize, resolve and restir.
 void query_launch_shapes(int sm_count, LaunchShape* shapes);
 void launch_tonemap(const float4* beauty, uint8_t* rgba, long long pixels, cudaStream_t stream);
 
