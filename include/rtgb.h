@@ -96,6 +96,54 @@ typedef struct rtgb_material {
     int32_t openpbr_index;
 } rtgb_material;
 
+/* OpenPbrCompiledMaterial, src/common/openpbr_core.h:33-122: the OpenPBR
+ * parameter block (OpenPbrCoreMaterial, field for field) followed by the
+ * texture bindings. A texture index < 0 means "use the parameter". Color
+ * bindings carry the source color space (0 raw, 1 linear sRGB, 2 sRGB
+ * texture: decoded with the sRGB transfer curve). */
+typedef struct rtgb_openpbr_material {
+    float base_weight;
+    float base_color[3];
+    float base_diffuse_roughness;
+    float base_metalness;
+    float specular_weight;
+    float specular_color[3];
+    float specular_roughness;
+    float specular_ior;
+    float specular_roughness_anisotropy;
+    float transmission_weight;
+    float transmission_color[3];
+    float transmission_depth;
+    float transmission_dispersion_scale;
+    float transmission_dispersion_abbe_number;
+    float subsurface_weight;
+    float subsurface_color[3];
+    float subsurface_radius;
+    float subsurface_radius_scale[3];
+    float subsurface_scatter_anisotropy;
+    float fuzz_weight;
+    float fuzz_color[3];
+    float fuzz_roughness;
+    float coat_weight;
+    float coat_color[3];
+    float coat_roughness;
+    float coat_roughness_anisotropy;
+    float coat_ior;
+    float coat_darkening;
+    float thin_film_weight;
+    float thin_film_thickness;      /* micrometres */
+    float thin_film_ior;
+    float emission_luminance;
+    float emission_color[3];
+    float geometry_opacity;
+    int32_t geometry_thin_walled;
+    /* color bindings: base, specular, transmission, emission */
+    int32_t color_texture[4];
+    int32_t color_space[4];
+    /* scalar bindings: base_metalness, specular_roughness (texture's red channel) */
+    int32_t scalar_texture[2];
+} rtgb_openpbr_material;
+
 /* PackedSphere, launch_params.h:135-141 */
 typedef struct rtgb_sphere {
     float center[3];
@@ -185,6 +233,8 @@ typedef struct rtgb_scene {
     const rtgb_analytic_light* analytic_lights;
     int32_t analytic_light_count;
     float background[3];
+    const rtgb_openpbr_material* openpbr_materials;   /* rtgb_material::openpbr_index */
+    int32_t openpbr_material_count;
 } rtgb_scene;
 
 /* ------------------------------------------------------------------------ */

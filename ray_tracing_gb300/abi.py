@@ -34,6 +34,57 @@ class Material(C.Structure):
                 ("fuzz", C.c_float), ("type", C.c_int32), ("openpbr_index", C.c_int32)]
 
 
+OPENPBR_PARAMS = [
+    ("base_weight", 1), ("base_color", 3), ("base_diffuse_roughness", 1), ("base_metalness", 1),
+    ("specular_weight", 1), ("specular_color", 3), ("specular_roughness", 1), ("specular_ior", 1),
+    ("specular_roughness_anisotropy", 1), ("transmission_weight", 1), ("transmission_color", 3),
+    ("transmission_depth", 1), ("transmission_dispersion_scale", 1), ("transmission_dispersion_abbe_number", 1),
+    ("subsurface_weight", 1), ("subsurface_color", 3), ("subsurface_radius", 1), ("subsurface_radius_scale", 3),
+    ("subsurface_scatter_anisotropy", 1), ("fuzz_weight", 1), ("fuzz_color", 3), ("fuzz_roughness", 1),
+    ("coat_weight", 1), ("coat_color", 3), ("coat_roughness", 1), ("coat_roughness_anisotropy", 1),
+    ("coat_ior", 1), ("coat_darkening", 1), ("thin_film_weight", 1), ("thin_film_thickness", 1),
+    ("thin_film_ior", 1), ("emission_luminance", 1), ("emission_color", 3), ("geometry_opacity", 1),
+]
+
+# OpenPbrCoreMaterial defaults (src/common/openpbr_core.h:33-77)
+OPENPBR_DEFAULTS = {
+    "base_weight": 1.0, "base_color": (0.8, 0.8, 0.8), "base_diffuse_roughness": 0.0, "base_metalness": 0.0,
+    "specular_weight": 1.0, "specular_color": (1.0, 1.0, 1.0), "specular_roughness": 0.3, "specular_ior": 1.5,
+    "specular_roughness_anisotropy": 0.0, "transmission_weight": 0.0, "transmission_color": (1.0, 1.0, 1.0),
+    "transmission_depth": 0.0, "transmission_dispersion_scale": 0.0, "transmission_dispersion_abbe_number": 20.0,
+    "subsurface_weight": 0.0, "subsurface_color": (0.8, 0.8, 0.8), "subsurface_radius": 1.0,
+    "subsurface_radius_scale": (1.0, 0.5, 0.25), "subsurface_scatter_anisotropy": 0.0, "fuzz_weight": 0.0,
+    "fuzz_color": (1.0, 1.0, 1.0), "fuzz_roughness": 0.5, "coat_weight": 0.0, "coat_color": (1.0, 1.0, 1.0),
+    "coat_roughness": 0.0, "coat_roughness_anisotropy": 0.0, "coat_ior": 1.6, "coat_darkening": 1.0,
+    "thin_film_weight": 0.0, "thin_film_thickness": 0.5, "thin_film_ior": 1.4, "emission_luminance": 0.0,
+    "emission_color": (1.0, 1.0, 1.0), "geometry_opacity": 1.0, "geometry_thin_walled": 0,
+}
+
+
+class OpenPbrMaterial(C.Structure):
+    _fields_ = ([(n, C.c_float if k == 1 else f3) for n, k in OPENPBR_PARAMS]
+                + [("geometry_thin_walled", C.c_int32), ("color_texture", C.c_int32 * 4),
+                   ("color_space", C.c_int32 * 4), ("scalar_texture", C.c_int32 * 2)])
+
+    @classmethod
+    def make(cls, **kw) -> "OpenPbrMaterial":
+        """Material with the reference defaults, overridden by `kw`; all textures unbound."""
+        m = cls()
+        vals = dict(OPENPBR_DEFAULTS)
+        vals.update(kw)
+        for name, value in vals.items():
+            if name in ("color_texture", "color_space", "scalar_texture"):
+                continue
+            if isinstance(value, (tuple, list)):
+                getattr(m, name)[:] = [float(v) for v in value]
+            else:
+                setattr(m, name, value)
+        m.color_texture[:] = list(kw.get("color_texture", (-1, -1, -1, -1)))
+        m.color_space[:] = list(kw.get("color_space", (1, 1, 1, 1)))
+        m.scalar_texture[:] = list(kw.get("scalar_texture", (-1, -1)))
+        return m
+
+
 class Sphere(C.Structure):
     _fields_ = [("center", f3), ("radius", C.c_float), ("material_index", C.c_int32)]
 
@@ -71,7 +122,8 @@ class Scene(C.Structure):
                 ("triangles", C.POINTER(Triangle)), ("triangle_count", C.c_int32),
                 ("media", C.POINTER(Medium)), ("medium_count", C.c_int32),
                 ("analytic_lights", C.POINTER(AnalyticLight)), ("analytic_light_count", C.c_int32),
-                ("background", f3)]
+                ("background", f3),
+                ("openpbr_materials", C.POINTER(OpenPbrMaterial)), ("openpbr_material_count", C.c_int32)]
 
 
 class Pinhole32(C.Structure):

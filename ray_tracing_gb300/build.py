@@ -90,11 +90,11 @@ def build_product(jobs: int | None = None, verbose: bool = False) -> Path:
 
 def build_oracle() -> Path:
     ORACLE_LIB.parent.mkdir(exist_ok=True)
-    srcs = [ORACLE_DIR / "radiance_oracle.cpp"]
-    deps = srcs + [ORACLE_DIR / "oracle_math.h", INCLUDE / "rtgb.h"]
+    srcs = [ORACLE_DIR / "radiance_oracle.cpp", ORACLE_DIR / "openpbr_kat.cpp"]
+    deps = srcs + [ORACLE_DIR / "oracle_math.h", INCLUDE / "rtgb.h", CSRC / "openpbr.h"]
     if _stale(ORACLE_LIB, deps):
         _run(["g++", "-O2", "-std=c++20", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-              "-I", str(INCLUDE), *map(str, srcs), "-o", str(ORACLE_LIB), "-lpthread"])
+              "-I", str(INCLUDE), "-I", str(CSRC), *map(str, srcs), "-o", str(ORACLE_LIB), "-lpthread"])
     return ORACLE_LIB
 
 
