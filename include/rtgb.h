@@ -507,6 +507,30 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
 /* RenderProfile::quality/balanced/realtime (render_profile.h:27-63). */
 rtgb_status rtgb_profile_preset(const char* name, rtgb_render_profile* out_profile);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free LBVH build. No counterpart in the reference.              */
+/* ------------------------------------------------------------------------ */
+#define RTGB_STATIC_LBVH_MAX_PRIMITIVES 131072
+
+/* The device LBVH build of rtgb_prepare_scene over caller-owned boxes, with all
+ * scratch carved from one fixed device array compiled into the library, so
+ * the call never allocates device or host memory. Same outputs as
+ * rtgb_download_lbvh for the same boxes.
+ *   aabb_lo/aabb_hi   device, 4 floats per primitive (x, y, z, unused), 16-byte aligned
+ *   sorted_morton     device, primitive_count words
+ *   sorted_primitive  device, primitive_count words (sorted slot -> input index)
+ *   node_children     device, 2 per internal node (a negative child c is sorted slot ~c)
+ *   nodes             device, 16 floats per internal node (child boxes inline), 16-byte aligned
+ *   stream            cudaStream_t of `device` (0: legacy default stream)
+ *   message           optional caller buffer for the error text
+ * 2 <= primitive_count <= RTGB_STATIC_LBVH_MAX_PRIMITIVES, else RTGB_INVALID_ARGUMENT.
+ * The first call on a device looks up the array's address there; make it
+ * before any stream capture. Calls overlapping in time share the one array
+ * and race: serialise them. Asynchronous on `stream`. */
+rtgb_status rtgb_build_lbvh_static(int32_t device, const float* aabb_lo, const float* aabb_hi,
+    int32_t primitive_count, uint32_t* sorted_morton, int32_t* sorted_primitive, int32_t* node_children,
+    float* nodes, void* stream, char* message, size_t message_size);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

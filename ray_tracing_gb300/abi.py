@@ -236,7 +236,11 @@ SIGNATURES = {
     "rtgb_pack_camera_pose": (C.c_int, [P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]),
     "rtgb_default_rig": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, P(CameraRig)]),
     "rtgb_profile_preset": (C.c_int, [C.c_char_p, P(RenderProfile)]),
+    "rtgb_build_lbvh_static": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_size_t]),
 }
+
+STATIC_LBVH_MAX_PRIMITIVES = 131072
 
 _lib = None
 
