@@ -454,8 +454,12 @@ void* rtgb_stream(rtgb_handle handle);
 
 /* Parity support (only with rtgb_create_info::debug_path_records).
  * Per path (pixel-major, then sample) and bounce: hit code
- *   -1 miss, (k << 28) | index with k = 0 sphere, 1 quad, 2 triangle,
- *   4 medium, 5 analytic light; and the path's final radiance (float3).
+ *   -1 miss, (k << 28) | (decisions << 22) | index with k = 0 sphere, 1 quad,
+ *   2 triangle, 4 medium, 5 analytic light; decisions: bit 0 emissive NEE
+ *   visible, bit 1 analytic/ReSTIR NEE visible, bits 2-5 the OpenPBR scatter
+ *   event (1-9, 10 = random-walk scattering inside the medium); indexes of
+ *   2^22 and above share bits with the decisions. And the path's final
+ *   radiance (float3).
  * `paths` must equal the frame's total path count. */
 rtgb_status rtgb_download_path_records(rtgb_handle handle, int32_t camera_index,
     int32_t* hit_codes, int32_t max_bounces, float* radiance_rgb, int64_t paths);

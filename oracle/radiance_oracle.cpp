@@ -14,9 +14,15 @@
 // src/realtime/gpu/gpu_scene_acceleration.cpp:145-179, traversed as in
 // programs.cu:1619-1652). Both give the same closest hit up to equal-t ties.
 //
+// OpenPBR materials run through ray_tracing_gb300/csrc/openpbr.h, the same
+// host/device header the CUDA path uses (as the reference shares
+// src/common/openpbr_core.h); that header is pinned word for word to the
+// reference's by tests/test_openpbr_kats.py.
+//
 // Compiled with -ffp-contract=off; multi-draw RNG calls evaluate left to right.
 #include "../include/rtgb.h"
 #include "oracle_math.h"
+#include "openpbr.h"
 
 #include <algorithm>
 #include <atomic>
@@ -32,6 +38,8 @@ namespace {
 constexpr float kRayEpsilon = 1e-3f;
 constexpr float kRayFar = 1e30f;
 constexpr double kCameraEpsilon = 1e-12;
+
+namespace pbr = rtgb::pbr;
 
 struct Ray {
     V3 origin;
@@ -79,7 +87,19 @@ struct PathState {
     bool prev_delta = true;
     Ray ray{};
     bool alive = true;
+    pbr::Medium subsurface{};       // OpenPBR random-walk medium the path is inside
+    int subsurface_material = -1;   // its OpenPBR material index
+    int decisions = 0;              // this bounce's discrete outcomes, for the parity record
 };
+
+// Parity record of one bounce: (k << 28) | (decisions << 22) | index, where the
+// decisions are bit 0 emissive NEE visible, bit 1 analytic (or ReSTIR) NEE
+// visible, bits 2-5 the scatter event (OpenPBR sample event 1-9, 10 a
+// random-walk scattering inside the medium, 0 otherwise).
+constexpr int kDecisionShift = 22;
+constexpr int kDecisionNeeEmissive = 1;
+constexpr int kDecisionNeeAnalytic = 2;
+constexpr int kDecisionWalk = 10;
 
 struct LightSample {
     V3 position{0, 0, 0};
@@ -140,6 +160,7 @@ struct Scene {
     std::vector<rtgb_triangle> triangles;
     std::vector<rtgb_medium> media;
     std::vector<rtgb_analytic_light> analytic;
+    std::vector<rtgb_openpbr_material> openpbr;
     std::vector<PackedLight> lights;
     V3 background{0, 0, 0};
     bool use_bvh = false;
@@ -174,11 +195,28 @@ V3 average_texture(const Scene& s, int index, int depth) {
     return {0, 0, 0};
 }
 
+pbr::V3 pv(const V3& v) { return pbr::V3{v.x, v.y, v.z}; }
+V3 fv(const pbr::V3& v) { return V3{v.x, v.y, v.z}; }
+
+// The OpenPBR parameter block is the first 204 bytes of rtgb_openpbr_material.
+pbr::Mat openpbr_parameters(const rtgb_openpbr_material& c) {
+    pbr::Mat m;
+    std::memcpy(&m, &c, sizeof m);
+    return m;
+}
+
+// material_emission_luminance, packed_scene_preparation.cpp:227-251
 float emission_luminance(const Scene& s, int material_index) {
     if (material_index < 0 || material_index >= static_cast<int>(s.materials.size())) return 0.0f;
     const rtgb_material& m = s.materials[static_cast<size_t>(material_index)];
     if (m.type == 3) return luminance(average_texture(s, m.emission_texture, 0));
-    return 0.0f;  // OpenPBR emission is not part of this oracle
+    if (m.type != 5 || m.openpbr_index < 0 || m.openpbr_index >= static_cast<int>(s.openpbr.size())) return 0.0f;
+    const rtgb_openpbr_material& c = s.openpbr[static_cast<size_t>(m.openpbr_index)];
+    pbr::Mat params = openpbr_parameters(c);
+    if (c.color_texture[3] >= 0) {
+        pbr::apply_color(params, 3, pv(average_texture(s, c.color_texture[3], 0)), c.color_space[3]);
+    }
+    return pbr::luminance(pbr::emission(params));
 }
 
 void build_light_distribution(Scene& s) {
@@ -824,11 +862,55 @@ public:
         }
         if (h.material_type == 3 && !h.front_face) h.emission = {0, 0, 0};
         if (h.material_type != 3) h.emission = {0, 0, 0};
-        if (h.material_type == 5) {  // no OpenPBR table in this oracle: unresolved material
-            h.material_type = -1;
-            h.base_color = {0, 0, 0};
-            h.emission = {0, 0, 0};
+        if (h.material_type == 5) {
+            const rtgb_openpbr_material* c = openpbr_material(m.openpbr_index);
+            if (c == nullptr) {
+                h.material_type = -1;
+                h.base_color = {0, 0, 0};
+                h.emission = {0, 0, 0};
+                return;
+            }
+            pbr::Mat params = openpbr_parameters(*c);
+            apply_color_binding(params, *c, 0, h.tex_u, h.tex_v, h.position);
+            apply_color_binding(params, *c, 3, h.tex_u, h.tex_v, h.position);
+            h.base_color = fv(params.base_color);
+            h.emission = fv(pbr::emission(params));
         }
+    }
+
+    // resolve_openpbr_material, programs.cu:909-921
+    const rtgb_openpbr_material* openpbr_material(int index) const {
+        if (index < 0 || index >= static_cast<int>(s_.openpbr.size())) return nullptr;
+        return &s_.openpbr[static_cast<size_t>(index)];
+    }
+
+    // evaluate_openpbr_color_binding, programs.cu:923-932 (input: 0 base, 1 specular,
+    // 2 transmission, 3 emission color)
+    void apply_color_binding(pbr::Mat& params, const rtgb_openpbr_material& c, int input, float u, float v,
+        const V3& p) const {
+        if (c.color_texture[input] < 0) return;
+        pbr::apply_color(params, input, pv(eval_texture(s_, c.color_texture[input], u, v, p)), c.color_space[input]);
+    }
+
+    // evaluate_openpbr_scattering_material, programs.cu:944-960
+    pbr::Mat scattering_parameters(const Hit& h) const {
+        const rtgb_openpbr_material& c = *openpbr_material(h.openpbr_index);
+        pbr::Mat params = openpbr_parameters(c);
+        if (c.color_texture[0] >= 0) params.base_color = pv(h.base_color);
+        apply_color_binding(params, c, 1, h.tex_u, h.tex_v, h.position);
+        apply_color_binding(params, c, 2, h.tex_u, h.tex_v, h.position);
+        for (int k = 0; k < 2; ++k) {
+            if (c.scalar_texture[k] >= 0) {
+                pbr::apply_scalar(params, k, eval_texture(s_, c.scalar_texture[k], h.tex_u, h.tex_v, h.position).x);
+            }
+        }
+        return params;
+    }
+
+    static pbr::Context transport_context(const PathState& st) {
+        pbr::Context ctx = pbr::default_context();
+        ctx.throughput = pv(st.throughput);
+        return ctx;
     }
 
     static bool try_sphere(const rtgb_sphere& sp, const Ray& ray, float tmin, float tmax, Hit& h) {
@@ -1077,14 +1159,31 @@ public:
 
     // ---- shading: programs.cu:1011-1354 ----------------------------------
 
+    // evaluate_material_emission, programs.cu:1011-1024
     V3 material_emission(const rtgb_material& m, float u, float v, const V3& p) const {
-        if (m.type == 5) return {0, 0, 0};
+        if (m.type == 5) {
+            const rtgb_openpbr_material* c = openpbr_material(m.openpbr_index);
+            if (c == nullptr) return {0, 0, 0};
+            pbr::Mat params = openpbr_parameters(*c);
+            apply_color_binding(params, *c, 3, u, v, p);
+            return fv(pbr::emission(params));
+        }
         return eval_texture(s_, m.emission_texture, u, v, p);
     }
 
+    // direct_material_response, programs.cu:1026-1055
     V3 direct_response(const Hit& h, const PathState& st, const V3& ldir, float& bsdf_pdf) const {
-        (void)st;
         bsdf_pdf = 0.0f;
+        if (h.material_type == 5) {
+            if (openpbr_material(h.openpbr_index) == nullptr) return {0, 0, 0};
+            const pbr::Mat params = scattering_parameters(h);
+            const pbr::Frame frame = pbr::make_frame(pv(h.geometric_normal), pbr::V3{0.0f, 0.0f, 0.0f});
+            const pbr::Eval e = pbr::evaluate(params, frame, pv(mul(normalize(st.ray.direction), -1.0f)), pv(ldir),
+                transport_context(st));
+            const float cosine = std::fabs(dot(h.shading_normal, ldir));
+            bsdf_pdf = e.pdf;
+            return mul(fv(e.value), cosine);
+        }
         if (h.material_type == 0) {
             const float c = std::fmax(dot(h.shading_normal, ldir), 0.0f);
             bsdf_pdf = c / kPi;
@@ -1385,6 +1484,9 @@ public:
         scene_.triangles.assign(sc.triangles, sc.triangles + sc.triangle_count);
         scene_.media.assign(sc.media, sc.media + sc.medium_count);
         scene_.analytic.assign(sc.analytic_lights, sc.analytic_lights + sc.analytic_light_count);
+        if (sc.openpbr_materials != nullptr && sc.openpbr_material_count > 0) {
+            scene_.openpbr.assign(sc.openpbr_materials, sc.openpbr_materials + sc.openpbr_material_count);
+        }
         scene_.background = from3(sc.background);
         scene_.use_bvh = use_bvh;
         build_light_distribution(scene_);
@@ -1663,6 +1765,7 @@ private:
         if (max_t <= kRayEpsilon) return;
         ++rays;
         if (tracer_.occluded(shadow, max_t)) return;
+        st.decisions |= kDecisionNeeAnalytic;
         st.radiance = add(st.radiance, mul(st.throughput, mul(num, r.estimator_weight)));
     }
 
@@ -1680,6 +1783,7 @@ private:
         if (tracer_.occluded(shadow, max_t)) return;
         const float mis = bsdf_avail ? power_heuristic(l.pdf, bp) : 1.0f;
         const V3 direct = mul(mul(l.emission, resp), mis / l.pdf);
+        st.decisions |= kDecisionNeeEmissive;
         st.radiance = add(st.radiance, mul(st.throughput, direct));
     }
 
@@ -1700,6 +1804,7 @@ private:
         if (tracer_.occluded(shadow, max_t)) return;
         const float mis = l.delta || !bsdf_avail ? 1.0f : power_heuristic(l.pdf, bp);
         const V3 direct = mul(mul(l.emission, resp), mis / l.pdf);
+        st.decisions |= kDecisionNeeAnalytic;
         st.radiance = add(st.radiance, mul(st.throughput, direct));
     }
 
@@ -1714,8 +1819,8 @@ private:
         st.prev_delta = delta;
     }
 
-    // sample_bsdf, programs.cu:2463-2565 (legacy materials)
-    static void sample_bsdf(const Hit& h, uint32_t& rng, PathState& st) {
+    // sample_bsdf, programs.cu:2463-2565
+    void sample_bsdf(const Hit& h, uint32_t& rng, PathState& st) const {
         if (!st.alive) return;
         if (h.material_type == 3) {
             st.alive = false;
@@ -1766,6 +1871,37 @@ private:
             record_scatter(st, h, 0.0f, true);
             return;
         }
+        if (h.material_type == 5) {
+            if (tracer_.openpbr_material(h.openpbr_index) == nullptr) {
+                st.alive = false;
+                return;
+            }
+            const pbr::Mat params = tracer_.scattering_parameters(h);
+            const pbr::Frame frame = pbr::make_frame(pv(h.geometric_normal), pbr::V3{0.0f, 0.0f, 0.0f});
+            const float u_lobe = rnd(rng);
+            const float u1 = rnd(rng);
+            const float u2 = rnd(rng);
+            const pbr::Sample smp = pbr::sample(params, frame, pv(mul(normalize(st.ray.direction), -1.0f)), u_lobe, u1,
+                u2, Tracer::transport_context(st));
+            if (smp.valid == 0) {
+                st.alive = false;
+                return;
+            }
+            const V3 d = fv(smp.wi);
+            st.ray.origin = add(h.position, mul(d, kRayEpsilon));
+            st.ray.direction = normalize(d);
+            st.throughput = mul(st.throughput, fv(smp.weight));
+            st.decisions |= smp.event << 2;
+            record_scatter(st, h, smp.pdf, smp.delta != 0);
+            if (smp.event == pbr::kSubsurfaceEntry) {
+                st.subsurface = pbr::subsurface_medium(params);
+                st.subsurface_material = h.openpbr_index;
+            } else if (smp.event == pbr::kSubsurfaceExit) {
+                st.subsurface = pbr::Medium{};
+                st.subsurface_material = -1;
+            }
+            return;
+        }
         if (h.material_type == 4) {
             const V3 d = random_unit_vector(rng);
             st.ray.origin = add(h.position, mul(d, kRayEpsilon));
@@ -1802,7 +1938,11 @@ private:
             if (!p.state->codes.empty()) {
                 codes = &p.state->codes[(static_cast<size_t>(pixel) * static_cast<size_t>(spp) + static_cast<size_t>(s)) * static_cast<size_t>(mb)];
             }
+            int last_b = -1;
             for (int b = 0; b < mb && st.alive; ++b) {
+                if (codes && last_b >= 0) codes[last_b] |= st.decisions << kDecisionShift;
+                st.decisions = 0;
+                last_b = b;
                 ++rays;
                 Hit h = tracer_.intersect(st.ray, kRayEpsilon, kRayFar, &rng);
                 const AnalyticHit ah = tracer_.intersect_analytic(st.ray, kRayEpsilon, h.hit ? h.t : kRayFar);
@@ -1820,6 +1960,29 @@ private:
                     st.radiance = add(st.radiance, mul(st.throughput, tracer_.analytic_infinite_radiance(st)));
                     st.alive = false;
                     break;
+                }
+                // OpenPBR random-walk segment inside the entered material (programs.cu:1878-1902)
+                if (st.subsurface.active != 0) {
+                    if (h.material_type != 5 || h.openpbr_index != st.subsurface_material || h.front_face) {
+                        st.alive = false;
+                        break;
+                    }
+                    const float ray_len = std::sqrt(len_sq(st.ray.direction));
+                    const pbr::Segment seg = pbr::subsurface_segment(st.subsurface, h.t * ray_len, rnd(rng),
+                        Tracer::transport_context(st));
+                    st.throughput = mul(st.throughput, fv(seg.weight));
+                    if (seg.scattered != 0) {
+                        const V3 incident = normalize(st.ray.direction);
+                        const float g1 = rnd(rng);
+                        const float g2 = rnd(rng);
+                        const V3 dir = fv(pbr::sample_hg(pv(incident), st.subsurface.anisotropy, g1, g2));
+                        st.ray.origin = add(st.ray.origin, mul(st.ray.direction, seg.distance / std::fmax(ray_len, 1e-8f)));
+                        st.ray.direction = dir;
+                        st.ray.origin = add(st.ray.origin, mul(st.ray.direction, kRayEpsilon));
+                        st.prev_valid = false;
+                        st.decisions |= kDecisionWalk << 2;
+                        continue;
+                    }
                 }
                 if (!captured && b == 0) {
                     sn = h.shading_normal;
@@ -1851,6 +2014,7 @@ private:
                     }
                 }
             }
+            if (codes && last_b >= 0) codes[last_b] |= st.decisions << kDecisionShift;
             beauty = add(beauty, st.radiance);
             if (!p.state->path_radiance.empty()) {
                 float* pr = &p.state->path_radiance[(static_cast<size_t>(pixel) * static_cast<size_t>(spp) + static_cast<size_t>(s)) * 3];

@@ -337,6 +337,8 @@ struct DeviceScene {
     int analytic_node_count;
     const int* infinite_analytic;   // distant/dome light indices, reference order
     int infinite_analytic_count;
+    const rtgb_openpbr_material* openpbr;  // compiled OpenPBR materials (rtgb_material::openpbr_index)
+    int openpbr_count;
     float background[3];
 };
 

@@ -25,6 +25,7 @@ struct rtgb_host_scene {
     std::vector<rtgb_triangle> triangles;
     std::vector<rtgb_medium> media;
     std::vector<rtgb_analytic_light> analytic;
+    std::vector<rtgb_openpbr_material> openpbr;
     std::array<float, 3> background {0.0f, 0.0f, 0.0f};
 };
 
@@ -106,6 +107,30 @@ public:
         m.openpbr_index = -1;
         s_.materials.push_back(m);
         return static_cast<int>(s_.materials.size()) - 1;
+    }
+    // Image texture over texels appended to the scene's texel array (RGB rows).
+    int image_texture(int width, int height, const std::vector<float>& rgb) {
+        rtgb_texture t {};
+        t.type = RTGB_TEXTURE_IMAGE;
+        t.even_texture = -1;
+        t.odd_texture = -1;
+        t.image_offset = static_cast<int32_t>(s_.texels.size() / 3);
+        t.image_width = width;
+        t.image_height = height;
+        t.u_address_mode = 2;
+        t.v_address_mode = 2;
+        t.filter_type = 1;
+        t.scale = 1.0f;
+        s_.texels.insert(s_.texels.end(), rgb.begin(), rgb.end());
+        s_.textures.push_back(t);
+        return static_cast<int>(s_.textures.size()) - 1;
+    }
+    // An OpenPBR material (OpenPbrMaterialDesc) and its compiled parameter block.
+    int openpbr(const rtgb_openpbr_material& om) {
+        s_.openpbr.push_back(om);
+        const int m = material(RTGB_MATERIAL_OPENPBR, -1, -1, 1.0, 0.0);
+        s_.materials[static_cast<size_t>(m)].openpbr_index = static_cast<int32_t>(s_.openpbr.size()) - 1;
+        return m;
     }
     // add_diffuse_color / add_emissive_color (shared_scene_builders.cpp:41-53)
     int diffuse(const Vec3& c) { return material(RTGB_MATERIAL_LAMBERTIAN, constant_texture(c), -1, 1.0, 0.0); }
@@ -362,6 +387,227 @@ void build_random_spheres(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
     b.background({0.02, 0.025, 0.04});
 }
 
+// OpenPbrCoreMaterial defaults (src/common/openpbr_core.h:33-77), all
+// textures unbound, color bindings in linear sRGB.
+rtgb_openpbr_material openpbr_defaults() {
+    rtgb_openpbr_material m {};
+    auto c3 = [](float* d, float x, float y, float z) {
+        d[0] = x;
+        d[1] = y;
+        d[2] = z;
+    };
+    m.base_weight = 1.0f;
+    c3(m.base_color, 0.8f, 0.8f, 0.8f);
+    m.specular_weight = 1.0f;
+    c3(m.specular_color, 1.0f, 1.0f, 1.0f);
+    m.specular_roughness = 0.3f;
+    m.specular_ior = 1.5f;
+    c3(m.transmission_color, 1.0f, 1.0f, 1.0f);
+    m.transmission_dispersion_abbe_number = 20.0f;
+    c3(m.subsurface_color, 0.8f, 0.8f, 0.8f);
+    m.subsurface_radius = 1.0f;
+    c3(m.subsurface_radius_scale, 1.0f, 0.5f, 0.25f);
+    c3(m.fuzz_color, 1.0f, 1.0f, 1.0f);
+    m.fuzz_roughness = 0.5f;
+    c3(m.coat_color, 1.0f, 1.0f, 1.0f);
+    m.coat_ior = 1.6f;
+    m.coat_darkening = 1.0f;
+    m.thin_film_thickness = 0.5f;
+    m.thin_film_ior = 1.4f;
+    c3(m.emission_color, 1.0f, 1.0f, 1.0f);
+    m.geometry_opacity = 1.0f;
+    for (int k = 0; k < 4; ++k) {
+        m.color_texture[k] = -1;
+        m.color_space[k] = 1;
+    }
+    m.scalar_texture[0] = -1;
+    m.scalar_texture[1] = -1;
+    return m;
+}
+
+// OpenPBR material gallery: a row of spheres, one per feature of the OpenPBR
+// BSDF (F82 metal, smooth and rough glass, thin-walled glass, dispersion, thin
+// film, coat, fuzz, random-walk and thin-walled subsurface, cut-out opacity,
+// texture-bound roughness/metalness/specular color), on an OpenPBR floor with
+// an sRGB checker base color, lit by an OpenPBR emissive quad and sphere (the
+// sphere's emission color texture-bound) and `detail` analytic sphere lights
+// (default 24) for ReSTIR DI. Camera slot 0 of the default rig looks at it.
+void build_openpbr_gallery(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
+    Builder b(s);
+    SplitMix rng(0x09e7b7c0ull ^ seed);
+    auto base = [](float r, float g, float bl) {
+        rtgb_openpbr_material m = openpbr_defaults();
+        m.base_color[0] = r;
+        m.base_color[1] = g;
+        m.base_color[2] = bl;
+        return m;
+    };
+    // floor: OpenPBR dielectric with an sRGB-encoded checker base color
+    {
+        rtgb_openpbr_material m = base(0.5f, 0.5f, 0.5f);
+        m.base_diffuse_roughness = 0.5f;
+        m.specular_roughness = 0.45f;
+        m.color_texture[0] = b.checker_texture(0.5, b.constant_texture({0.85, 0.82, 0.75}), b.constant_texture({0.25, 0.3, 0.35}));
+        m.color_space[0] = 2;
+        // 1 cm below the spheres: a solid checker flips sign on the plane y = 0,
+        // where the cell of a hit would hang on the last bit of its position
+        b.quad(b.openpbr(m), {-8.0, -0.01, -2.0}, {16.0, 0.0, 0.0}, {0.0, 0.0, 14.0});
+    }
+    b.quad(b.diffuse({0.6, 0.55, 0.5}), {-8.0, 0.0, 9.0}, {16.0, 0.0, 0.0}, {0.0, 5.0, 0.0});
+    std::vector<rtgb_openpbr_material> row;
+    {
+        rtgb_openpbr_material m = base(1.0f, 0.78f, 0.34f);  // gold, F82 tint
+        m.base_metalness = 1.0f;
+        m.specular_roughness = 0.25f;
+        m.specular_color[2] = 0.6f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(1.0f, 1.0f, 1.0f);  // smooth glass
+        m.transmission_weight = 1.0f;
+        m.specular_roughness = 0.0f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(1.0f, 1.0f, 1.0f);  // rough tinted glass
+        m.transmission_weight = 1.0f;
+        m.specular_roughness = 0.3f;
+        m.transmission_color[0] = 0.6f;
+        m.transmission_color[1] = 0.9f;
+        m.transmission_color[2] = 0.8f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(1.0f, 1.0f, 1.0f);  // thin-walled glass
+        m.transmission_weight = 1.0f;
+        m.specular_roughness = 0.1f;
+        m.geometry_thin_walled = 1;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(1.0f, 1.0f, 1.0f);  // dispersive glass
+        m.transmission_weight = 1.0f;
+        m.specular_roughness = 0.0f;
+        m.specular_ior = 1.7f;
+        m.transmission_dispersion_scale = 1.0f;
+        m.transmission_dispersion_abbe_number = 18.0f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.05f, 0.05f, 0.08f);  // thin-film soap-bubble dielectric
+        m.thin_film_weight = 1.0f;
+        m.thin_film_thickness = 0.45f;
+        m.thin_film_ior = 1.33f;
+        m.specular_roughness = 0.15f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.7f, 0.1f, 0.08f);  // clear-coated car paint
+        m.base_metalness = 0.6f;
+        m.specular_roughness = 0.4f;
+        m.coat_weight = 1.0f;
+        m.coat_roughness = 0.05f;
+        m.coat_color[2] = 0.85f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.2f, 0.05f, 0.3f);  // velvet
+        m.fuzz_weight = 1.0f;
+        m.fuzz_color[0] = 0.9f;
+        m.fuzz_color[1] = 0.6f;
+        m.fuzz_color[2] = 1.0f;
+        m.fuzz_roughness = 0.5f;
+        m.base_diffuse_roughness = 1.0f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.9f, 0.7f, 0.6f);  // skin-like random walk
+        m.subsurface_weight = 1.0f;
+        m.subsurface_color[0] = 0.9f;
+        m.subsurface_color[1] = 0.6f;
+        m.subsurface_color[2] = 0.5f;
+        m.subsurface_radius = 0.25f;
+        m.subsurface_scatter_anisotropy = 0.3f;
+        m.specular_roughness = 0.35f;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.3f, 0.8f, 0.3f);  // leaf: thin-walled subsurface
+        m.subsurface_weight = 0.8f;
+        m.subsurface_color[0] = 0.4f;
+        m.subsurface_color[1] = 0.9f;
+        m.subsurface_color[2] = 0.3f;
+        m.subsurface_scatter_anisotropy = 0.4f;
+        m.geometry_thin_walled = 1;
+        row.push_back(m);
+    }
+    {
+        rtgb_openpbr_material m = base(0.2f, 0.4f, 0.9f);  // cut-out
+        m.geometry_opacity = 0.45f;
+        row.push_back(m);
+    }
+    {
+        // roughness and metalness from a small image, specular color from a checker
+        rtgb_openpbr_material m = base(0.8f, 0.8f, 0.85f);
+        const int w = 8, h = 8;
+        std::vector<float> rough(static_cast<size_t>(w * h * 3)), metal(static_cast<size_t>(w * h * 3));
+        for (int y = 0; y < h; ++y) {
+            for (int x = 0; x < w; ++x) {
+                const float r = static_cast<float>(rng.uniform(0.05, 0.9));
+                const float mt = ((x / 2 + y / 2) & 1) ? 1.0f : 0.0f;
+                for (int k = 0; k < 3; ++k) {
+                    rough[static_cast<size_t>((y * w + x) * 3 + k)] = r;
+                    metal[static_cast<size_t>((y * w + x) * 3 + k)] = mt;
+                }
+            }
+        }
+        m.scalar_texture[1] = b.image_texture(w, h, rough);
+        m.scalar_texture[0] = b.image_texture(w, h, metal);
+        m.color_texture[1] = b.checker_texture(4.0, b.constant_texture({1.0, 0.8, 0.6}), b.constant_texture({0.6, 0.8, 1.0}));
+        row.push_back(m);
+    }
+    const int n = static_cast<int>(row.size());
+    for (int i = 0; i < n; ++i) {
+        const int col = i % 6, line = i / 6;
+        const double x = -2.75 + 1.1 * col;
+        const double z = 4.0 + 1.4 * line;
+        b.sphere(b.openpbr(row[static_cast<size_t>(i)]), {x, 0.45, z}, 0.45);
+    }
+    // emitters: an OpenPBR quad overhead (one-sided geometry, two-sided OpenPBR emission)
+    // and a small OpenPBR sphere whose emission color is texture-bound
+    {
+        rtgb_openpbr_material m = base(0.0f, 0.0f, 0.0f);
+        m.emission_luminance = 6.0f;
+        m.emission_color[0] = 1.0f;
+        m.emission_color[1] = 0.9f;
+        m.emission_color[2] = 0.75f;
+        b.quad(b.openpbr(m), {-1.5, 3.2, 3.5}, {3.0, 0.0, 0.0}, {0.0, 0.0, 2.5});
+    }
+    {
+        rtgb_openpbr_material m = base(0.1f, 0.1f, 0.1f);
+        m.emission_luminance = 4.0f;
+        m.color_texture[3] = b.checker_texture(8.0, b.constant_texture({1.0, 0.3, 0.2}), b.constant_texture({0.2, 0.5, 1.0}));
+        m.color_space[3] = 1;
+        b.sphere(b.openpbr(m), {3.6, 1.4, 6.5}, 0.3);
+    }
+    const int lights = detail > 0 ? static_cast<int>(detail) : 24;
+    std::vector<double> weights;
+    for (int i = 0; i < lights; ++i) {
+        const double strength = rng.uniform(2.0, 12.0);
+        rtgb_analytic_light& l = b.analytic(RTGB_ANALYTIC_SPHERE);
+        set3(l.position, {rng.uniform(-4.0, 4.0), rng.uniform(1.5, 3.5), rng.uniform(1.0, 8.0)});
+        set3(l.basis_x, {1.0, 0.0, 0.0});
+        set3(l.basis_y, {0.0, 1.0, 0.0});
+        set3(l.basis_z, {0.0, 0.0, 1.0});
+        set3(l.radiance, {strength, strength * rng.uniform(0.6, 1.0), strength * rng.uniform(0.5, 1.0)});
+        l.radius = static_cast<float>(rng.uniform(0.05, 0.15));
+        l.world_area = static_cast<float>(4.0 * std::numbers::pi * l.radius * l.radius);
+        weights.push_back(strength * l.world_area);
+    }
+    finalize_analytic_distribution(s, weights);
+    b.background({0.03, 0.035, 0.05});
+}
+
 // Seeded procedural triangle scene: a displaced-grid terrain plus icosphere
 // instances, constant per-object materials, and `emissive` emissive
 // triangles (a fraction of the icosphere faces). The triangle budget is
@@ -562,6 +808,7 @@ rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t deta
     else if (n == "restir_acceptance") build_restir_acceptance(*s);
     else if (n == "random_spheres") build_random_spheres(*s, seed, detail);
     else if (n == "triangle_terrain") build_triangle_terrain(*s, seed, detail);
+    else if (n == "openpbr_gallery") build_openpbr_gallery(*s, seed, detail);
     else {
         delete s;
         return RTGB_INVALID_ARGUMENT;
@@ -591,6 +838,8 @@ rtgb_status rtgb_host_scene_view(const rtgb_host_scene* s, rtgb_scene* v) {
     v->medium_count = static_cast<int32_t>(s->media.size());
     v->analytic_lights = s->analytic.data();
     v->analytic_light_count = static_cast<int32_t>(s->analytic.size());
+    v->openpbr_materials = s->openpbr.data();
+    v->openpbr_material_count = static_cast<int32_t>(s->openpbr.size());
     std::memcpy(v->background, s->background.data(), sizeof v->background);
     return RTGB_OK;
 }

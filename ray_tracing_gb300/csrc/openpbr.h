@@ -13,10 +13,15 @@
 
 #include <cmath>
 
+// PBR_HD: small helpers, inlined everywhere. PBR_CALL: the large entry points
+// (evaluate, sample), kept as real calls on the device so the many call sites
+// of the shading kernels share one copy of their code.
 #if defined(__CUDACC__)
 #define PBR_HD __host__ __device__ __forceinline__
+#define PBR_CALL __host__ __device__ inline __noinline__
 #else
 #define PBR_HD inline
+#define PBR_CALL inline
 #endif
 
 namespace rtgb {
@@ -1015,7 +1020,7 @@ PBR_HD V3 reflection_fresnel(const Mat& m, float cm, float co, bool entering, co
 
 // ---- evaluate_openpbr_core (openpbr_core.h:1679-1860) ---------------------------------
 
-PBR_HD Eval evaluate(const Mat& m, Frame f, const V3& wo_world, const V3& wi_world, const Context& ctx) {
+PBR_CALL Eval evaluate(const Mat& m, Frame f, const V3& wo_world, const V3& wi_world, const Context& ctx) {
     Eval res{zero3(), 0.0f};
     const V3 won = vnorm(wo_world);
     const V3 win = vnorm(wi_world);
@@ -1231,7 +1236,7 @@ PBR_HD Sample sample_boundary(const Mat& m, Frame f, const V3& wo_world, float u
 }
 
 // sample_openpbr_core (openpbr_core.h:1995-2297)
-PBR_HD Sample sample(const Mat& m, Frame f, const V3& wo_world, float u_lobe, float u1, float u2, const Context& ctx) {
+PBR_CALL Sample sample(const Mat& m, Frame f, const V3& wo_world, float u_lobe, float u1, float u2, const Context& ctx) {
     Sample s = empty_sample();
     const V3 won = vnorm(wo_world);
     if (len2(won) <= 0.0f) return s;
@@ -1422,3 +1427,4 @@ PBR_HD Sample sample(const Mat& m, Frame f, const V3& wo_world, float u_lobe, fl
 }  // namespace rtgb
 
 #undef PBR_HD
+#undef PBR_CALL

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "lbvh.cuh"
+#include "openpbr.h"
 #include "wavefront.cuh"
 
 namespace rtgb {
@@ -173,12 +174,13 @@ struct rtgb_renderer {
     bool record = false;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
-    LaunchShape shapes[7]{};
+    LaunchShape shapes[kLaunchShapes]{};
     std::string error;
 
     // scene
     bool prepared = false;
     DeviceScene scene{};
+    DevBuf openpbr;
     DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
         triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
         sorted_keys, sorted_vals;
@@ -305,13 +307,24 @@ struct rtgb_renderer {
         return 0.0f;
     }
 
+    // material_emission_luminance, packed_scene_preparation.cpp:227-251
     float emission_lum(const rtgb_scene& s, int mi) const {
         if (mi < 0 || mi >= s.material_count) return 0.0f;
         const rtgb_material& m = s.materials[mi];
-        if (m.type != 3) return 0.0f;
         float c[3];
-        average_texture_lum_r(s, m.emission_texture, 0, c);
-        return luminance(c[0], c[1], c[2]);
+        if (m.type == 3) {
+            average_texture_lum_r(s, m.emission_texture, 0, c);
+            return luminance(c[0], c[1], c[2]);
+        }
+        if (m.type != 5 || m.openpbr_index < 0 || m.openpbr_index >= s.openpbr_material_count) return 0.0f;
+        const rtgb_openpbr_material& om = s.openpbr_materials[m.openpbr_index];
+        pbr::Mat params;
+        std::memcpy(&params, &om, sizeof params);
+        if (om.color_texture[3] >= 0) {
+            average_texture_lum_r(s, om.color_texture[3], 0, c);
+            pbr::apply_color(params, 3, pbr::V3{c[0], c[1], c[2]}, om.color_space[3]);
+        }
+        return pbr::luminance(pbr::emission(params));
     }
 
     void validate_scene(const rtgb_scene& s) {
@@ -326,6 +339,7 @@ struct rtgb_renderer {
         check(s.triangles, s.triangle_count, "triangle");
         check(s.media, s.medium_count, "medium");
         check(s.analytic_lights, s.analytic_light_count, "analytic light");
+        check(s.openpbr_materials, s.openpbr_material_count, "OpenPBR material");
         const long long surfaces = static_cast<long long>(s.sphere_count) + s.quad_count + s.triangle_count;
         if (surfaces == 0) throw Invalid{"render_radiance requires at least one surface primitive"};
         if (surfaces >= (1ll << 28)) throw Invalid{"scene exceeds 2^28 surface primitives"};
@@ -343,6 +357,10 @@ struct rtgb_renderer {
         d.triangles = upload(triangles, s.triangles, static_cast<size_t>(s.triangle_count), stream);
         d.media = upload(media, s.media, static_cast<size_t>(s.medium_count), stream);
         d.materials = upload(materials, s.materials, static_cast<size_t>(s.material_count), stream);
+        d.openpbr = s.openpbr_material_count > 0
+                        ? upload(openpbr, s.openpbr_materials, static_cast<size_t>(s.openpbr_material_count), stream)
+                        : nullptr;
+        d.openpbr_count = s.openpbr_material_count;
         d.textures = upload(textures, s.textures, static_cast<size_t>(s.texture_count), stream);
         d.texels = s.image_texel_count > 0 ? upload(texels, s.image_texels, 3 * static_cast<size_t>(s.image_texel_count), stream) : nullptr;
         d.sphere_count = s.sphere_count;
@@ -599,7 +617,7 @@ struct rtgb_renderer {
         const size_t align = 256;
         auto sz = [&](size_t b) { return (b + align - 1) & ~(align - 1); };
         const size_t f4 = sz(static_cast<size_t>(n) * 16), i1 = sz(static_cast<size_t>(n) * 4), i2 = sz(static_cast<size_t>(n) * 8);
-        size_t total = f4 * 15 + i2 + i1 * 6;
+        size_t total = f4 * 17 + i2 + i1 * 7;
         const bool scratch = true;
         if (scratch) total += sz(static_cast<size_t>(n) * sizeof(Reservoir));
         if (need_records) total += sz(static_cast<size_t>(n) * 4 * bounces);
@@ -631,6 +649,9 @@ struct rtgb_renderer {
         P.shadow_queue = reinterpret_cast<int*>(take(i1));
         P.restir_queue = reinterpret_cast<int*>(take(i1));
         P.res_written = reinterpret_cast<int*>(take(i1));
+        P.sss_mat = reinterpret_cast<int*>(take(i1));
+        P.sss_ext = reinterpret_cast<float4*>(take(f4));
+        P.sss_alb = reinterpret_cast<float4*>(take(f4));
         P.res_scratch = reinterpret_cast<Reservoir*>(take(sz(static_cast<size_t>(n) * sizeof(Reservoir))));
         P.codes = need_records ? reinterpret_cast<int*>(take(sz(static_cast<size_t>(n) * 4 * bounces))) : nullptr;
         paths = P;
@@ -725,10 +746,11 @@ struct rtgb_renderer {
             launch_trace(d_fp, scene, paths, d_counters, b, shapes[1], stream);
             mark(k);
             launch_reset_counters(d_counters, b, stream);
-            launch_shade(d_fp, scene, paths, d_counters, b, shapes[2], stream);
-            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes[6], stream);
+            const bool pbr_scene = scene.openpbr_count > 0;
+            launch_shade(d_fp, scene, paths, d_counters, b, shapes[pbr_scene ? 7 : 2], stream);
+            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes[pbr_scene ? 8 : 6], stream);
             mark(k);
-            launch_shadow(scene, paths, d_counters, b, shapes[3], stream);
+            launch_shadow(d_fp, scene, paths, d_counters, b, shapes[3], stream);
             mark(k);
         }
         launch_finalize(d_fp, paths, d_counters, shapes[4], stream);

@@ -1,0 +1,19 @@
+// OpenPBR instance of the shade kernel, k_shade<true> (shade_stage.cuh), in its
+// own translation unit so the large OpenPBR code compiles in parallel with the
+// rest and never enters the legacy instances.
+#include "shade_stage.cuh"
+
+namespace rtgb {
+
+void launch_shade_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
+    LaunchShape shape, cudaStream_t stream) {
+    k_shade<true><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
+}
+
+LaunchShape query_shade_pbr_shape(int sm_count) {
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<true>, 128, 0);
+    return LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+}
+
+}  // namespace rtgb

@@ -5,9 +5,15 @@
 // and a light BVH that return the same results.
 #pragma once
 
+#include <cstddef>
+
 #include "device_common.cuh"
+#include "openpbr.h"
 
 namespace rtgb {
+
+static_assert(offsetof(rtgb_openpbr_material, color_texture) == sizeof(pbr::Mat),
+    "rtgb_openpbr_material starts with the OpenPBR parameter block");
 
 struct Hit {
     float t;
@@ -159,8 +165,42 @@ RTGB_D float3 eval_texture(const DeviceScene& s, int index, float u, float v, co
     return f3(1.0f, 0.0f, 1.0f);
 }
 
-// populate_material, programs.cu:961-1009 (OpenPBR resolves to no material:
-// material_type -1, like a missing compiled material).
+// ---- OpenPBR materials (programs.cu:148-160, :909-960) ----------------------------
+
+RTGB_D pbr::V3 pv(const float3& v) { return pbr::V3{v.x, v.y, v.z}; }
+RTGB_D float3 fv(const pbr::V3& v) { return f3(v.x, v.y, v.z); }
+
+// resolve_openpbr_material, programs.cu:909-921
+RTGB_D const rtgb_openpbr_material* openpbr_material(const DeviceScene& s, int index) {
+    if (index < 0 || index >= s.openpbr_count || s.openpbr == nullptr) return nullptr;
+    return s.openpbr + index;
+}
+
+RTGB_D void openpbr_load(const rtgb_openpbr_material& c, pbr::Mat& m) {
+    const float* src = reinterpret_cast<const float*>(&c);
+    float* dst = reinterpret_cast<float*>(&m);
+#pragma unroll
+    for (int k = 0; k < static_cast<int>(sizeof(pbr::Mat) / 4); ++k) dst[k] = src[k];
+}
+
+// evaluate_openpbr_color_binding, programs.cu:923-932 (input 0 base, 1 specular,
+// 2 transmission, 3 emission color)
+RTGB_D void openpbr_color_binding(const DeviceScene& s, pbr::Mat& m, const rtgb_openpbr_material& c, int input,
+    float u, float v, const float3& p);
+
+// evaluate_openpbr_scattering_material, programs.cu:944-960: the parameters the
+// BSDF sees at a hit (the base color already evaluated by populate_material).
+RTGB_D void openpbr_scattering(const DeviceScene& s, const Hit& h, pbr::Mat& m);
+
+RTGB_D pbr::Context transport_context(const float3& throughput) {
+    pbr::Context ctx = pbr::default_context();
+    ctx.throughput = pv(throughput);
+    return ctx;
+}
+
+// populate_material, programs.cu:961-1009. Instances without kPbr resolve no
+// OpenPBR material (they run only for scenes that have none).
+template <bool kPbr>
 RTGB_D void populate_material(const DeviceScene& s, int mi, Hit& h) {
     if (mi < 0 || mi >= s.material_count || s.materials == nullptr) {
         h.base = f3(0.0f, 0.0f, 0.0f);
@@ -185,9 +225,21 @@ RTGB_D void populate_material(const DeviceScene& s, int mi, Hit& h) {
     if (h.mtype == 3 && !h.front) h.emis = f3(0.0f, 0.0f, 0.0f);
     if (h.mtype != 3) h.emis = f3(0.0f, 0.0f, 0.0f);
     if (h.mtype == 5) {
-        h.mtype = -1;
-        h.base = f3(0.0f, 0.0f, 0.0f);
-        h.emis = f3(0.0f, 0.0f, 0.0f);
+        const rtgb_openpbr_material* c = kPbr ? openpbr_material(s, m.openpbr_index) : nullptr;
+        if (c == nullptr) {
+            h.mtype = -1;
+            h.base = f3(0.0f, 0.0f, 0.0f);
+            h.emis = f3(0.0f, 0.0f, 0.0f);
+            return;
+        }
+        if constexpr (kPbr) {
+            pbr::Mat params;
+            openpbr_load(*c, params);
+            openpbr_color_binding(s, params, *c, 0, h.u, h.v, h.pos);
+            openpbr_color_binding(s, params, *c, 3, h.u, h.v, h.pos);
+            h.base = fv(params.base_color);
+            h.emis = fv(pbr::emission(params));
+        }
     }
 }
 
@@ -200,6 +252,7 @@ RTGB_D void set_face(const float3& d, const float3& outward, Hit& h) {
 // Rebuilds the full hit record of the winning primitive (try_hit_sphere/quad/
 // triangle, programs.cu:1421-1547). Re-running the test over (eps, far) picks
 // the same root the traversal accepted, so t, uv and normals are identical.
+template <bool kPbr>
 RTGB_D bool reconstruct_surface(const DeviceScene& s, int code, const float3& o, const float3& d, Hit& h) {
     const int type = static_cast<unsigned>(code) >> 28;
     const int idx = code & 0x0fffffff;
@@ -265,11 +318,12 @@ RTGB_D bool reconstruct_surface(const DeviceScene& s, int code, const float3& o,
     } else {
         return false;
     }
-    populate_material(s, mi, h);
+    populate_material<kPbr>(s, mi, h);
     return true;
 }
 
 // Medium scattering event (programs.cu:1738-1750): no primitive identity.
+template <bool kPbr>
 RTGB_D void reconstruct_medium(const DeviceScene& s, int medium, float t, const float3& o, const float3& d, Hit& h) {
     h.t = t;
     h.pos = add(o, mul(d, t));
@@ -280,7 +334,7 @@ RTGB_D void reconstruct_medium(const DeviceScene& s, int medium, float t, const 
     h.v = 0.0f;
     h.ptype = -1;
     h.pidx = -1;
-    populate_material(s, s.media[medium].material_index, h);
+    populate_material<kPbr>(s, s.media[medium].material_index, h);
 }
 
 // hit_medium_boundary, programs.cu:1356-1419
@@ -607,11 +661,24 @@ RTGB_D float3 sphere_direction(float u0, float u1) {
     return f3(r * cosf(phi), r * sinf(phi), z);
 }
 
+// evaluate_material_emission, programs.cu:1011-1024
+template <bool kPbr>
 RTGB_D float3 material_emission(const DeviceScene& s, const rtgb_material& m, float u, float v, const float3& p) {
-    if (m.type == 5) return f3(0.0f, 0.0f, 0.0f);
+    if (m.type == 5) {
+        if constexpr (kPbr) {
+            const rtgb_openpbr_material* c = openpbr_material(s, m.openpbr_index);
+            if (c == nullptr) return f3(0.0f, 0.0f, 0.0f);
+            pbr::Mat params;
+            openpbr_load(*c, params);
+            openpbr_color_binding(s, params, *c, 3, u, v, p);
+            return fv(pbr::emission(params));
+        }
+        return f3(0.0f, 0.0f, 0.0f);
+    }
     return eval_texture(s, m.emission_texture, u, v, p);
 }
 
+template <bool kPbr>
 RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t& rng) {
     LightSample smp = empty_sample();
     const float3 sp = rcv.pos;
@@ -738,7 +805,7 @@ RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t&
         cond = area_pdf(0.5f * da, d2, ac);
     }
     if (cond <= 0.0f || smp.material_index < 0 || smp.material_index >= s.material_count) return empty_sample();
-    smp.emission = material_emission(s, s.materials[smp.material_index], tu, tv, smp.position);
+    smp.emission = material_emission<kPbr>(s, s.materials[smp.material_index], tu, tv, smp.position);
     smp.pdf = sel * cond;
     smp.valid = smp.pdf > 0.0f && max_comp(smp.emission) > 0.0f;
     return smp;
@@ -829,8 +896,44 @@ RTGB_D LightSample analytic_candidate(const DeviceScene& s, const float3& sp, in
 }
 
 // direct_material_response, programs.cu:1026-1055 (legacy materials)
-RTGB_D float3 direct_response(const Hit& h, const float3& ldir, float& bsdf_pdf) {
+RTGB_D void openpbr_color_binding(const DeviceScene& s, pbr::Mat& m, const rtgb_openpbr_material& c, int input,
+    float u, float v, const float3& p) {
+    const int tex = c.color_texture[input];
+    if (tex < 0) return;
+    pbr::apply_color(m, input, pv(eval_texture(s, tex, u, v, p)), c.color_space[input]);
+}
+
+RTGB_D void openpbr_scattering(const DeviceScene& s, const Hit& h, pbr::Mat& m) {
+    const rtgb_openpbr_material& c = s.openpbr[h.openpbr];
+    openpbr_load(c, m);
+    if (c.color_texture[0] >= 0) m.base_color = pv(h.base);
+    openpbr_color_binding(s, m, c, 1, h.u, h.v, h.pos);
+    openpbr_color_binding(s, m, c, 2, h.u, h.v, h.pos);
+    for (int k = 0; k < 2; ++k) {
+        if (c.scalar_texture[k] >= 0) pbr::apply_scalar(m, k, eval_texture(s, c.scalar_texture[k], h.u, h.v, h.pos).x);
+    }
+}
+
+// OpenPBR branch of direct_material_response (programs.cu:1038-1054) with the
+// hit's scattering parameters already evaluated; `ray_d` is the incoming ray.
+RTGB_D float3 openpbr_response(const pbr::Mat& m, const Hit& h, const float3& ray_d, const float3& thr,
+    const float3& ldir, float& bsdf_pdf) {
+    const pbr::Frame frame = pbr::make_frame(pv(h.gn), pbr::V3{0.0f, 0.0f, 0.0f});
+    const pbr::Eval e = pbr::evaluate(m, frame, pv(mul(normalize(ray_d), -1.0f)), pv(ldir), transport_context(thr));
+    const float cosine = fabsf(dot(h.sn, ldir));
+    bsdf_pdf = e.pdf;
+    return mul(fv(e.value), cosine);
+}
+
+// direct_material_response, programs.cu:1026-1055. `pm` holds the OpenPBR
+// scattering parameters when h.mtype == 5 (evaluated once per hit).
+template <bool kPbr>
+RTGB_D float3 direct_response(const Hit& h, const pbr::Mat* pm, const float3& ray_d, const float3& thr,
+    const float3& ldir, float& bsdf_pdf) {
     bsdf_pdf = 0.0f;
+    if constexpr (kPbr) {
+        if (h.mtype == 5) return openpbr_response(*pm, h, ray_d, thr, ldir, bsdf_pdf);
+    }
     if (h.mtype == 0) {
         const float c = fmaxf(dot(h.sn, ldir), 0.0f);
         bsdf_pdf = c / kPi;

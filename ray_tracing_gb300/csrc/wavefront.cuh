@@ -41,6 +41,9 @@ struct Paths {
     int* shadow_queue;
     int* restir_queue;       // bounce-0 surfaces waiting for ReSTIR DI
     int* codes;              // optional parity record [path][max_bounces]
+    int* sss_mat;            // OpenPBR material whose random-walk medium the path is inside, -1 outside
+    float4* sss_ext;         // that medium's extinction.xyz, w = Henyey-Greenstein anisotropy
+    float4* sss_alb;         // its single-scattering albedo.xyz
 };
 
 struct Counters {
@@ -95,7 +98,7 @@ void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
     LaunchShape shape, cudaStream_t stream);
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream);
-void launch_shadow(DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
+void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream);
 void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
     cudaStream_t stream);
@@ -105,7 +108,20 @@ void launch_direction_debug(const CameraDev& cam, uint8_t* rgba, cudaStream_t st
 void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
 // Persistent grid sizes: SM count x resident blocks per SM for raygen, trace,
 // shade, shadow, finalize, resolve and restir.
+// shapes[0..6]: raygen, trace, shade, shadow, finalize, resolve, restir;
+// shapes[7..8]: the OpenPBR instances of shade and restir.
 void query_launch_shapes(int sm_count, LaunchShape* shapes);
+constexpr int kLaunchShapes = 9;
+
+// OpenPBR instances of the shade stage (shade_pbr.cu, restir_pbr.cu);
+// launch_shade and launch_restir forward to them when the scene has OpenPBR
+// materials.
+void launch_shade_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
+    LaunchShape shape, cudaStream_t stream);
+void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
+    cudaStream_t stream);
+LaunchShape query_shade_pbr_shape(int sm_count);
+LaunchShape query_restir_pbr_shape(int sm_count);
 void launch_tonemap(const float4* beauty, uint8_t* rgba, long long pixels, cudaStream_t stream);
 
 // Scene preparation kernels (scene_prep.cu).
