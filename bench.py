@@ -14,8 +14,8 @@ value   = rays traced (primary + extension + shadow + ReSTIR visibility) per
 e2e     = the same metric through the C ABI with host buffers: rtgb_render_frame
           and the download of every camera's beauty/normal/albedo/depth into
           pinned host memory, wall-clock timed per step.
-roofline: the launch with the largest share of the frame, SURVEY per-unit
-          algorithmic bytes over its CUDA-event durations, against the measured
+roofline: the launch with the largest share of the frame, per-unit algorithmic
+          bytes (SoA stream bytes per ray / path segment / pixel) over its CUDA-event durations, against the measured
           HBM copy bandwidth.
 cpu_baseline / --impl reference: the CPU oracle (restatement of the reference's
           radiance kernel, with the reference's median-split BVH) on all host
@@ -49,7 +49,8 @@ WIDTH, HEIGHT, CAMERAS = 640, 480, 4
 LIGHTS = 1024
 L2_FLUSH_BYTES = 256 << 20
 
-# SURVEY 8(d) algorithmic bytes per unit (SoA stream bytes, BVH traffic excluded)
+# Algorithmic bytes per unit: SoA stream bytes read + written per ray, path
+# segment or pixel; BVH node and primitive traffic is excluded.
 BYTES_RAYGEN = 32 + 48          # per path: ray + path state
 BYTES_TRACE = 32 + 16           # per ray: read ray, write hit
 BYTES_SHADE = 16 + 48 + 48 + 32 + 32 + 16   # per path segment
@@ -196,7 +197,7 @@ def run_reference(args, rank, world):
 
 def roofline(stage_ms, frames_stats, spatial):
     """Roofline record of the launch slot (kernel at a bounce) with the largest
-    average time per frame; SURVEY per-unit algorithmic bytes over its
+    average time per frame; per-unit algorithmic bytes over its
     CUDA-event durations, against the measured HBM copy bandwidth."""
     peaks = {}
     p = ROOT / "MEASURED_PEAKS.json"

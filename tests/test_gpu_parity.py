@@ -16,7 +16,7 @@ from ray_tracing_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 
-REL = 1e-4          # radiance tolerance along identical paths (spec bound)
+REL = 1e-4          # radiance tolerance along identical paths (1e-4 relative per pixel)
 MAX_DIVERGED = 2e-3  # fraction of paths allowed to take a different (tied) branch
 
 
