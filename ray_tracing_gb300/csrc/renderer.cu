@@ -617,7 +617,9 @@ struct rtgb_renderer {
         const size_t align = 256;
         auto sz = [&](size_t b) { return (b + align - 1) & ~(align - 1); };
         const size_t f4 = sz(static_cast<size_t>(n) * 16), i1 = sz(static_cast<size_t>(n) * 4), i2 = sz(static_cast<size_t>(n) * 8);
-        size_t total = f4 * 17 + i2 + i1 * 7;
+        const size_t src2 = sz(static_cast<size_t>(n) * 8 * kMaxReuseSources);
+        const size_t src1 = sz(static_cast<size_t>(n) * 4 * kMaxReuseSources);
+        size_t total = f4 * 17 + i2 + i1 * 8 + src2 + 2 * src1;
         const bool scratch = true;
         if (scratch) total += sz(static_cast<size_t>(n) * sizeof(Reservoir));
         if (need_records) total += sz(static_cast<size_t>(n) * 4 * bounces);
@@ -652,6 +654,10 @@ struct rtgb_renderer {
         P.sss_mat = reinterpret_cast<int*>(take(i1));
         P.sss_ext = reinterpret_cast<float4*>(take(f4));
         P.sss_alb = reinterpret_cast<float4*>(take(f4));
+        P.res_meta = reinterpret_cast<int*>(take(i1));
+        P.res_src = reinterpret_cast<int2*>(take(src2));
+        P.res_src_t = reinterpret_cast<float*>(take(src1));
+        P.vis_queue = reinterpret_cast<int*>(take(src1));
         P.res_scratch = reinterpret_cast<Reservoir*>(take(sz(static_cast<size_t>(n) * sizeof(Reservoir))));
         P.codes = need_records ? reinterpret_cast<int*>(take(sz(static_cast<size_t>(n) * 4 * bounces))) : nullptr;
         paths = P;
@@ -748,7 +754,7 @@ struct rtgb_renderer {
             launch_reset_counters(d_counters, b, stream);
             const bool pbr_scene = scene.openpbr_count > 0;
             launch_shade(d_fp, scene, paths, d_counters, b, shapes[pbr_scene ? 7 : 2], stream);
-            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes[pbr_scene ? 8 : 6], stream);
+            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes, stream);
             mark(k);
             launch_shadow(d_fp, scene, paths, d_counters, b, shapes[3], stream);
             mark(k);
@@ -780,6 +786,10 @@ struct rtgb_renderer {
             pixels += static_cast<long long>(rig.cameras[c].width) * rig.cameras[c].height;
         }
         if (pixels * spp >= (1ll << 31)) throw Invalid{"frame exceeds 2^31 paths"};
+        // the bias-correction ray queue packs (path << 4) | source into an int
+        if (profile.enable_restir_di != 0 && pixels * spp >= (1ll << 27)) {
+            throw Invalid{"ReSTIR DI frames are limited to 2^27 paths"};
+        }
         if (layout_changed) {
             // resize_history -> reset_history (device_frame_buffers.cpp:80-98)
             for (int c = 0; c < RTGB_MAX_CAMERAS; ++c) {

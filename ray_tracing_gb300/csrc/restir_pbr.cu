@@ -1,18 +1,25 @@
-// OpenPBR instance of the ReSTIR DI kernel, k_restir<true> (shade_stage.cuh),
+// OpenPBR instances of the ReSTIR DI passes (shade_stage.cuh),
 // in its own translation unit for the same reasons as shade_pbr.cu.
 #include "shade_stage.cuh"
 
 namespace rtgb {
 
-void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
-    cudaStream_t stream) {
-    k_restir<true><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters);
+void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
+    const LaunchShape* shapes, cudaStream_t stream) {
+    k_restir_ris<true><<<shapes[11].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_vis<true><<<shapes[12].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir<true><<<shapes[8].grid, 128, 0, stream>>>(fp, scene, paths, counters);
 }
 
-LaunchShape query_restir_pbr_shape(int sm_count) {
+// shapes[8], [11], [12]: the final, RIS and visibility passes.
+void query_restir_pbr_shapes(int sm_count, LaunchShape* shapes) {
     int blocks = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir<true>, 128, 0);
-    return LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    shapes[8] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir_ris<true>, 128, 0);
+    shapes[11] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir_vis<true>, 128, 0);
+    shapes[12] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
 }
 
 }  // namespace rtgb

@@ -167,22 +167,96 @@ RTGB_D Surface load_surface(const Reservoir* r) {
     return s;
 }
 
-// accumulate_restir_analytic_direct_light, programs.cu:2315-2449. Writes the
-// reservoir and the shadow query of its selected sample into slot 1.
+// ---- ReSTIR DI (accumulate_restir_analytic_direct_light, programs.cu:2315-2449) ----
+//
+// Three wavefront passes at the ReSTIR bounce, in the reference's order of
+// RNG draws and floating-point sums:
+//   k_restir_ris  initial RIS over the candidates, then the temporal and
+//                 spatial merges (every RNG draw of the reuse); the reservoir
+//                 and its reuse sources are parked per path;
+//   k_restir_vis  the BASIC bias-correction target of every reuse source: one
+//                 closest-hit ray from the previous camera to the source surface
+//                 (restir_target_at_previous_surface, :2210-2247);
+//   k_restir      bias-corrected finalisation, the reservoir store, the
+//                 selected sample's shadow query and the BSDF scatter.
+// Splitting the visibility rays out of the RIS loop lets each pass run with its
+// own register budget and occupancy; no value or draw order changes.
+
+constexpr int kMaxSources = kMaxReuseSources;
+constexpr int kGuide = 1024;          // CDF guide-table buckets
+
+// First i with u < cdf[i] (else count-1), the same index as sample_cdf, found
+// from a guide table: guide[j] = first i with j/kGuide < cdf[i] bounds the
+// answer for u in [j/kGuide, (j+1)/kGuide) between guide[j] and guide[j+1].
+RTGB_D int sample_cdf_guided(const float* cdf, const int* guide, int count, float u) {
+    if (count <= 0) return -1;
+    const float s = u < 0.0f ? 0.0f : (u < 1.0f ? u : 0.99999994f);
+    const int j = static_cast<int>(s * static_cast<float>(kGuide));
+    int lo = guide[j], hi = guide[j + 1];
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s < cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo < count ? lo : count - 1;
+}
+
+// Builds guide[0..kGuide] over cdf (all threads of the block; ends with a barrier).
+RTGB_D void build_guide(const float* cdf, int count, int* guide) {
+    for (int j = threadIdx.x; j <= kGuide; j += blockDim.x) {
+        const float t = static_cast<float>(j) * (1.0f / static_cast<float>(kGuide));
+        int lo = 0, hi = count;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (t < cdf[mid]) hi = mid;
+            else lo = mid + 1;
+        }
+        guide[j] = j == kGuide ? count : lo;
+    }
+    __syncthreads();
+}
+
+// meta word of a parked reservoir: source count, selected source + 1, canonical M
+RTGB_D int pack_meta(int nsrc, int selected_src, int canonical) {
+    return nsrc | ((selected_src + 1) << 8) | (canonical << 16);
+}
+
+// Initial RIS and reuse merges (programs.cu:2322-2399). Leaves the reservoir
+// with its surface set and the merge sources in src_index/mult.
 template <bool kPbr>
-RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const FrameBufs& hist, int c, int x, int y,
-    long long path, const Hit& h, const pbr::Mat* pm, const float3& ray_d, uint32_t& rng, bool bsdf_avail,
-    const float3& thr, float4& sh_o, float4& sh_d, float4& sh_c) {
+RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide, int c, int x, int y, const Hit& h,
+    const pbr::Mat* pm, const float3& ray_d, uint32_t& rng, bool bsdf_avail, const float3& thr, Reservoir& r,
+    int* src_index, int* mult, int& nsrc, int& selected_src, int& canonical) {
     const FrameParams& fp = ctx.fp;
     const DeviceScene& s = ctx.s;
-    ++ctx.restir_runs;
     const CameraDev& cam = fp.cam[c];
-    Reservoir r = empty_reservoir();
+    r = empty_reservoir();
     const int req = fp.restir_candidates > 0 ? fp.restir_candidates : 1;
     const int count = req < 32 ? req : 32;
-    for (int k = 0; k < count; ++k) {
+    // Two candidates per step: the four draws of each (light, u0, u1, then the
+    // reservoir's) keep their order, and the two light evaluations overlap.
+    int k = 0;
+    for (; k + 1 < count; k += 2) {
+        Candidate ca, cb;
+        ca.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
+        ca.u0 = rnd(rng);
+        ca.u1 = rnd(rng);
+        const float ua = rnd(rng);
+        cb.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
+        cb.u0 = rnd(rng);
+        cb.u1 = rnd(rng);
+        const float ub = rnd(rng);
+        const LightSample la = analytic_candidate(s, h.pos, ca.light_index, ca.u0, ca.u1);
+        const LightSample lb = analytic_candidate(s, h.pos, cb.light_index, cb.u0, cb.u1);
+        float ta = 0.0f, tb = 0.0f;
+        unshadowed<kPbr>(h, pm, ray_d, thr, la, bsdf_avail, ta);
+        unshadowed<kPbr>(h, pm, ray_d, thr, lb, bsdf_avail, tb);
+        reservoir_update(r, ca, ta, la.pdf > 0.0f ? ta / la.pdf : 0.0f, 1, ua);
+        reservoir_update(r, cb, tb, lb.pdf > 0.0f ? tb / lb.pdf : 0.0f, 1, ub);
+    }
+    if (k < count) {
         Candidate cand;
-        cand.light_index = sample_cdf(ctx.analytic_cdf, s.analytic_count, rnd(rng));
+        cand.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
         cand.u0 = rnd(rng);
         cand.u1 = rnd(rng);
         const LightSample l = analytic_candidate(s, h.pos, cand.light_index, cand.u0, cand.u1);
@@ -191,13 +265,9 @@ RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const F
         const float w = l.pdf > 0.0f ? t / l.pdf : 0.0f;
         reservoir_update(r, cand, t, w, 1, rnd(rng));
     }
-    const int canonical = r.candidate_count;
-    // Reuse sources are kept as history pixel indices; their surfaces are
-    // re-read for bias correction instead of being held in local memory.
-    int src_index[9];
-    int mult[9];
-    int nsrc = 0;
-    int selected_src = -1;
+    canonical = r.candidate_count;
+    nsrc = 0;
+    selected_src = -1;
     const Reservoir* hres = hist.reservoirs + cam.pixel_offset;
     const Surface cur_surface = restir_surface(h);
     const int nbrs = fp.restir_spatial < 8 ? fp.restir_spatial : 8;
@@ -224,8 +294,8 @@ RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const F
     }
     if (nbrs > 0 && have_prev) {
         const int rot = (x * 3 + y * 5 + static_cast<int>(fp.stream)) & 7;
-        for (int k = 0; k < nbrs; ++k) {
-            const int oi = (rot + k) & 7;
+        for (int n = 0; n < nbrs; ++n) {
+            const int oi = (rot + n) & 7;
             // kOffsets of programs.cu:2187-2196
             const int dx = (oi == 0 || oi == 4 || oi == 6) ? -1 : ((oi == 1 || oi == 5 || oi == 7) ? 1 : 0);
             const int dy = (oi == 2 || oi == 4 || oi == 5) ? -1 : ((oi == 3 || oi == 6 || oi == 7) ? 1 : 0);
@@ -240,7 +310,7 @@ RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const F
             float t = 0.0f;
             unshadowed<kPbr>(h, pm, ray_d, thr, l, bsdf_avail, t);
             const MergeResult m = reservoir_merge(r, prev, t, fp.restir_max_spatial, rnd(rng), false);
-            if (m.multiplicity > 0 && nsrc < 9) {
+            if (m.multiplicity > 0 && nsrc < kMaxSources) {
                 src_index[nsrc] = ni;
                 mult[nsrc] = m.multiplicity;
                 if (m.selected != 0) selected_src = nsrc;
@@ -249,12 +319,26 @@ RTGB_D void restir_direct(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, const F
         }
     }
     r.surface = cur_surface;
+}
+
+// Bias correction, reservoir store and the selected sample's shadow query
+// (programs.cu:2400-2449) from the parked reservoir and the source targets.
+template <bool kPbr>
+RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, int c, int x, int y, long long path,
+    const Hit& h, const pbr::Mat* pm, const float3& ray_d, bool bsdf_avail, const float3& thr, Reservoir& r, int meta,
+    float4& sh_o, float4& sh_d, float4& sh_c) {
+    const FrameParams& fp = ctx.fp;
+    const DeviceScene& s = ctx.s;
+    const CameraDev& cam = fp.cam[c];
+    const int nsrc = meta & 0xff;
+    const int selected_src = ((meta >> 8) & 0xff) - 1;
+    const int canonical = meta >> 16;
     if (fp.restir_bias == 1 && nsrc > 0 && r.valid != 0) {
         float sel_t = r.selected_target;
         float sum = r.selected_target * static_cast<float>(canonical);
         for (int k = 0; k < nsrc; ++k) {
-            const float t = target_at_previous<kPbr>(ctx, c, load_surface(hres + src_index[k]), r.selected, bsdf_avail);
-            sum += t * static_cast<float>(mult[k]);
+            const float t = P.res_src_t[path * kMaxSources + k];
+            sum += t * static_cast<float>(P.res_src[path * kMaxSources + k].y);
             if (selected_src == k) sel_t = t;
         }
         reservoir_finalize_basic(r, sel_t, sum, nsrc);
@@ -596,26 +680,103 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
     }
 }
 
-// ReSTIR DI for the deferred bounce-0 surfaces, then their BSDF scatter.
+// ReSTIR DI for the deferred bounce-0 surfaces: the three passes described at
+// restir_gather, then the BSDF scatter.
 constexpr int kSharedCdf = 4096;
+
+// Shared-memory copy of the analytic-light CDF (when it fits) and its guide table.
+struct RestirShared {
+    float cdf[kSharedCdf];
+    int guide[kGuide + 1];
+};
+
+RTGB_D const float* stage_cdf(const DeviceScene& s, RestirShared& sh) {
+    const bool shared = s.analytic_count <= kSharedCdf;
+    if (shared) {
+        for (int k = threadIdx.x; k < s.analytic_count; k += blockDim.x) sh.cdf[k] = s.analytic_cdf[k];
+        __syncthreads();
+    }
+    const float* cdf = shared ? sh.cdf : s.analytic_cdf;
+    build_guide(cdf, s.analytic_count, sh.guide);
+    return cdf;
+}
+
+template <bool kPbr>
+__global__ void __launch_bounds__(128) k_restir_ris(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+    Counters* counters) {
+    __shared__ RestirShared sh;
+    const FrameParams& fp = *fpp;
+    const FrameBufs hist = fp.hist;
+    const int count = counters->restir;
+    if (count == 0) return;
+    const float* cdf = stage_cdf(s, sh);
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, cdf};
+    constexpr int bounce = 0;
+    const bool bsdf_avail = bounce + 1 < fp.max_bounces;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int path = P.restir_queue[i];
+        const float4 hr = P.hit[path];
+        PathRegs st;
+        load_path(P, path, st);
+        uint32_t rng = P.rng[path];
+        Hit h;
+        rebuild_hit<kPbr>(s, hr, st, h);
+        pbr::Mat pm;
+        if constexpr (kPbr) {
+            if (h.mtype == 5) openpbr_scattering(s, h, pm);
+        }
+        const int c = camera_of_path(fp, path);
+        const CameraDev& cam = fp.cam[c];
+        const int pixel = static_cast<int>((path - cam.path_offset) / fp.spp);
+        Reservoir r;
+        int src_index[kMaxSources], mult[kMaxSources];
+        int nsrc = 0, selected_src = -1, canonical = 0;
+        restir_gather<kPbr>(ctx, hist, sh.guide, c, pixel % cam.width, pixel / cam.width, h, &pm, st.d, rng,
+            bsdf_avail, st.thr, r, src_index, mult, nsrc, selected_src, canonical);
+        P.res_scratch[path] = r;
+        P.rng[path] = rng;
+        P.res_meta[path] = pack_meta(nsrc, selected_src, canonical);
+        for (int k = 0; k < nsrc; ++k) P.res_src[static_cast<long long>(path) * kMaxSources + k] = make_int2(src_index[k], mult[k]);
+        const bool bias = fp.restir_bias == 1 && r.valid != 0;
+        for (int k = 0; k < kMaxSources; ++k) {
+            queue_push(P.vis_queue, &counters->vis, (path << 4) | k, bias && k < nsrc);
+        }
+    }
+}
+
+template <bool kPbr>
+__global__ void __launch_bounds__(128) k_restir_vis(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+    Counters* counters) {
+    const FrameParams& fp = *fpp;
+    const FrameBufs hist = fp.hist;
+    const int count = counters->vis;
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, s.analytic_cdf};
+    constexpr int bounce = 0;
+    const bool bsdf_avail = bounce + 1 < fp.max_bounces;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int item = P.vis_queue[i];
+        const int path = item >> 4;
+        const int k = item & 15;
+        const int c = camera_of_path(fp, path);
+        const long long slot = static_cast<long long>(path) * kMaxSources + k;
+        const Reservoir* hres = hist.reservoirs + fp.cam[c].pixel_offset;
+        const Candidate sel = P.res_scratch[path].selected;
+        P.res_src_t[slot] = target_at_previous<kPbr>(ctx, c, load_surface(hres + P.res_src[slot].x), sel, bsdf_avail);
+    }
+    count_add(&counters->rays[3], ctx.vis_rays);
+    if (ctx.overflow) atomicAdd(&counters->overflow, ctx.overflow);
+}
 
 template <bool kPbr>
 __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters) {
-    __shared__ float cdf_shared[kSharedCdf];
     const FrameParams& fp = *fpp;
     FrameBufs cur = fp.cur;
-    const FrameBufs hist = fp.hist;
     const int count = counters->restir;
-    if (count == 0) return;
-    const bool shared = s.analytic_count <= kSharedCdf;
-    if (shared) {
-        for (int k = threadIdx.x; k < s.analytic_count; k += blockDim.x) cdf_shared[k] = s.analytic_cdf[k];
-        __syncthreads();
-    }
-    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, shared ? cdf_shared : s.analytic_cdf};
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, s.analytic_cdf};
     constexpr int bounce = 0;
     const int out = 1;
+    unsigned long long runs = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const int path = P.restir_queue[i];
         const float4 hr = P.hit[path];
@@ -633,8 +794,10 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         const CameraDev& cam = fp.cam[c];
         const int pixel = static_cast<int>((path - cam.path_offset) / fp.spp);
         float4 sh_o1, sh_d1, sh_c1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        restir_direct<kPbr>(ctx, P, cur, hist, c, pixel % cam.width, pixel / cam.width, path, h, &pm, st.d, rng, bsdf_avail,
-            st.thr, sh_o1, sh_d1, sh_c1);
+        Reservoir r = P.res_scratch[path];
+        ++runs;
+        restir_finish<kPbr>(ctx, P, cur, c, pixel % cam.width, pixel / cam.width, path, h, &pm, st.d, bsdf_avail,
+            st.thr, r, P.res_meta[path], sh_o1, sh_d1, sh_c1);
         int sss_event = 0, event = 0;
         const bool keep = bsdf_avail && scatter<kPbr>(fp, h, &pm, bounce, rng, st, sss_event, event);
         if constexpr (kPbr) {
@@ -653,9 +816,8 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         queue_push(P.shadow_queue, &counters->shadow, path, any_shadow);
         queue_push(P.queue[out], &counters->active[out], path, keep);
     }
-    count_add(&counters->rays[3], ctx.vis_rays);
-    count_add(&counters->restir_pixels, ctx.restir_runs);
-    if (ctx.overflow) atomicAdd(&counters->overflow, ctx.overflow);
+    count_add(&counters->restir_pixels, runs);
+    (void)ctx;
 }
 
 }  // namespace

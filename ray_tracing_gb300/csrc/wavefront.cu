@@ -260,6 +260,7 @@ __global__ void k_reset_counters(Counters* counters, int bounce) {
         counters->active[(bounce & 1) ^ 1] = 0;
         counters->shadow = 0;
         counters->restir = 0;
+        counters->vis = 0;
         if (bounce == 0) {
             for (int b = 0; b < 64; ++b) counters->shadow_bounce[b] = 0;
         }
@@ -322,13 +323,15 @@ void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counte
     k_shadow<<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
 }
 
-void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
-    cudaStream_t stream) {
+void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
+    const LaunchShape* shapes, cudaStream_t stream) {
     if (scene.openpbr_count > 0) {
-        launch_restir_pbr(fp, scene, paths, counters, shape, stream);
+        launch_restir_pbr(fp, scene, paths, counters, shapes, stream);
         return;
     }
-    k_restir<false><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_ris<false><<<shapes[9].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_vis<false><<<shapes[10].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir<false><<<shapes[6].grid, 128, 0, stream>>>(fp, scene, paths, counters);
 }
 
 void launch_finalize(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream) {
@@ -355,8 +358,12 @@ void query_launch_shapes(int sm_count, LaunchShape* shapes) {
     shapes[5] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 256};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir<false>, 128, 0);
     shapes[6] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir_ris<false>, 128, 0);
+    shapes[9] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir_vis<false>, 128, 0);
+    shapes[10] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     shapes[7] = query_shade_pbr_shape(sm_count);
-    shapes[8] = query_restir_pbr_shape(sm_count);
+    query_restir_pbr_shapes(sm_count, shapes);
 }
 
 void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream) {

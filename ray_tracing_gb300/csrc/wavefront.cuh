@@ -44,6 +44,10 @@ struct Paths {
     int* sss_mat;            // OpenPBR material whose random-walk medium the path is inside, -1 outside
     float4* sss_ext;         // that medium's extinction.xyz, w = Henyey-Greenstein anisotropy
     float4* sss_alb;         // its single-scattering albedo.xyz
+    int2* res_src;           // ReSTIR reuse sources [path][9]: history pixel, multiplicity
+    float* res_src_t;        // their bias-correction targets [path][9]
+    int* res_meta;           // per path: source count, selected source + 1, canonical M
+    int* vis_queue;          // (path << 4) | source of each bias-correction ray
 };
 
 struct Counters {
@@ -57,7 +61,7 @@ struct Counters {
     int bounce_active[64];           // paths entering each bounce of the last frame
     unsigned long long restir_pixels; // paths that ran ReSTIR DI in the last frame
     int restir;                       // ReSTIR queue length
-    int pad2;
+    int vis;                          // bias-correction ray queue length
     unsigned long long shadow_bounce[64];  // shadow rays traced per bounce
 };
 
@@ -100,8 +104,10 @@ void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
     LaunchShape shape, cudaStream_t stream);
 void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream);
-void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
-    cudaStream_t stream);
+// The three ReSTIR passes (RIS + merges, bias-correction rays, finalisation);
+// `shapes` is the full array filled by query_launch_shapes.
+void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
+    const LaunchShape* shapes, cudaStream_t stream);
 void launch_finalize(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
 void launch_resolve(const FrameParams* fp, LaunchShape shape, cudaStream_t stream);
 void launch_direction_debug(const CameraDev& cam, uint8_t* rgba, cudaStream_t stream);
@@ -109,19 +115,23 @@ void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
 // Persistent grid sizes: SM count x resident blocks per SM for raygen, trace,
 // shade, shadow, finalize, resolve and restir.
 // shapes[0..6]: raygen, trace, shade, shadow, finalize, resolve, restir;
-// shapes[7..8]: the OpenPBR instances of shade and restir.
+// shapes[7..8]: the OpenPBR instances of shade and restir; [9..10]: restir RIS
+// and visibility passes; [11..12]: their OpenPBR instances.
 void query_launch_shapes(int sm_count, LaunchShape* shapes);
-constexpr int kLaunchShapes = 9;
+constexpr int kLaunchShapes = 13;
+
+// Reuse sources kept per path by the ReSTIR passes: temporal + up to 8 spatial.
+constexpr int kMaxReuseSources = 9;
 
 // OpenPBR instances of the shade stage (shade_pbr.cu, restir_pbr.cu);
 // launch_shade and launch_restir forward to them when the scene has OpenPBR
 // materials.
 void launch_shade_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream);
-void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, LaunchShape shape,
-    cudaStream_t stream);
+void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
+    const LaunchShape* shapes, cudaStream_t stream);
 LaunchShape query_shade_pbr_shape(int sm_count);
-LaunchShape query_restir_pbr_shape(int sm_count);
+void query_restir_pbr_shapes(int sm_count, LaunchShape* shapes);
 void launch_tonemap(const float4* beauty, uint8_t* rgba, long long pixels, cudaStream_t stream);
 
 // Scene preparation kernels (scene_prep.cu).
