@@ -329,6 +329,7 @@ struct DeviceScene {
     const int* quad_light;
     const int* triangle_light;
     const rtgb_analytic_light* analytic;
+    const float4* analytic_nrm;     // analytic_light_normal of every light, computed once at prepare
     const float* analytic_cdf;
     int analytic_count;
     const BvhNode* analytic_nodes;  // BVH over finite, non-point analytic lights

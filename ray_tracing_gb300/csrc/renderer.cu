@@ -180,7 +180,7 @@ struct rtgb_renderer {
     // scene
     bool prepared = false;
     DeviceScene scene{};
-    DevBuf openpbr;
+    DevBuf openpbr, analytic_nrm;
     DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
         triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
         sorted_keys, sorted_vals;
@@ -431,6 +431,10 @@ struct rtgb_renderer {
         const int na = s.analytic_light_count;
         d.analytic = upload(analytic, s.analytic_lights, static_cast<size_t>(na), stream);
         d.analytic_count = na;
+        d.analytic_nrm = na > 0 ? static_cast<const float4*>(analytic_nrm.ensure(static_cast<size_t>(na) * sizeof(float4)))
+                                : nullptr;
+        launch_analytic_normals(d, const_cast<float4*>(d.analytic_nrm), stream);
+        RTGB_CHECK(cudaGetLastError());
         std::vector<float> acdf(static_cast<size_t>(na));
         std::vector<int> inf, finite;
         for (int i = 0; i < na; ++i) {

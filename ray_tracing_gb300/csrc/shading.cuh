@@ -870,10 +870,10 @@ RTGB_D LightSample analytic_candidate(const DeviceScene& s, const float3& sp, in
         const float radial = l.radius * sqrtf(u0);
         const float phi = 2.0f * kPi * u1;
         smp.position = add(center, add(mul(ld3(l.basis_x), radial * cosf(phi)), mul(ld3(l.basis_y), radial * sinf(phi))));
-        smp.normal = analytic_normal(l);
+        smp.normal = xyz(s.analytic_nrm[li]);
     } else if (l.type == 2) {
         smp.position = add(center, add(mul(ld3(l.basis_x), (u0 - 0.5f) * l.width), mul(ld3(l.basis_y), (u1 - 0.5f) * l.height)));
-        smp.normal = analytic_normal(l);
+        smp.normal = xyz(s.analytic_nrm[li]);
     } else if (l.type == 3) {
         const float phi = 2.0f * kPi * u0;
         const float rx = l.radius * cosf(phi);

@@ -294,6 +294,19 @@ __global__ void k_tonemap(const float4* __restrict__ beauty, uint8_t* rgba, long
 
 }  // namespace
 
+// analytic_light_normal (programs.cu:661-666) of every analytic light, once per
+// scene: the same device function the candidates would run, so the table holds
+// exactly the values they would compute.
+__global__ void k_analytic_normals(DeviceScene s, float4* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < s.analytic_count) out[i] = f4(analytic_normal(s.analytic[i]), 0.0f);
+}
+
+void launch_analytic_normals(DeviceScene scene, float4* out, cudaStream_t stream) {
+    if (scene.analytic_count <= 0) return;
+    k_analytic_normals<<<(scene.analytic_count + 255) / 256, 256, 0, stream>>>(scene, out);
+}
+
 void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream) {
     const long long n = static_cast<long long>(cam.width) * cam.height;
     const int grid = static_cast<int>((n + 255) / 256 < 8192 ? (n + 255) / 256 : 8192);
