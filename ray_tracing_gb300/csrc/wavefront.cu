@@ -56,9 +56,24 @@ __global__ void __launch_bounds__(256) k_raygen(const FrameParams* __restrict__ 
         P.queue[0][path] = static_cast<int>(path);
         P.sss_mat[path] = -1;
         if (P.res_written) P.res_written[path] = 0;
-        if (sample == 0) cur.reservoirs[cam.pixel_offset + pixel] = zero_reservoir();
         if (fp.record_paths) {
             for (int b = 0; b < fp.max_bounces; ++b) P.codes[path * fp.max_bounces + b] = -2;
+        }
+    }
+    // The per-launch memset of the reservoir buffer (optix_renderer.cpp:253-254)
+    // as flat 16-byte stores over every active pixel's 84-byte reservoir; the
+    // frame buffers are 256-byte aligned.
+    {
+        const long long bytes = fp.total_pixels * static_cast<long long>(sizeof(Reservoir));
+        const long long n16 = bytes >> 4;
+        float4* base = reinterpret_cast<float4*>(cur.reservoirs);
+        const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n16;
+             i += static_cast<long long>(gridDim.x) * blockDim.x) {
+            base[i] = z;
+        }
+        if (blockIdx.x == 0 && threadIdx.x < ((bytes & 15) >> 2)) {
+            reinterpret_cast<int*>(base + n16)[threadIdx.x] = 0;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
