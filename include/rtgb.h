@@ -512,6 +512,29 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
 rtgb_status rtgb_profile_preset(const char* name, rtgb_render_profile* out_profile);
 
 /* ------------------------------------------------------------------------ */
+/* Denoiser layer primitive (replaces the closed OptiX denoiser's network,   */
+/* src/realtime/gpu/denoiser.cpp:111-185, with this library's U-Net).       */
+/* ------------------------------------------------------------------------ */
+
+/* Packs PyTorch conv2d weights (c_out x c_in_used x 3 x 3, float) into the
+ * BF16 layout rtgb_conv3x3_bf16 reads: [tap = dy*3+dx][c_in/8][c_out][8],
+ * input channels past c_in_used zero. `packed` holds 9 * c_in * c_out values. */
+rtgb_status rtgb_conv3x3_pack_weights(const float* weight_oihw, int32_t c_out, int32_t c_in_used,
+    int32_t c_in, uint16_t* packed);
+
+/* y[n, y, x, y_channel_offset + o] = act(bias[o] + sum conv3x3(x)) on the
+ * tensor cores (tcgen05, TMA halo tiles, FP32 accumulation): x is NHWC BF16
+ * with c_in channels (multiple of 16, <= 128), zero padding 1, stride 1;
+ * c_out a multiple of 16, <= 64; y is NHWC BF16 with y_channels channels.
+ * act = ReLU when relu != 0. device_error (device int, may be null) receives a
+ * non-zero code if a bounded wait inside the kernel ran out. Asynchronous on
+ * `stream` (a cudaStream_t). */
+rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, int32_t w, int32_t c_in,
+    const void* packed_weight, const float* bias, int32_t c_out, int32_t relu, void* y,
+    int32_t y_channels, int32_t y_channel_offset, int32_t* device_error, void* stream,
+    char* message, size_t message_size);
+
+/* ------------------------------------------------------------------------ */
 /* Allocation-free LBVH build. No counterpart in the reference.              */
 /* ------------------------------------------------------------------------ */
 #define RTGB_STATIC_LBVH_MAX_PRIMITIVES 131072

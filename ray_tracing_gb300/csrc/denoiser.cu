@@ -1,0 +1,319 @@
+// Denoiser convolutions on the sm_103a tensor cores.
+//
+// k_conv3x3 is an implicit-GEMM 3x3 convolution (stride 1, zero padding 1) over
+// NHWC BF16 tensors with FP32 accumulation in TMEM:
+//   * a CTA owns a tile of 8 x 16 output pixels (the GEMM's M = 128 rows) and
+//     every output channel (N = C_out <= 64);
+//   * the 10 x 18 input halo of the tile arrives by TMA, one box of 8 channels
+//     (16 bytes) per load, so each box lands as a dense [18][10][8] block: the
+//     image border is the TMA's zero fill, which is exactly the convolution's
+//     zero padding;
+//   * the packed weights of all nine taps stay resident in shared memory;
+//   * one thread issues, per tap and per 16 input channels, a
+//     tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) whose A operand is the halo
+//     shifted by the tap: with the [row][col][8 channels] box layout an 8-pixel
+//     row of the window is one 8 x 16-byte core matrix, core matrices of the
+//     next row are 160 bytes apart and those of the next 8 channels one box
+//     apart, so no im2col copy exists;
+//   * the epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
+//     lanes 32w..32w+31, i.e. tile rows 4w..4w+3), adds the bias, applies ReLU
+//     and stores BF16 into an NHWC tensor at a channel offset, so encoder
+//     outputs land directly in the decoder's concatenation buffers.
+// The grid is persistent (one CTA per SM); every mbarrier wait is bounded.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "rtgb.h"
+#include "tc_primitives.cuh"
+
+namespace rtgb {
+namespace {
+
+constexpr int kTileW = 8;
+constexpr int kTileH = 16;
+constexpr int kHaloW = kTileW + 2;
+constexpr int kHaloH = kTileH + 2;
+constexpr int kBoxBytes = kHaloW * kHaloH * 16;   // one 8-channel box: 2880 bytes
+constexpr int kBoxStride = 2944;                  // boxes 128-byte aligned in shared memory
+constexpr int kRowBytes = kHaloW * 16;            // next tile row of a box
+constexpr int kMaxCout = 64;
+constexpr int kMaxCin = 128;
+constexpr uint32_t kTmemCols = 64;
+constexpr int kSpin = 1 << 22;
+// The whole opt-in shared memory of a CTA: the kernel needs at most
+// 128 + 16 * 2944 + 9 * 128 * 64 * 2 bytes, and one CTA runs per SM anyway.
+constexpr int kConvSmem = 227 * 1024;
+
+struct ConvArgs {
+    int n, h, w, cin, cout;
+    int y_channels, y_offset, relu;
+    const uint4* weight;   // packed [tap][cin/8][cout][8] BF16
+    const float* bias;     // cout
+    __nv_bfloat16* y;
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t* tma_bar = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* mma_bar = tma_bar + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
+    uint8_t* sa = smem + 128;
+    const int boxes = a.cin >> 3;
+    uint8_t* sb = sa + boxes * kBoxStride;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tma_bar, 1);
+        tc::mbar_init(mma_bar, 1);
+        tc::mbar_fence_init();
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(tmem_slot, kTmemCols);
+        tc::tmem_relinquish();
+    }
+    const int wvec = 9 * a.cin * a.cout * 2 / 16;
+    for (int i = threadIdx.x; i < wvec; i += blockDim.x) reinterpret_cast<uint4*>(sb)[i] = a.weight[i];
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int tiles_x = (a.w + kTileW - 1) / kTileW;
+    const int tiles_y = (a.h + kTileH - 1) / kTileH;
+    const int per_image = tiles_x * tiles_y;
+    const int total = per_image * a.n;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, a.cout);
+    const uint32_t abase = tc::smem_u32(sa);
+    const uint32_t bbase = tc::smem_u32(sb);
+    const uint32_t bstep = static_cast<uint32_t>(a.cout) * 16u;
+    uint32_t tma_phase = 0, mma_phase = 0;
+    int failed = 0;
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+        const int img = tile / per_image;
+        const int t = tile - img * per_image;
+        const int ty = t / tiles_x;
+        const int x0 = (t - ty * tiles_x) * kTileW;
+        const int y0 = ty * kTileH;
+        if (threadIdx.x == 0) {
+            tc::mbar_arrive_expect_tx(tma_bar, static_cast<uint32_t>(boxes * kBoxBytes));
+            for (int b = 0; b < boxes; ++b) tc::tma_load_4d(sa + b * kBoxStride, &xmap, tma_bar, b * 8, x0 - 1, y0 - 1, img);
+        }
+        const bool loaded = tc::mbar_wait(tma_bar, tma_phase, kSpin);
+        tma_phase ^= 1u;
+        if (__syncthreads_or(!loaded)) {
+            failed = 1;
+            break;
+        }
+        tc::tc_fence_after();
+        if (threadIdx.x == 0) {
+            uint32_t acc = 0;
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dy = tap / 3;
+                const int dx = tap - dy * 3;
+                for (int s = 0; s < (boxes >> 1); ++s) {
+                    const uint64_t ad = tc::smem_desc(
+                        abase + static_cast<uint32_t>(2 * s * kBoxStride + dy * kRowBytes + dx * 16), kBoxStride, kRowBytes);
+                    const uint64_t bd =
+                        tc::smem_desc(bbase + static_cast<uint32_t>(tap * boxes + 2 * s) * bstep, bstep, 128);
+                    tc::umma_bf16(tmem, ad, bd, idesc, acc);
+                    acc = 1;
+                }
+            }
+            tc::umma_commit(mma_bar);
+        }
+        const bool done = tc::mbar_wait(mma_bar, mma_phase, kSpin);
+        mma_phase ^= 1u;
+        if (__syncthreads_or(!done)) {
+            failed = 2;
+            break;
+        }
+        tc::tc_fence_after();
+        const int m = warp * 32 + lane;
+        const int yy = y0 + (m >> 3);
+        const int xx = x0 + (m & 7);
+        const bool inside = yy < a.h && xx < a.w;
+        __nv_bfloat16* out =
+            a.y + ((static_cast<long long>(img) * a.h + yy) * a.w + xx) * a.y_channels + a.y_offset;
+        for (int g = 0; g < (a.cout >> 4); ++g) {
+            uint32_t v[16];
+            tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v);
+            tc::tmem_wait_ld();
+            if (inside) {
+                uint32_t packed[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
+                    float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
+                    if (a.relu) {
+                        lo = fmaxf(lo, 0.0f);
+                        hi = fmaxf(hi, 0.0f);
+                    }
+                    packed[k] = pack_bf16x2(lo, hi);
+                }
+                uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
+                dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+                dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+            }
+        }
+        tc::tc_fence_before();
+        __syncthreads();
+    }
+    if (failed != 0) {
+        // let copies and MMAs still in flight land before the TMEM is released
+        if (failed == 1) tc::mbar_wait(tma_bar, tma_phase ^ 1u, kSpin);
+        if (failed == 2) tc::mbar_wait(mma_bar, mma_phase ^ 1u, kSpin);
+        if (threadIdx.x == 0 && a.err != nullptr) atomicExch(a.err, failed);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+// ---- host ----------------------------------------------------------------------------------
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiled fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess) {
+            fn = reinterpret_cast<EncodeTiled>(p);
+        }
+    });
+    return fn;
+}
+
+void set_message(char* msg, size_t cap, const char* text) {
+    if (msg != nullptr && cap > 0) std::snprintf(msg, cap, "%s", text);
+}
+
+uint16_t to_bf16(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return static_cast<uint16_t>((u >> 16) | 0x40u);  // quiet NaN
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return static_cast<uint16_t>(u >> 16);
+}
+
+}  // namespace
+
+// Encodes the TMA map of an NHWC BF16 tensor for k_conv3x3's halo boxes.
+bool conv_input_map(CUtensorMap* map, const void* x, int n, int h, int w, int c) {
+    EncodeTiled enc = encode_tiled();
+    if (enc == nullptr) return false;
+    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(c), static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h),
+        static_cast<cuuint64_t>(n)};
+    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(c) * 2, static_cast<cuuint64_t>(w) * c * 2,
+        static_cast<cuuint64_t>(h) * w * c * 2};
+    const cuuint32_t box[4] = {8, kHaloW, kHaloH, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launches k_conv3x3; `map` must describe x (conv_input_map).
+cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
+    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream) {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+    });
+    if (attr != cudaSuccess) return attr;
+    ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
+        static_cast<__nv_bfloat16*>(y), err};
+    const long long tiles = static_cast<long long>((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * n;
+    const int grid = static_cast<int>(tiles < grid_limit ? tiles : grid_limit);
+    k_conv3x3<<<grid > 0 ? grid : 1, 128, kConvSmem, stream>>>(map, a);
+    return cudaGetLastError();
+}
+
+bool conv_shape_ok(int cin, int cout, int y_channels, int y_offset) {
+    return cin >= 16 && cin <= kMaxCin && cin % 16 == 0 && cout >= 16 && cout <= kMaxCout && cout % 16 == 0 &&
+           y_offset >= 0 && y_offset % 8 == 0 && y_channels % 8 == 0 && y_offset + cout <= y_channels;
+}
+
+}  // namespace rtgb
+
+extern "C" rtgb_status rtgb_conv3x3_pack_weights(const float* weight_oihw, int32_t c_out, int32_t c_in_used,
+    int32_t c_in, uint16_t* packed) {
+    if (weight_oihw == nullptr || packed == nullptr || c_in_used > c_in || c_in % 8 != 0 || c_out <= 0 ||
+        c_in_used <= 0) {
+        return RTGB_INVALID_ARGUMENT;
+    }
+    // packed[tap][c_in/8][c_out][8], tap = dy * 3 + dx; cross-correlation as conv2d
+    const int boxes = c_in / 8;
+    for (int tap = 0; tap < 9; ++tap) {
+        const int dy = tap / 3, dx = tap % 3;
+        for (int b = 0; b < boxes; ++b) {
+            for (int o = 0; o < c_out; ++o) {
+                for (int j = 0; j < 8; ++j) {
+                    const int ci = b * 8 + j;
+                    const float v = ci < c_in_used ? weight_oihw[((static_cast<size_t>(o) * c_in_used + ci) * 3 + dy) * 3 + dx]
+                                                   : 0.0f;
+                    packed[((static_cast<size_t>(tap) * boxes + b) * c_out + o) * 8 + j] = rtgb::to_bf16(v);
+                }
+            }
+        }
+    }
+    return RTGB_OK;
+}
+
+extern "C" rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, int32_t w, int32_t c_in,
+    const void* packed_weight, const float* bias, int32_t c_out, int32_t relu, void* y, int32_t y_channels,
+    int32_t y_channel_offset, int32_t* device_error, void* stream, char* message, size_t message_size) {
+    using namespace rtgb;
+    set_message(message, message_size, "");
+    if (x == nullptr || packed_weight == nullptr || bias == nullptr || y == nullptr || n <= 0 || h <= 0 || w <= 0) {
+        set_message(message, message_size, "null pointer or empty extent");
+        return RTGB_INVALID_ARGUMENT;
+    }
+    if (!conv_shape_ok(c_in, c_out, y_channels, y_channel_offset)) {
+        set_message(message, message_size,
+            "c_in must be a multiple of 16 in [16, 128], c_out a multiple of 16 in [16, 64], the output channel "
+            "offset and count multiples of 8 with offset + c_out <= count");
+        return RTGB_INVALID_ARGUMENT;
+    }
+    if ((reinterpret_cast<uintptr_t>(x) & 15u) != 0 || (reinterpret_cast<uintptr_t>(y) & 15u) != 0 ||
+        (reinterpret_cast<uintptr_t>(packed_weight) & 15u) != 0) {
+        set_message(message, message_size, "tensors must be 16-byte aligned");
+        return RTGB_INVALID_ARGUMENT;
+    }
+    CUtensorMap map;
+    if (!conv_input_map(&map, x, n, h, w, c_in)) {
+        set_message(message, message_size, "cuTensorMapEncodeTiled failed");
+        return RTGB_RUNTIME_ERROR;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const cudaError_t e = launch_conv3x3(map, n, h, w, c_in, packed_weight, bias, c_out, relu, y, y_channels,
+        y_channel_offset, device_error, sms > 0 ? sms : 1, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        set_message(message, message_size, cudaGetErrorString(e));
+        return RTGB_RUNTIME_ERROR;
+    }
+    return RTGB_OK;
+}
