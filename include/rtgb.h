@@ -424,8 +424,10 @@ rtgb_status rtgb_download_frame(rtgb_handle handle, int32_t camera_index, float*
     float* normal_rgba, float* albedo_rgba, float* depth, float* download_ms);
 
 /* Copies any device frame buffer of one camera (flow, trust, denoiser normal)
- * to host: which = 0 beauty, 1 normal, 2 denoiser_normal, 3 albedo, 4 depth,
- * 5 flow, 6 flow_trustworthiness. `bytes` must equal the buffer size. */
+ * to host: which = 0 beauty (the path tracer's, before denoising), 1 normal,
+ * 2 denoiser_normal, 3 albedo, 4 depth, 5 flow, 6 flow_trustworthiness,
+ * 8 denoised beauty (only after a denoised frame). `bytes` must equal the
+ * buffer size. */
 rtgb_status rtgb_download_buffer(rtgb_handle handle, int32_t camera_index, int32_t which,
     void* host, size_t bytes);
 
@@ -510,6 +512,22 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
 
 /* RenderProfile::quality/balanced/realtime (render_profile.h:27-63). */
 rtgb_status rtgb_profile_preset(const char* name, rtgb_render_profile* out_profile);
+
+/* ------------------------------------------------------------------------ */
+/* Learned denoiser: OptixDenoiserWrapper::run (denoiser.cpp:111-185) is      */
+/* replaced by a BF16 U-Net on the tensor cores. With parameters set, frames */
+/* rendered with rtgb_render_profile::enable_denoise != 0 are denoised after */
+/* the resolve pass; the frame views and rtgb_download_frame then return the  */
+/* denoised beauty and denoise_ms its device time. Without parameters the    */
+/* plain accumulated beauty is returned (the reference's no-denoiser path).  */
+/* ------------------------------------------------------------------------ */
+
+/* Number of network parameters rtgb_set_denoiser_params expects. */
+int64_t rtgb_denoiser_param_count(void);
+
+/* Parameters in layer order, each layer's conv weight (out x in x 3 x 3, as
+ * PyTorch's conv2d) then its bias; NULL clears them (plain path). */
+rtgb_status rtgb_set_denoiser_params(rtgb_handle handle, const float* params, int64_t count);
 
 /* ------------------------------------------------------------------------ */
 /* Denoiser layer primitive (replaces the closed OptiX denoiser's network,   */

@@ -236,6 +236,8 @@ SIGNATURES = {
     "rtgb_pack_camera_pose": (C.c_int, [P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]),
     "rtgb_default_rig": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, P(CameraRig)]),
     "rtgb_profile_preset": (C.c_int, [C.c_char_p, P(RenderProfile)]),
+    "rtgb_denoiser_param_count": (C.c_int64, []),
+    "rtgb_set_denoiser_params": (C.c_int, [Handle, C.c_void_p, C.c_int64]),
     "rtgb_conv3x3_pack_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "rtgb_conv3x3_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                                     C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,

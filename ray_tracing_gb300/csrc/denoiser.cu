@@ -233,14 +233,21 @@ bool conv_input_map(CUtensorMap* map, const void* x, int n, int h, int w, int c)
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Launches k_conv3x3; `map` must describe x (conv_input_map).
-cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
-    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream) {
+// Opts k_conv3x3 into its shared-memory size (once per process; call it
+// outside stream capture).
+cudaError_t conv_init() {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
         attr = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
     });
+    return attr;
+}
+
+// Launches k_conv3x3; `map` must describe x (conv_input_map).
+cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
+    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream) {
+    const cudaError_t attr = conv_init();
     if (attr != cudaSuccess) return attr;
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
         static_cast<__nv_bfloat16*>(y), err};
@@ -317,3 +324,320 @@ extern "C" rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, in
     }
     return RTGB_OK;
 }
+
+// ---- the U-Net -------------------------------------------------------------------------------
+
+#include <string>
+#include <vector>
+
+#include "denoiser.cuh"
+
+namespace rtgb {
+namespace {
+
+struct LayerSpec {
+    int cin_used, cin, cout_used, cout, relu;
+};
+
+// in order: e1a e1b e2a e2b e3a e3b d2a d2b d1a d1b head
+constexpr LayerSpec kLayers[] = {
+    {10, 16, 32, 32, 1}, {32, 32, 32, 32, 1}, {32, 32, 48, 48, 1}, {48, 48, 48, 48, 1}, {48, 48, 64, 64, 1},
+    {64, 64, 64, 64, 1}, {112, 112, 48, 48, 1}, {48, 48, 48, 48, 1}, {80, 80, 32, 32, 1}, {32, 32, 32, 32, 1},
+    {32, 32, 3, 16, 0},
+};
+constexpr int kLayerCount = sizeof(kLayers) / sizeof(kLayers[0]);
+constexpr int kInChannels = 16;
+
+__device__ __forceinline__ __nv_bfloat16 bf(float v) { return __float2bfloat16_rn(v); }
+
+// Network input: log1p(radiance), albedo, camera-space normal, log1p(depth), 6 zeros.
+__global__ void k_dn_pack(const FrameParams* __restrict__ fpp, long long offset, long long count,
+    __nv_bfloat16* __restrict__ out) {
+    const FrameBufs f = fpp->cur;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const long long p = offset + i;
+        const float4 b = f.beauty[p];
+        const float4 a = f.albedo[p];
+        const float4 nn = f.dnormal[p];
+        const float d = f.depth[p];
+        __align__(16) __nv_bfloat16 v[16];
+        v[0] = bf(log1pf(fmaxf(b.x, 0.0f)));
+        v[1] = bf(log1pf(fmaxf(b.y, 0.0f)));
+        v[2] = bf(log1pf(fmaxf(b.z, 0.0f)));
+        v[3] = bf(a.x);
+        v[4] = bf(a.y);
+        v[5] = bf(a.z);
+        v[6] = bf(nn.x);
+        v[7] = bf(nn.y);
+        v[8] = bf(nn.z);
+        v[9] = bf(log1pf(fmaxf(d, 0.0f)));
+#pragma unroll
+        for (int k = 10; k < 16; ++k) v[k] = bf(0.0f);
+        uint4* dst = reinterpret_cast<uint4*>(out + i * kInChannels);
+        dst[0] = reinterpret_cast<const uint4*>(v)[0];
+        dst[1] = reinterpret_cast<const uint4*>(v)[1];
+    }
+}
+
+// 2x2 average pooling of channels [0, c) of a `cs`-channel tensor into a dense
+// c-channel tensor at half resolution (windows clipped at odd borders).
+__global__ void k_dn_pool(const __nv_bfloat16* __restrict__ in, int n, int h, int w, int cs, int c,
+    __nv_bfloat16* __restrict__ out) {
+    const int ho = (h + 1) >> 1, wo = (w + 1) >> 1;
+    const int groups = c >> 3;
+    const long long total = static_cast<long long>(n) * ho * wo * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = static_cast<int>(i % groups);
+        long long r = i / groups;
+        const int x = static_cast<int>(r % wo);
+        r /= wo;
+        const int y = static_cast<int>(r % ho);
+        const int img = static_cast<int>(r / ho);
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        int cnt = 0;
+        for (int dy = 0; dy < 2; ++dy) {
+            const int yy = 2 * y + dy;
+            if (yy >= h) continue;
+            for (int dx = 0; dx < 2; ++dx) {
+                const int xx = 2 * x + dx;
+                if (xx >= w) continue;
+                const uint4 q = *reinterpret_cast<const uint4*>(in + ((static_cast<long long>(img) * h + yy) * w + xx) * cs + g * 8);
+                const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) acc[k] += __bfloat162float(e[k]);
+                ++cnt;
+            }
+        }
+        const float inv = 1.0f / static_cast<float>(cnt);
+        __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = bf(acc[k] * inv);
+        *reinterpret_cast<uint4*>(out + ((static_cast<long long>(img) * ho + y) * wo + x) * c + g * 8) =
+            *reinterpret_cast<const uint4*>(v);
+    }
+}
+
+// Nearest 2x upsampling of a dense c-channel tensor (h2 x w2) into channels
+// [off, off + c) of a cs-channel tensor of size h x w.
+__global__ void k_dn_upsample(const __nv_bfloat16* __restrict__ in, int n, int h, int w, int c,
+    __nv_bfloat16* __restrict__ out, int cs, int off) {
+    const int h2 = (h + 1) >> 1, w2 = (w + 1) >> 1;
+    const int groups = c >> 3;
+    const long long total = static_cast<long long>(n) * h * w * groups;
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int g = static_cast<int>(i % groups);
+        long long r = i / groups;
+        const int x = static_cast<int>(r % w);
+        r /= w;
+        const int y = static_cast<int>(r % h);
+        const int img = static_cast<int>(r / h);
+        const uint4 q =
+            *reinterpret_cast<const uint4*>(in + ((static_cast<long long>(img) * h2 + (y >> 1)) * w2 + (x >> 1)) * c + g * 8);
+        *reinterpret_cast<uint4*>(out + ((static_cast<long long>(img) * h + y) * w + x) * cs + off + g * 8) = q;
+    }
+}
+
+// Network output (channels 0..2 of a 16-channel tensor, log1p radiance) to float4.
+__global__ void k_dn_unpack(const __nv_bfloat16* __restrict__ in, long long count, float4* __restrict__ out) {
+    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const uint2 q = *reinterpret_cast<const uint2*>(in + i * 16);
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
+        out[i] = make_float4(expm1f(fmaxf(__bfloat162float(e[0]), 0.0f)), expm1f(fmaxf(__bfloat162float(e[1]), 0.0f)),
+            expm1f(fmaxf(__bfloat162float(e[2]), 0.0f)), 1.0f);
+    }
+}
+
+struct DevMem {
+    void* p = nullptr;
+    size_t bytes = 0;
+    void* ensure(size_t b) {
+        if (b <= bytes && p) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, b) != cudaSuccess) {
+            p = nullptr;
+            return nullptr;
+        }
+        bytes = b;
+        return p;
+    }
+    ~DevMem() {
+        if (p) cudaFree(p);
+    }
+};
+
+int grid_for(long long work, int sms) {
+    const long long g = (work + 255) / 256;
+    const long long cap = static_cast<long long>(sms) * 8;
+    return static_cast<int>(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+}  // namespace
+
+// Activations of one batch shape (n cameras of h x w) and the TMA maps of
+// every layer's input. A frame with cameras of several sizes keeps one set per
+// size, so launches captured in a CUDA graph keep valid addresses.
+struct Acts {
+    DevMem mem;
+    int n = 0, h = 0, w = 0;
+    __nv_bfloat16 *in16 = nullptr, *t1 = nullptr, *cat1 = nullptr, *t5 = nullptr, *t6 = nullptr, *out16 = nullptr;
+    __nv_bfloat16 *p1 = nullptr, *t2 = nullptr, *cat2 = nullptr, *t4 = nullptr, *t4b = nullptr;
+    __nv_bfloat16 *p2 = nullptr, *t3 = nullptr, *t3b = nullptr;
+    CUtensorMap maps[kLayerCount];
+};
+
+struct UNet {
+    DevMem weights[kLayerCount];
+    DevMem biases[kLayerCount];
+    bool ready = false;
+    std::vector<Acts*> sets;
+    ~UNet() {
+        for (Acts* a : sets) delete a;
+    }
+};
+
+long long unet_param_count() {
+    long long n = 0;
+    for (const LayerSpec& l : kLayers) n += static_cast<long long>(l.cout_used) * l.cin_used * 9 + l.cout_used;
+    return n;
+}
+
+UNet* unet_create() { return new UNet(); }
+void unet_destroy(UNet* net) { delete net; }
+bool unet_ready(const UNet* net) { return net != nullptr && net->ready; }
+
+bool unet_set_params(UNet* net, const float* params, long long count, std::string& error) {
+    net->ready = false;
+    if (params == nullptr) return true;
+    if (count != unet_param_count()) {
+        error = "denoiser parameters: expected " + std::to_string(unet_param_count()) + " values, got " +
+                std::to_string(count);
+        return false;
+    }
+    const float* p = params;
+    for (int li = 0; li < kLayerCount; ++li) {
+        const LayerSpec& l = kLayers[li];
+        std::vector<float> w(static_cast<size_t>(l.cout) * l.cin_used * 9, 0.0f);
+        std::memcpy(w.data(), p, sizeof(float) * l.cout_used * l.cin_used * 9);  // rows past cout_used stay zero
+        p += static_cast<long long>(l.cout_used) * l.cin_used * 9;
+        std::vector<float> b(static_cast<size_t>(l.cout), 0.0f);
+        std::memcpy(b.data(), p, sizeof(float) * l.cout_used);
+        p += l.cout_used;
+        std::vector<uint16_t> packed(static_cast<size_t>(9) * l.cin * l.cout);
+        if (rtgb_conv3x3_pack_weights(w.data(), l.cout, l.cin_used, l.cin, packed.data()) != RTGB_OK) {
+            error = "denoiser parameters: packing failed";
+            return false;
+        }
+        void* dw = net->weights[li].ensure(packed.size() * 2);
+        void* db = net->biases[li].ensure(b.size() * 4);
+        if (dw == nullptr || db == nullptr || cudaMemcpy(dw, packed.data(), packed.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(db, b.data(), b.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            error = "denoiser parameters: device upload failed";
+            return false;
+        }
+    }
+    net->ready = true;
+    return true;
+}
+
+namespace {
+
+Acts* unet_buffers(UNet* unet, int n, int h, int w) {
+    for (Acts* a : unet->sets) {
+        if (a->n == n && a->h == h && a->w == w) return a;
+    }
+    Acts* net = new Acts();
+    const long long full = static_cast<long long>(n) * h * w;
+    const long long half = static_cast<long long>(n) * ((h + 1) / 2) * ((w + 1) / 2);
+    const long long quarter = static_cast<long long>(n) * ((h + 3) / 4) * ((w + 3) / 4);
+    // channels per resolution: full 16 + 32 + 80 + 32 + 32 + 16, half 32 + 48 + 112 + 48 + 48, quarter 48 + 64 + 64
+    const long long elems = full * 208 + half * 288 + quarter * 176;
+    char* base = static_cast<char*>(net->mem.ensure(static_cast<size_t>(elems) * 2 + 64 * 256));
+    if (base == nullptr) {
+        delete net;
+        return nullptr;
+    }
+    auto take = [&](long long count, int ch) {
+        char* r = base;
+        base += ((count * ch * 2) + 255) & ~255ll;
+        return reinterpret_cast<__nv_bfloat16*>(r);
+    };
+    net->in16 = take(full, 16);
+    net->t1 = take(full, 32);
+    net->cat1 = take(full, 80);
+    net->t5 = take(full, 32);
+    net->t6 = take(full, 32);
+    net->out16 = take(full, 16);
+    net->p1 = take(half, 32);
+    net->t2 = take(half, 48);
+    net->cat2 = take(half, 112);
+    net->t4 = take(half, 48);
+    net->t4b = take(half, 48);
+    net->p2 = take(quarter, 48);
+    net->t3 = take(quarter, 64);
+    net->t3b = take(quarter, 64);
+    const int h2 = (h + 1) / 2, w2 = (w + 1) / 2, h4 = (h2 + 1) / 2, w4 = (w2 + 1) / 2;
+    const struct {
+        const void* x;
+        int h, w, c;
+    } inputs[kLayerCount] = {{net->in16, h, w, 16}, {net->t1, h, w, 32}, {net->p1, h2, w2, 32}, {net->t2, h2, w2, 48},
+        {net->p2, h4, w4, 48}, {net->t3, h4, w4, 64}, {net->cat2, h2, w2, 112}, {net->t4, h2, w2, 48},
+        {net->cat1, h, w, 80}, {net->t5, h, w, 32}, {net->t6, h, w, 32}};
+    for (int li = 0; li < kLayerCount; ++li) {
+        if (!conv_input_map(&net->maps[li], inputs[li].x, n, inputs[li].h, inputs[li].w, inputs[li].c)) {
+            delete net;
+            return nullptr;
+        }
+    }
+    net->n = n;
+    net->h = h;
+    net->w = w;
+    unet->sets.push_back(net);
+    return net;
+}
+
+}  // namespace
+
+bool unet_prepare(UNet* unet, int n, int h, int w) {
+    return conv_init() == cudaSuccess && unet_buffers(unet, n, h, w) != nullptr;
+}
+
+cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, int n, int h, int w, float4* out,
+    int* err, int sms, cudaStream_t stream) {
+    if (!unet->ready) return cudaErrorInvalidValue;
+    Acts* net = unet_buffers(unet, n, h, w);
+    if (net == nullptr) return cudaErrorMemoryAllocation;
+    const long long full = static_cast<long long>(n) * h * w;
+    const int h2 = (h + 1) / 2, w2 = (w + 1) / 2, h4 = (h2 + 1) / 2, w4 = (w2 + 1) / 2;
+    auto conv = [&](int li, int hh, int ww, void* y, int ych, int yoff) {
+        const LayerSpec& l = kLayers[li];
+        return launch_conv3x3(net->maps[li], n, hh, ww, l.cin, unet->weights[li].p, static_cast<const float*>(unet->biases[li].p),
+            l.cout, l.relu, y, ych, yoff, err, sms, stream);
+    };
+    cudaError_t e;
+    k_dn_pack<<<grid_for(full, sms), 256, 0, stream>>>(fp, pixel_offset, full, net->in16);
+    if ((e = conv(0, h, w, net->t1, 32, 0)) != cudaSuccess) return e;
+    if ((e = conv(1, h, w, net->cat1, 80, 0)) != cudaSuccess) return e;
+    k_dn_pool<<<grid_for(static_cast<long long>(n) * h2 * w2 * 4, sms), 256, 0, stream>>>(net->cat1, n, h, w, 80, 32, net->p1);
+    if ((e = conv(2, h2, w2, net->t2, 48, 0)) != cudaSuccess) return e;
+    if ((e = conv(3, h2, w2, net->cat2, 112, 0)) != cudaSuccess) return e;
+    k_dn_pool<<<grid_for(static_cast<long long>(n) * h4 * w4 * 6, sms), 256, 0, stream>>>(net->cat2, n, h2, w2, 112, 48, net->p2);
+    if ((e = conv(4, h4, w4, net->t3, 64, 0)) != cudaSuccess) return e;
+    if ((e = conv(5, h4, w4, net->t3b, 64, 0)) != cudaSuccess) return e;
+    k_dn_upsample<<<grid_for(static_cast<long long>(n) * h2 * w2 * 8, sms), 256, 0, stream>>>(net->t3b, n, h2, w2, 64, net->cat2, 112, 48);
+    if ((e = conv(6, h2, w2, net->t4, 48, 0)) != cudaSuccess) return e;
+    if ((e = conv(7, h2, w2, net->t4b, 48, 0)) != cudaSuccess) return e;
+    k_dn_upsample<<<grid_for(full * 6, sms), 256, 0, stream>>>(net->t4b, n, h, w, 48, net->cat1, 80, 32);
+    if ((e = conv(8, h, w, net->t5, 32, 0)) != cudaSuccess) return e;
+    if ((e = conv(9, h, w, net->t6, 32, 0)) != cudaSuccess) return e;
+    if ((e = conv(10, h, w, net->out16, 16, 0)) != cudaSuccess) return e;
+    k_dn_unpack<<<grid_for(full, sms), 256, 0, stream>>>(net->out16, full, out + pixel_offset);
+    return cudaGetLastError();
+}
+
+}  // namespace rtgb

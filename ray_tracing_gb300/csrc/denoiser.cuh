@@ -1,0 +1,42 @@
+// The learned denoiser that replaces the OptiX AOV denoiser of the reference
+// (src/realtime/gpu/denoiser.cpp:111-185): a small BF16 U-Net over the frame's
+// radiance, albedo, camera-space normal and depth, run on the tensor cores by
+// k_conv3x3 (denoiser.cu).
+//
+// Network (3x3 convolutions, ReLU except the last, 2x2 average pooling,
+// nearest upsampling, skip connections by channel concatenation):
+//   full res   in(10) -> 32 -> 32 ------------------------------ cat(32 + 48) -> 32 -> 32 -> 3
+//   1/2 res              pool -> 48 -> 48 -------- cat(48 + 64) -> 48 -> 48 -> up
+//   1/4 res                      pool -> 64 -> 64 -> up
+// Inputs per pixel: log1p(radiance) (3), albedo (3), camera-space normal (3),
+// log1p(depth) (1); output log1p(radiance), expm1 back to linear.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "wavefront.cuh"
+
+namespace rtgb {
+
+struct UNet;
+
+UNet* unet_create();
+void unet_destroy(UNet* net);
+// Parameters in layer order, each layer's weight (out x in x 3 x 3, as PyTorch's
+// conv2d) then bias; count must equal unet_param_count(). nullptr clears them.
+bool unet_set_params(UNet* net, const float* params, long long count, std::string& error);
+bool unet_ready(const UNet* net);
+long long unet_param_count();
+// Allocates the activations and TMA maps of an (n, h, w) batch; call before
+// stream capture so captured launches find them in place.
+bool unet_prepare(UNet* net, int n, int h, int w);
+// Denoises n cameras of equal size w x h whose pixels start at `pixel_offset`
+// in the frame-wide buffers of *fp (fp->cur); writes float4 radiance into
+// out[pixel_offset ...]. `err` (device int) receives a kernel's bounded-wait
+// failure code.
+cudaError_t unet_run(UNet* net, const FrameParams* fp, long long pixel_offset, int n, int h, int w, float4* out,
+    int* err, int sm_count, cudaStream_t stream);
+
+}  // namespace rtgb

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "denoiser.cuh"
 #include "lbvh.cuh"
 #include "openpbr.h"
 #include "wavefront.cuh"
@@ -181,6 +182,13 @@ struct rtgb_renderer {
     bool prepared = false;
     DeviceScene scene{};
     DevBuf openpbr, analytic_nrm;
+    // learned denoiser (replaces OptixDenoiserWrapper, denoiser.cpp:111-185)
+    UNet* unet = nullptr;
+    DevBuf denoised;          // float4 per pixel of the last denoised frame
+    bool last_denoised = false;
+    bool denoise_this_frame = false;
+    float last_denoise_ms = 0.0f;
+    cudaEvent_t ev_dn0 = nullptr, ev_dn1 = nullptr;
     DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
         triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
         sorted_keys, sorted_vals;
@@ -226,7 +234,8 @@ struct rtgb_renderer {
     uint64_t frame_h2d = 0;
     // graph
     cudaGraphExec_t graph_exec = nullptr;
-    long long graph_key[4] = {-1, -1, -1, -1};
+    long long graph_key[5] = {-1, -1, -1, -1, -1};
+    long long unet_generation = 0;
 
     void fail_cuda(const CudaFailure& f) {
         error = std::string("CUDA failure at ") + f.expr + ": " + cudaGetErrorString(f.err);
@@ -238,13 +247,26 @@ struct rtgb_renderer {
         graph_key[0] = -1;
     }
 
+    void set_denoiser(const float* params, long long count) {
+        RTGB_CHECK(cudaSetDevice(device));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        if (!unet) unet = unet_create();
+        std::string err;
+        if (!unet_set_params(unet, params, count, err)) throw Invalid{err};
+        ++unet_generation;
+        drop_graph();
+    }
+
     ~rtgb_renderer() {
         if (stream) cudaStreamSynchronize(stream);
         drop_graph();
+        unet_destroy(unet);
+        if (ev_dn0) cudaEventDestroy(ev_dn0);
+        if (ev_dn1) cudaEventDestroy(ev_dn1);
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba};
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_nrm, &denoised};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -768,6 +790,23 @@ struct rtgb_renderer {
         launch_resolve(d_fp, shapes[5], stream);
         mark(k);
         stage_count = stage_timing ? k - 1 : 0;
+        if (denoise_this_frame) enqueue_denoise();
+    }
+
+    // Denoises every run of consecutive equal-size cameras as one batch into
+    // `denoised`, between two external events (denoise_ms).
+    void enqueue_denoise() {
+        RTGB_CHECK(cudaEventRecordWithFlags(ev_dn0, stream, cudaEventRecordExternal));
+        const FrameParams& fp = h_fp;
+        int c = 0;
+        while (c < fp.cam_count) {
+            int e = c + 1;
+            while (e < fp.cam_count && fp.cam[e].width == fp.cam[c].width && fp.cam[e].height == fp.cam[c].height) ++e;
+            RTGB_CHECK(unet_run(unet, d_fp, fp.cam[c].pixel_offset, e - c, fp.cam[c].height, fp.cam[c].width,
+                denoised.as<float4>(), &d_counters->denoise_error, sm_count, stream));
+            c = e;
+        }
+        RTGB_CHECK(cudaEventRecordWithFlags(ev_dn1, stream, cudaEventRecordExternal));
     }
 
     int render(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active, bool sync,
@@ -808,6 +847,28 @@ struct rtgb_renderer {
         total_paths = pixels * spp;
         ensure_frames(pixels);
         ensure_paths(total_paths, spp, mb);
+        denoise_this_frame = profile.enable_denoise != 0 && unet_ready(unet);
+        if (denoise_this_frame) {
+            if (!ev_dn0) {
+                RTGB_CHECK(cudaEventCreate(&ev_dn0));
+                RTGB_CHECK(cudaEventCreate(&ev_dn1));
+            }
+            if (denoised.bytes < static_cast<size_t>(pixels) * 16) {
+                drop_graph();
+                denoised.ensure(static_cast<size_t>(pixels) * 16);
+            }
+            for (int c = 0; c < active;) {
+                int e = c + 1;
+                while (e < active && rig.cameras[e].width == rig.cameras[c].width &&
+                       rig.cameras[e].height == rig.cameras[c].height) {
+                    ++e;
+                }
+                if (!unet_prepare(unet, e - c, rig.cameras[c].height, rig.cameras[c].width)) {
+                    throw CudaFailure{cudaErrorMemoryAllocation, "denoiser activations / tensor maps (unet_prepare)"};
+                }
+                c = e;
+            }
+        }
 
         FrameParams& fp = h_fp;
         std::memset(&fp, 0, sizeof fp);
@@ -847,7 +908,8 @@ struct rtgb_renderer {
         RTGB_CHECK(cudaMemcpyAsync(d_fp, &fp, sizeof fp, cudaMemcpyHostToDevice, stream));
 
         RTGB_CHECK(cudaEventRecord(ev_start, stream));
-        const long long key[4] = {total_paths, mb, static_cast<long long>(paths.ray_o != nullptr), reinterpret_cast<long long>(scene.prims)};
+        const long long key[5] = {total_paths, mb, static_cast<long long>(paths.ray_o != nullptr),
+            reinterpret_cast<long long>(scene.prims), (denoise_this_frame ? 1ll : 0ll) | (static_cast<long long>(unet_generation) << 1)};
         if (use_graph) {
             if (!graph_exec || std::memcmp(key, graph_key, sizeof key) != 0) {
                 drop_graph();
@@ -879,6 +941,7 @@ struct rtgb_renderer {
             last_h[c] = rig.cameras[c].height;
         }
         last_count = active;
+        last_denoised = denoise_this_frame;
         last_spp = spp;
         last_bounces = mb;
         last = cur;
@@ -897,6 +960,10 @@ struct rtgb_renderer {
                 error = "device reported " + std::to_string(h_counters->error) + " inconsistent hit records";
                 return RTGB_DEVICE_FAULT_FLAG;
             }
+            if (h_counters->denoise_error != 0) {
+                error = "a denoiser kernel gave up waiting (code " + std::to_string(h_counters->denoise_error) + ")";
+                return RTGB_DEVICE_FAULT_FLAG;
+            }
         }
         return RTGB_OK;
     }
@@ -907,7 +974,7 @@ struct rtgb_renderer {
         v.camera_index = c;
         v.width = last_w[c];
         v.height = last_h[c];
-        v.beauty = f.beauty + o;
+        v.beauty = last_denoised ? denoised.as<float4>() + o : f.beauty + o;
         v.normal = f.normal + o;
         v.denoiser_normal = f.dnormal + o;
         v.albedo = f.albedo + o;
@@ -920,7 +987,13 @@ struct rtgb_renderer {
         float ms = 0.0f;
         RTGB_CHECK(cudaEventElapsedTime(&ms, ev_start, ev_stop));
         out->frame_render_ms = ms;
-        for (int c = 0; c < out->camera_count; ++c) out->cameras[c].render_ms = ms;
+        float dn = 0.0f;
+        if (last_denoised) RTGB_CHECK(cudaEventElapsedTime(&dn, ev_dn0, ev_dn1));
+        last_denoise_ms = dn;
+        for (int c = 0; c < out->camera_count; ++c) {
+            out->cameras[c].render_ms = ms;
+            out->cameras[c].denoise_ms = dn;
+        }
         const Counters& k = *h_counters;
         out->primary_rays = k.rays[0];
         out->extension_rays = k.rays[1];
@@ -944,7 +1017,8 @@ struct rtgb_renderer {
         const FrameBufs& f = frames[last];
         const long long o = last_pixel_offset[c];
         RTGB_CHECK(cudaEventRecord(ev_start, stream));
-        if (beauty) RTGB_CHECK(cudaMemcpyAsync(beauty, f.beauty + o, n * 16, cudaMemcpyDeviceToHost, stream));
+        const void* bsrc = last_denoised ? static_cast<const void*>(denoised.as<float4>() + o) : static_cast<const void*>(f.beauty + o);
+        if (beauty) RTGB_CHECK(cudaMemcpyAsync(beauty, bsrc, n * 16, cudaMemcpyDeviceToHost, stream));
         if (normal) RTGB_CHECK(cudaMemcpyAsync(normal, f.normal + o, n * 16, cudaMemcpyDeviceToHost, stream));
         if (albedo) RTGB_CHECK(cudaMemcpyAsync(albedo, f.albedo + o, n * 16, cudaMemcpyDeviceToHost, stream));
         if (depth) RTGB_CHECK(cudaMemcpyAsync(depth, f.depth + o, n * 4, cudaMemcpyDeviceToHost, stream));
@@ -969,6 +1043,11 @@ struct rtgb_renderer {
             case 5: src = f.flow + o; need = n * 8; break;
             case 6: src = f.trust + o; need = n * 4; break;
             case 7: src = f.reservoirs + o; need = n * sizeof(Reservoir); break;
+            case 8:
+                if (!last_denoised) throw Invalid{"the last frame was not denoised"};
+                src = denoised.as<float4>() + o;
+                need = n * 16;
+                break;
             default: throw Invalid{"unknown frame buffer"};
         }
         if (bytes != need) throw Invalid{"buffer size mismatch: expected " + std::to_string(need) + " bytes"};
@@ -1063,7 +1142,7 @@ rtgb_status rtgb_frame_stats(rtgb_handle h, rtgb_frame_views* out) {
         out->sample_stream = h->sample_stream - 1;
         for (int c = 0; c < h->last_count; ++c) h->fill_view(c, out->cameras[c]);
         h->fill_stats(out);
-        return h->h_counters->error != 0 ? RTGB_DEVICE_FAULT_FLAG : RTGB_OK;
+        return h->h_counters->error != 0 || h->h_counters->denoise_error != 0 ? RTGB_DEVICE_FAULT_FLAG : RTGB_OK;
     });
 }
 
@@ -1105,12 +1184,22 @@ rtgb_status rtgb_download_frame(rtgb_handle h, int32_t c, float* beauty, float* 
 
 rtgb_status rtgb_download_buffer(rtgb_handle h, int32_t c, int32_t which, void* host, size_t bytes) {
     if (!h || !host) return RTGB_INVALID_ARGUMENT;
-    if (which < 0 || which > 6) return RTGB_INVALID_ARGUMENT;
+    if (which < 0 || which > 8 || which == 7) return RTGB_INVALID_ARGUMENT;
     return guarded(h, [&] {
         h->download_buffer(c, which, host, bytes);
         return RTGB_OK;
     });
 }
+
+rtgb_status rtgb_set_denoiser_params(rtgb_handle h, const float* params, int64_t count) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->set_denoiser(params, count);
+        return RTGB_OK;
+    });
+}
+
+int64_t rtgb_denoiser_param_count(void) { return rtgb::unet_param_count(); }
 
 rtgb_status rtgb_download_reservoirs(rtgb_handle h, int32_t c, void* host, size_t bytes) {
     if (!h || !host) return RTGB_INVALID_ARGUMENT;

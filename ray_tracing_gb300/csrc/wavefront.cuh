@@ -56,7 +56,8 @@ struct Counters {
     int error;
     unsigned long long rays[4];  // primary, extension, shadow, restir visibility
     int overflow;
-    int pad[3];
+    int denoise_error;                // a denoiser kernel's bounded wait ran out
+    int pad[2];
     unsigned long long cum_rays[4];  // running totals since the counters were last cleared
     int bounce_active[64];           // paths entering each bounce of the last frame
     unsigned long long restir_pixels; // paths that ran ReSTIR DI in the last frame

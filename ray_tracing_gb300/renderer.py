@@ -127,7 +127,17 @@ class Renderer:
                            ms.value)
 
     BUFFERS = {"beauty": (0, 4), "normal": (1, 4), "denoiser_normal": (2, 4), "albedo": (3, 4), "depth": (4, 1),
-               "flow": (5, 2), "flow_trustworthiness": (6, 1)}
+               "flow": (5, 2), "flow_trustworthiness": (6, 1), "denoised": (8, 4)}
+
+    def set_denoiser(self, params) -> None:
+        """Loads the U-Net parameters (flat float32, layer order; None clears them)."""
+        if params is None:
+            self._check(self.lib.rtgb_set_denoiser_params(self.h, None, 0), "set_denoiser_params")
+            self._denoiser_params = None
+            return
+        arr = np.ascontiguousarray(params, dtype=np.float32)
+        self._check(self.lib.rtgb_set_denoiser_params(self.h, arr.ctypes.data, arr.size), "set_denoiser_params")
+        self._denoiser_params = arr
 
     def buffer(self, cam: int, name: str) -> np.ndarray:
         which, ch = self.BUFFERS[name]

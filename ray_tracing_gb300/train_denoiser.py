@@ -1,0 +1,145 @@
+"""Trains the U-Net denoiser on frames this path tracer renders.
+
+For every training scene the renderer produces
+  * noisy inputs: 1-spp frames with ReSTIR DI (temporal + spatial reuse), the
+    configuration the denoiser runs on, several frames into a sequence so the
+    reservoirs carry history; and
+  * targets: plain path tracing (no ReSTIR) averaged to `--target-spp` samples
+    per pixel, frames rendered independently (accumulation reset each frame).
+The network (ray_tracing_gb300/denoiser.py) is trained on random crops with an
+L1 loss on log1p(radiance) and saved as BF16 parameters in the layer order of
+rtgb_set_denoiser_params.
+
+    python -m ray_tracing_gb300.train_denoiser --out ray_tracing_gb300/weights/denoiser_unet.npz
+
+Training runs on PyTorch (the optimiser and autograd are tooling); inference
+in the renderer runs on the library's tensor-core kernels.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import denoiser, scenes
+from .renderer import Renderer
+
+TRAIN_SCENES = [
+    ("random_spheres", 1, 1024), ("random_spheres", 2, 512), ("random_spheres", 3, 2048), ("random_spheres", 4, 256),
+    ("random_spheres", 5, 1024), ("triangle_terrain", 1, 200000), ("triangle_terrain", 2, 100000),
+    ("openpbr_gallery", 0, 24), ("openpbr_gallery", 1, 48), ("final_room", 0, 0), ("bouncing_spheres", 0, 0),
+    ("cornell_box", 0, 0), ("smoke", 0, 0),
+]
+VALID_SCENE = ("random_spheres", 7, 1024)
+
+
+def noisy_profile():
+    return scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1,
+                          restir_initial_candidates=32, restir_temporal_reuse=1, restir_spatial_neighbors=1)
+
+
+def plain_profile(spp: int):
+    return scenes.profile("balanced", samples_per_pixel=spp, max_bounces=4, enable_denoise=0, enable_restir_di=0)
+
+
+def render_pair(name, seed, detail, width, height, cams, noisy_frames, target_spp, spp_per_frame):
+    """Per camera: (inputs (F, H, W, 10 source channels), target (H, W, 3)) of one scene."""
+    sc = scenes.HostScene(name, seed=seed, detail=detail)
+    rig = scenes.default_rig(name, cams, width, height)
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    r.reset_sequence(1000 + seed)
+    prof = noisy_profile()
+    frames = [[] for _ in range(cams)]
+    for f in range(noisy_frames[-1] + 1):
+        r.render_frame(rig, prof, cams)
+        if f in noisy_frames:
+            for c in range(cams):
+                frames[c].append(np.concatenate([r.buffer(c, "beauty")[..., :3], r.buffer(c, "albedo")[..., :3],
+                                                 r.buffer(c, "denoiser_normal")[..., :3],
+                                                 r.buffer(c, "depth")[..., None]], axis=-1))
+    pprof = plain_profile(spp_per_frame)
+    acc = [None] * cams
+    n = max(1, target_spp // spp_per_frame)
+    for _ in range(n):
+        r.reset_accumulation()
+        r.render_frame(rig, pprof, cams)
+        for c in range(cams):
+            cur = r.buffer(c, "beauty")[..., :3].astype(np.float64)
+            acc[c] = cur if acc[c] is None else acc[c] + cur
+    r.close()
+    return [(np.stack(frames[c]).astype(np.float32), (acc[c] / n).astype(np.float32)) for c in range(cams)]
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--out", type=Path, default=denoiser.WEIGHTS)
+    ap.add_argument("--width", type=int, default=640)
+    ap.add_argument("--height", type=int, default=480)
+    ap.add_argument("--target-spp", type=int, default=1024)
+    ap.add_argument("--spp-per-frame", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--crop", type=int, default=128)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=0)
+    args = ap.parse_args(argv)
+
+    import torch
+    dev = torch.device("cuda", 0)
+    t0 = time.time()
+    inputs, targets = [], []
+    for name, seed, detail in TRAIN_SCENES:
+        for x, y in render_pair(name, seed, detail, args.width, args.height, 4, (2, 3, 5), args.target_spp,
+                                args.spp_per_frame):
+            inputs.append(torch.from_numpy(x).to(dev))
+            targets.append(torch.from_numpy(y).to(dev))
+        print(f"rendered {name}/{seed}: {time.time() - t0:.1f} s", flush=True)
+    valid = render_pair(*VALID_SCENE, args.width, args.height, 4, (3,), args.target_spp, args.spp_per_frame)
+    vx = torch.from_numpy(np.stack([v[0][0] for v in valid])).to(dev)
+    vy = torch.from_numpy(np.stack([v[1] for v in valid])).to(dev)
+
+    def prep(src):  # (B, H, W, 10) AOVs -> network input (B, 10, H, W)
+        return denoiser.make_input(src[..., 0:3], src[..., 3:6], src[..., 6:9], src[..., 9], xp=torch)
+
+    torch.manual_seed(args.seed)
+    gen = torch.Generator(device="cpu").manual_seed(args.seed)
+    model = denoiser.build_model().to(dev)
+    opt = torch.optim.Adam(model.parameters(), lr=args.lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, args.steps)
+    cs = args.crop
+    for step in range(args.steps):
+        xs, ys = [], []
+        for _ in range(args.batch):
+            si = int(torch.randint(len(inputs), (1,), generator=gen))
+            fi = int(torch.randint(inputs[si].shape[0], (1,), generator=gen))
+            H, W = inputs[si].shape[1:3]
+            yy = int(torch.randint(0, H - cs + 1, (1,), generator=gen)) & ~3
+            xx = int(torch.randint(0, W - cs + 1, (1,), generator=gen)) & ~3
+            xs.append(inputs[si][fi, yy:yy + cs, xx:xx + cs])
+            ys.append(targets[si][yy:yy + cs, xx:xx + cs])
+        x = prep(torch.stack(xs))
+        y = torch.log1p(torch.stack(ys).clamp_min(0)).permute(0, 3, 1, 2)
+        loss = torch.nn.functional.l1_loss(model(x), y)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        sched.step()
+        if step % 500 == 0 or step == args.steps - 1:
+            with torch.no_grad():
+                pred = torch.expm1(model(prep(vx)).clamp_min(0)).permute(0, 2, 3, 1)
+                rel = ((pred - vy) ** 2 / (vy ** 2 + 1e-2)).mean().item()
+                noisy = ((vx[..., 0:3] - vy) ** 2 / (vy ** 2 + 1e-2)).mean().item()
+            print(f"step {step}: loss {loss.item():.4f}  valid relMSE {rel:.5f} (noisy {noisy:.5f})", flush=True)
+    flat = denoiser.flatten(model)
+    args.out.parent.mkdir(parents=True, exist_ok=True)
+    np.savez_compressed(args.out, params_bf16=denoiser.to_bf16_bits(flat),
+                        train_scenes=np.array([f"{n}/{s}/{d}" for n, s, d in TRAIN_SCENES]),
+                        target_spp=np.array(args.target_spp), steps=np.array(args.steps))
+    print(f"saved {args.out} ({time.time() - t0:.1f} s)")
+
+
+if __name__ == "__main__":
+    main()
