@@ -5,7 +5,9 @@ Workload (one step = one frame of every camera):
   seeded random-sphere field (ground r=1000 + 22x22 r=0.2 spheres: 80% Lambertian,
   15% metal, 5% dielectric) with 1024 emissive rect lights as analytic lights;
   4 pinhole32 cameras 640x480, 1 spp, depth 4, ReSTIR DI with 32 initial
-  candidates, temporal reuse and 1 spatial neighbour, BASIC bias correction.
+  candidates, temporal reuse and 1 spatial neighbour, BASIC bias correction,
+  then the BF16 U-Net denoiser on the tensor cores (when its trained weights
+  are present: ray_tracing_gb300/weights/denoiser_unet.npz).
 
 value   = rays traced (primary + extension + shadow + ReSTIR visibility) per
           second of device time, inputs resident (Mrays/s); each frame is timed
@@ -14,6 +16,12 @@ value   = rays traced (primary + extension + shadow + ReSTIR visibility) per
 e2e     = the same metric through the C ABI with host buffers: rtgb_render_frame
           and the download of every camera's beauty/normal/albedo/depth into
           pinned host memory, wall-clock timed per step.
+equal_relmse: the headline comparison. A 4096-spp plain render of the same
+          frame is the reference r; relMSE = mean((x - r)^2 / (r^2 + 1e-2)).
+          The denoised pipeline's relMSE and ms/frame are measured, then the
+          plain path (no ReSTIR, no denoiser) is run at doubling sample counts
+          until its relMSE is no larger; its ms/frame there over the denoised
+          ms/frame is the speed-up at equal relMSE.
 roofline: the launch with the largest share of the frame, per-unit algorithmic
           bytes (SoA stream bytes per ray / path segment / pixel) over its CUDA-event durations, against the measured
           HBM copy bandwidth.
@@ -65,18 +73,114 @@ def workload_config(spatial=1):
         "scene": f"ground + 22x22 spheres, {LIGHTS} analytic rect lights",
         "cameras": f"{CAMERAS}x pinhole32 {WIDTH}x{HEIGHT}",
         "spp": 1, "max_bounces": 4, "restir_candidates": 32, "temporal_reuse": 1, "spatial_neighbors": spatial,
-        "denoise": "off (no learned denoiser in this build)",
+        "denoise": "BF16 U-Net (tcgen05 implicit-GEMM 3x3 convolutions)" if _weights() is not None
+                    else "off (trained weights absent)",
         "seed": SEED, "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed frames",
     }
+
+
+def _weights():
+    from ray_tracing_gb300 import denoiser
+    return denoiser.load_weights()
 
 
 def make_inputs():
     from ray_tracing_gb300 import scenes
     sc = scenes.HostScene("random_spheres", seed=0, detail=LIGHTS)
     rig = scenes.default_rig("random_spheres", CAMERAS, WIDTH, HEIGHT)
-    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1,
+    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4,
+                          enable_denoise=1 if _weights() is not None else 0, enable_restir_di=1,
                           restir_initial_candidates=32, restir_temporal_reuse=1, restir_spatial_neighbors=1)
     return sc, rig, prof
+
+
+# ---- equal-relMSE comparison ------------------------------------------------------
+
+RELMSE_EPS = 1e-2
+REFERENCE_SPP = 4096
+SPP_PER_FRAME = 16      # plain renders above this run as several frames, averaged
+
+
+def relmse(x: np.ndarray, ref: np.ndarray) -> float:
+    x = x.astype(np.float64)
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + RELMSE_EPS)))
+
+
+def plain_render(r, rig, spp: int):
+    """Averaged beauty of `spp` plain samples per pixel (no ReSTIR, no denoiser),
+    as frames of at most SPP_PER_FRAME spp with the accumulation reset each
+    frame; returns (per-camera images, device ms)."""
+    from ray_tracing_gb300 import scenes
+    chunks = [SPP_PER_FRAME] * (spp // SPP_PER_FRAME) + ([spp % SPP_PER_FRAME] if spp % SPP_PER_FRAME else [])
+    acc, ms = None, 0.0
+    for per in chunks:
+        prof = scenes.profile("balanced", samples_per_pixel=per, max_bounces=4, enable_denoise=0, enable_restir_di=0)
+        r.reset_accumulation()
+        v = r.render_frame(rig, prof, CAMERAS)
+        ms += v.frame_render_ms
+        cur = np.stack([r.buffer(c, "beauty")[..., :3].astype(np.float64) for c in range(CAMERAS)]) * per
+        acc = cur if acc is None else acc + cur
+    return acc / spp, ms
+
+
+def equal_relmse(sc, rig, prof, frames: int = 8):
+    from ray_tracing_gb300.renderer import Renderer
+    weights = _weights()
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    r.reset_sequence(SEED + 1)
+    ref, ref_ms = plain_render(r, rig, REFERENCE_SPP)
+    out = {"eps": RELMSE_EPS, "reference_spp": REFERENCE_SPP, "reference_ms": ref_ms}
+    if weights is None:
+        out["unavailable"] = "trained denoiser weights absent"
+        return out
+    # denoised pipeline: 1 spp + ReSTIR + U-Net, after warm-up frames for the reservoir history
+    r.set_denoiser(weights)
+    r.reset_sequence(SEED)
+    for _ in range(5):
+        r.render_frame(rig, prof, CAMERAS)
+    d_err, d_ms, d_dn, n_err, p_err1 = [], [], [], [], []
+    for _ in range(frames):
+        v = r.render_frame(rig, prof, CAMERAS)
+        d_ms.append(v.frame_render_ms)
+        d_dn.append(v.cameras[0].denoise_ms)
+        den = np.stack([r.buffer(c, "denoised")[..., :3] for c in range(CAMERAS)])
+        noisy = np.stack([r.buffer(c, "beauty")[..., :3] for c in range(CAMERAS)])
+        d_err.append(relmse(den, ref))
+        n_err.append(relmse(noisy, ref))
+    target = float(np.mean(d_err))
+    den_ms = float(np.median(d_ms))
+    r.set_denoiser(None)
+    spp, found = 1, None
+    trail = []
+    while spp <= 2048:
+        img, ms = plain_render(r, rig, spp)
+        e = relmse(img, ref)
+        trail.append({"spp": spp, "relmse": e, "ms": ms})
+        if e <= target:
+            found = trail[-1]
+            break
+        spp *= 2
+    if found is not None and len(trail) >= 2:
+        lo, hi = trail[-2]["spp"], trail[-1]["spp"]
+        while hi - lo > max(1, lo // 8):
+            mid = (lo + hi) // 2
+            img, ms = plain_render(r, rig, mid)
+            e = relmse(img, ref)
+            trail.append({"spp": mid, "relmse": e, "ms": ms})
+            if e <= target:
+                hi, found = mid, trail[-1]
+            else:
+                lo = mid
+    out.update({
+        "denoised": {"relmse": target, "ms_per_frame": den_ms, "denoise_ms": float(np.median(d_dn)),
+                     "noisy_input_relmse": float(np.mean(n_err)), "frames": frames},
+        "plain": found if found is not None else {"spp": None, "note": "not reached within 2048 spp"},
+        "plain_search": trail,
+        "speedup_at_equal_relmse": (found["ms"] / den_ms) if found is not None else None,
+    })
+    r.close()
+    return out
 
 
 # ---- clocks -------------------------------------------------------------------
@@ -195,6 +299,29 @@ def run_reference(args, rank, world):
 
 # ---- GPU arm --------------------------------------------------------------------------
 
+def denoiser_flops(width: int, height: int, cameras: int) -> float:
+    """Algorithmic FLOPs of one U-Net pass: 2 * pixels * C_in * C_out * 9 per
+    convolution at its resolution, with the network's real channel counts."""
+    from ray_tracing_gb300 import denoiser
+    full = float(width * height * cameras)
+    res = [full, full, full / 4, full / 4, full / 16, full / 16, full / 4, full / 4, full, full, full]
+    return sum(2.0 * px * ci * co * 9 for px, (ci, co) in zip(res, denoiser.LAYERS))
+
+
+def denoiser_record(denoise_ms):
+    """Tensor-core roofline of the denoiser stage (all its launches), against
+    the measured dense BF16 throughput."""
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("bf16_tflops")
+    note = "of measured (burst)" if peak else "of fallback"
+    peak = peak or 1900.0
+    ms = float(np.mean(denoise_ms)) if denoise_ms else 0.0
+    flops = denoiser_flops(WIDTH, HEIGHT, CAMERAS)
+    achieved = flops / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
+    return {"ms_per_frame": ms, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": note, "flops_per_frame": flops}
+
+
 def roofline(stage_ms, frames_stats, spatial):
     """Roofline record of the launch slot (kernel at a bounce) with the largest
     average time per frame; per-unit algorithmic bytes over its
@@ -252,12 +379,18 @@ def run_ours(args, rank, world, local_rank):
     sc, rig, prof = make_inputs()
     r = Renderer(device=local_rank, stage_timing=True)
     r.prepare_scene(sc.view)
+    weights = _weights() if prof.enable_denoise else None
+    if weights is not None:
+        r.set_denoiser(weights)
     r.reset_sequence(SEED)
     stream = torch.cuda.ExternalStream(r.stream_ptr())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
     for _ in range(args.warmup):
         r.render_frame(rig, prof, CAMERAS)
-    launches_per_frame = 3 + 4 * prof.max_bounces  # raygen + (trace, reset, shade, shadow) per bounce + finalize + resolve
+    # raygen, (trace, reset, shade, shadow) per bounce, the three ReSTIR passes,
+    # finalize, resolve; the denoiser: pack, 11 convolutions, 2 pools,
+    # 2 upsamples, unpack per batch of equal-size cameras (one batch here)
+    launches_per_frame = 1 + 4 * prof.max_bounces + 3 + 2 + (17 if weights is not None else 0)
 
     sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
                            if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
@@ -266,7 +399,7 @@ def run_ours(args, rank, world, local_rank):
         dist.barrier()
     torch.cuda.synchronize()
     rays0 = r.ray_totals()
-    frame_ms, stage_ms, frame_stats = [], [], []
+    frame_ms, stage_ms, frame_stats, denoise_ms = [], [], [], []
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     for _ in range(args.steps):
@@ -276,6 +409,7 @@ def run_ours(args, rank, world, local_rank):
         r.render_frame_async(rig, prof, CAMERAS)
         ev1.record(stream)
         v = r.frame_stats()
+        denoise_ms.append(v.cameras[0].denoise_ms)
         frame_ms.append(ev0.elapsed_time(ev1))
         stage_ms.append(r.stage_times())
         frame_stats.append({"paths": WIDTH * HEIGHT * CAMERAS, "pixels": WIDTH * HEIGHT * CAMERAS,
@@ -339,7 +473,10 @@ def run_ours(args, rank, world, local_rank):
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": launches_per_frame * args.steps,
+        "denoiser": denoiser_record(denoise_ms) if weights is not None else None,
     }
+    if world == 1 and not args.no_relmse:
+        line["equal_relmse"] = equal_relmse(sc, rig, prof)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, rig, prof)
     print(json.dumps(line), flush=True)
@@ -353,6 +490,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

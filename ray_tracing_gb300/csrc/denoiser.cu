@@ -45,9 +45,14 @@ constexpr int kMaxCout = 64;
 constexpr int kMaxCin = 128;
 constexpr uint32_t kTmemCols = 64;
 constexpr int kSpin = 1 << 22;
-// The whole opt-in shared memory of a CTA: the kernel needs at most
-// 128 + 16 * 2944 + 9 * 128 * 64 * 2 bytes, and one CTA runs per SM anyway.
+// Opt-in shared-memory ceiling; a launch asks for what its layer needs
+// (conv_smem_bytes), so small layers run several CTAs per SM.
 constexpr int kConvSmem = 227 * 1024;
+
+int conv_smem_bytes(int cin, int cout) {
+    const int need = 128 + (cin / 8) * kBoxStride + 9 * cin * cout * 2;
+    return (need + 1023) & ~1023;
+}
 
 struct ConvArgs {
     int n, h, w, cin, cout;
@@ -240,6 +245,10 @@ cudaError_t conv_init() {
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [] {
         attr = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmem);
+        if (attr == cudaSuccess) {
+            attr = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributePreferredSharedMemoryCarveout,
+                cudaSharedmemCarveoutMaxShared);
+        }
     });
     return attr;
 }
@@ -251,9 +260,17 @@ cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin,
     if (attr != cudaSuccess) return attr;
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
         static_cast<__nv_bfloat16*>(y), err};
+    const int smem = conv_smem_bytes(cin, cout);
+    // resident CTAs per SM: 228 KB of shared memory (1 KB reserved per CTA),
+    // 512 TMEM columns (kTmemCols each), 16 CTAs of 128 threads
+    int per_sm = (228 * 1024) / (smem + 1024);
+    per_sm = per_sm < static_cast<int>(512 / kTmemCols) ? per_sm : static_cast<int>(512 / kTmemCols);
+    per_sm = per_sm < 16 ? per_sm : 16;
+    per_sm = per_sm > 1 ? per_sm : 1;
     const long long tiles = static_cast<long long>((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * n;
-    const int grid = static_cast<int>(tiles < grid_limit ? tiles : grid_limit);
-    k_conv3x3<<<grid > 0 ? grid : 1, 128, kConvSmem, stream>>>(map, a);
+    const long long cap = static_cast<long long>(grid_limit) * per_sm;
+    const int grid = static_cast<int>(tiles < cap ? tiles : cap);
+    k_conv3x3<<<grid > 0 ? grid : 1, 128, smem, stream>>>(map, a);
     return cudaGetLastError();
 }
 
