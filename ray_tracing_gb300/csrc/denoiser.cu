@@ -18,7 +18,13 @@
 //   * the epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
 //     lanes 32w..32w+31, i.e. tile rows 4w..4w+3), adds the bias, applies ReLU
 //     and stores BF16 into an NHWC tensor at a channel offset, so encoder
-//     outputs land directly in the decoder's concatenation buffers.
+//     outputs land directly in the decoder's concatenation buffers;
+//   * two fused epilogues serve the U-Net: `pool` also writes the 2 x 2
+//     average of the (BF16-rounded) output at half resolution, the four pixels
+//     of a pooling window being lanes l, l+1, l+8, l+9 of one warp (tiles start
+//     at even coordinates), and `up` writes every output pixel to the 2 x 2
+//     block of a twice-as-large tensor (nearest upsampling into the decoder's
+//     concatenation buffer).
 // The grid is persistent (one CTA per SM); every mbarrier wait is bounded.
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -61,6 +67,9 @@ struct ConvArgs {
     const float* bias;     // cout
     __nv_bfloat16* y;
     int* err;
+    // fused epilogue variants (k_conv3x3's comment)
+    __nv_bfloat16* pool;   // non-null: also write the 2x2 average of the output (dense cout channels)
+    int up;                // non-zero: y is twice the input size, each output pixel written 2 x 2
 };
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
@@ -150,27 +159,68 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
         const int yy = y0 + (m >> 3);
         const int xx = x0 + (m & 7);
         const bool inside = yy < a.h && xx < a.w;
+        const int oh = a.up ? 2 * a.h : a.h, ow = a.up ? 2 * a.w : a.w;
+        const int oy = a.up ? 2 * yy : yy, ox = a.up ? 2 * xx : xx;
         __nv_bfloat16* out =
-            a.y + ((static_cast<long long>(img) * a.h + yy) * a.w + xx) * a.y_channels + a.y_offset;
+            a.y + ((static_cast<long long>(img) * oh + oy) * ow + ox) * a.y_channels + a.y_offset;
+        const int ph = (a.h + 1) >> 1, pw = (a.w + 1) >> 1;
         for (int g = 0; g < (a.cout >> 4); ++g) {
             uint32_t v[16];
             tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v);
             tc::tmem_wait_ld();
+            uint32_t packed[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
+                float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
+                if (a.relu) {
+                    lo = fmaxf(lo, 0.0f);
+                    hi = fmaxf(hi, 0.0f);
+                }
+                packed[k] = pack_bf16x2(lo, hi);
+            }
+            const uint4 q0 = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+            const uint4 q1 = make_uint4(packed[4], packed[5], packed[6], packed[7]);
             if (inside) {
-                uint32_t packed[8];
+                if (a.up) {
+                    for (int dy = 0; dy < 2; ++dy) {
+                        for (int dx = 0; dx < 2; ++dx) {
+                            if (oy + dy >= oh || ox + dx >= ow) continue;
+                            uint4* dst = reinterpret_cast<uint4*>(out + (static_cast<long long>(dy) * ow + dx) * a.y_channels + g * 16);
+                            dst[0] = q0;
+                            dst[1] = q1;
+                        }
+                    }
+                } else {
+                    uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
+                    dst[0] = q0;
+                    dst[1] = q1;
+                }
+            }
+            if (a.pool != nullptr) {
+                // 2x2 window: this lane, lane+1 (next column), lane+8 (next row), lane+9
+                const float cnt0 = inside ? 1.0f : 0.0f;
+                const float cnt1 = cnt0 + __shfl_down_sync(0xffffffffu, cnt0, 1);
+                const float cnt = cnt1 + __shfl_down_sync(0xffffffffu, cnt1, 8);
+                uint32_t pooled[8];
 #pragma unroll
                 for (int k = 0; k < 8; ++k) {
-                    float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
-                    float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
-                    if (a.relu) {
-                        lo = fmaxf(lo, 0.0f);
-                        hi = fmaxf(hi, 0.0f);
-                    }
-                    packed[k] = pack_bf16x2(lo, hi);
+                    const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&packed[k]);
+                    float lo = inside ? __low2float(b2) : 0.0f;
+                    float hi = inside ? __high2float(b2) : 0.0f;
+                    lo += __shfl_down_sync(0xffffffffu, lo, 1);
+                    hi += __shfl_down_sync(0xffffffffu, hi, 1);
+                    lo += __shfl_down_sync(0xffffffffu, lo, 8);
+                    hi += __shfl_down_sync(0xffffffffu, hi, 8);
+                    const float inv = cnt > 0.0f ? 1.0f / cnt : 0.0f;
+                    pooled[k] = pack_bf16x2(lo * inv, hi * inv);
                 }
-                uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
-                dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-                dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+                if (inside && ((m >> 3) & 1) == 0 && (m & 1) == 0) {
+                    uint4* dst = reinterpret_cast<uint4*>(
+                        a.pool + ((static_cast<long long>(img) * ph + (yy >> 1)) * pw + (xx >> 1)) * a.cout + g * 16);
+                    dst[0] = make_uint4(pooled[0], pooled[1], pooled[2], pooled[3]);
+                    dst[1] = make_uint4(pooled[4], pooled[5], pooled[6], pooled[7]);
+                }
             }
         }
         tc::tc_fence_before();
@@ -255,11 +305,12 @@ cudaError_t conv_init() {
 
 // Launches k_conv3x3; `map` must describe x (conv_input_map).
 cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
-    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream) {
+    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream,
+    void* pool = nullptr, int up = 0) {
     const cudaError_t attr = conv_init();
     if (attr != cudaSuccess) return attr;
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
-        static_cast<__nv_bfloat16*>(y), err};
+        static_cast<__nv_bfloat16*>(y), err, static_cast<__nv_bfloat16*>(pool), up};
     const int smem = conv_smem_bytes(cin, cout);
     // resident CTAs per SM: 228 KB of shared memory (1 KB reserved per CTA),
     // 512 TMEM columns (kTmemCols each), 16 CTAs of 128 threads
@@ -631,25 +682,33 @@ cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, 
     if (net == nullptr) return cudaErrorMemoryAllocation;
     const long long full = static_cast<long long>(n) * h * w;
     const int h2 = (h + 1) / 2, w2 = (w + 1) / 2, h4 = (h2 + 1) / 2, w4 = (w2 + 1) / 2;
-    auto conv = [&](int li, int hh, int ww, void* y, int ych, int yoff) {
+    auto conv = [&](int li, int hh, int ww, void* y, int ych, int yoff, void* pool = nullptr, int up = 0) {
         const LayerSpec& l = kLayers[li];
         return launch_conv3x3(net->maps[li], n, hh, ww, l.cin, unet->weights[li].p, static_cast<const float*>(unet->biases[li].p),
-            l.cout, l.relu, y, ych, yoff, err, sms, stream);
+            l.cout, l.relu, y, ych, yoff, err, sms, stream, pool, up);
     };
     cudaError_t e;
     k_dn_pack<<<grid_for(full, sms), 256, 0, stream>>>(fp, pixel_offset, full, net->in16);
     if ((e = conv(0, h, w, net->t1, 32, 0)) != cudaSuccess) return e;
-    if ((e = conv(1, h, w, net->cat1, 80, 0)) != cudaSuccess) return e;
-    k_dn_pool<<<grid_for(static_cast<long long>(n) * h2 * w2 * 4, sms), 256, 0, stream>>>(net->cat1, n, h, w, 80, 32, net->p1);
+    // the encoder's second convolutions also write the pooled tensor; the
+    // decoder inputs' upsampled halves are written by the layer below them
+    if ((e = conv(1, h, w, net->cat1, 80, 0, net->p1)) != cudaSuccess) return e;
     if ((e = conv(2, h2, w2, net->t2, 48, 0)) != cudaSuccess) return e;
-    if ((e = conv(3, h2, w2, net->cat2, 112, 0)) != cudaSuccess) return e;
-    k_dn_pool<<<grid_for(static_cast<long long>(n) * h4 * w4 * 6, sms), 256, 0, stream>>>(net->cat2, n, h2, w2, 112, 48, net->p2);
+    if ((e = conv(3, h2, w2, net->cat2, 112, 0, net->p2)) != cudaSuccess) return e;
     if ((e = conv(4, h4, w4, net->t3, 64, 0)) != cudaSuccess) return e;
-    if ((e = conv(5, h4, w4, net->t3b, 64, 0)) != cudaSuccess) return e;
-    k_dn_upsample<<<grid_for(static_cast<long long>(n) * h2 * w2 * 8, sms), 256, 0, stream>>>(net->t3b, n, h2, w2, 64, net->cat2, 112, 48);
+    if (2 * h4 == h2 && 2 * w4 == w2) {
+        if ((e = conv(5, h4, w4, net->cat2, 112, 48, nullptr, 1)) != cudaSuccess) return e;
+    } else {
+        if ((e = conv(5, h4, w4, net->t3b, 64, 0)) != cudaSuccess) return e;
+        k_dn_upsample<<<grid_for(static_cast<long long>(n) * h2 * w2 * 8, sms), 256, 0, stream>>>(net->t3b, n, h2, w2, 64, net->cat2, 112, 48);
+    }
     if ((e = conv(6, h2, w2, net->t4, 48, 0)) != cudaSuccess) return e;
-    if ((e = conv(7, h2, w2, net->t4b, 48, 0)) != cudaSuccess) return e;
-    k_dn_upsample<<<grid_for(full * 6, sms), 256, 0, stream>>>(net->t4b, n, h, w, 48, net->cat1, 80, 32);
+    if (2 * h2 == h && 2 * w2 == w) {
+        if ((e = conv(7, h2, w2, net->cat1, 80, 32, nullptr, 1)) != cudaSuccess) return e;
+    } else {
+        if ((e = conv(7, h2, w2, net->t4b, 48, 0)) != cudaSuccess) return e;
+        k_dn_upsample<<<grid_for(full * 6, sms), 256, 0, stream>>>(net->t4b, n, h, w, 48, net->cat1, 80, 32);
+    }
     if ((e = conv(8, h, w, net->t5, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(9, h, w, net->t6, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(10, h, w, net->out16, 16, 0)) != cudaSuccess) return e;
