@@ -388,9 +388,10 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(args.warmup):
         r.render_frame(rig, prof, CAMERAS)
     # raygen, (trace, reset, shade, shadow) per bounce, the three ReSTIR passes,
-    # finalize, resolve; the denoiser: pack, 11 convolutions, 2 pools,
-    # 2 upsamples, unpack per batch of equal-size cameras (one batch here)
-    launches_per_frame = 1 + 4 * prof.max_bounces + 3 + 2 + (17 if weights is not None else 0)
+    # finalize, resolve; the denoiser: pack, 11 convolutions (pooling and
+    # upsampling fused into them at these even sizes), unpack per batch of
+    # equal-size cameras (one batch here)
+    launches_per_frame = 1 + 4 * prof.max_bounces + 3 + 2 + (13 if weights is not None else 0)
 
     sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
                            if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)
