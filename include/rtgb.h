@@ -451,6 +451,22 @@ rtgb_status rtgb_tonemap_rgba8(rtgb_handle handle, int32_t camera_index, uint8_t
 
 rtgb_status rtgb_acceleration_info_get(rtgb_handle handle, rtgb_acceleration_info* out);
 
+/* Device identity, toolkit versions and device-global memory use (the
+ * RunEnvironment / GPU memory fields of the reference's benchmark report,
+ * utils/render_realtime.cpp:55-134). */
+typedef struct rtgb_device_info {
+    char name[256];
+    int32_t device;
+    int32_t major, minor;            /* compute capability */
+    int32_t multiprocessors;
+    int32_t driver_version;          /* cudaDriverGetVersion */
+    int32_t runtime_version;         /* cudaRuntimeGetVersion */
+    uint64_t total_bytes;
+    uint64_t used_bytes;             /* total - free (all processes) */
+} rtgb_device_info;
+
+rtgb_status rtgb_device_info_get(rtgb_handle handle, rtgb_device_info* out);
+
 /* The CUDA stream (cudaStream_t) every launch of this handle is issued on. */
 void* rtgb_stream(rtgb_handle handle);
 
@@ -521,6 +537,10 @@ rtgb_status rtgb_profile_preset(const char* name, rtgb_render_profile* out_profi
 /* denoised beauty and denoise_ms its device time. Without parameters the    */
 /* plain accumulated beauty is returned (the reference's no-denoiser path).  */
 /* ------------------------------------------------------------------------ */
+
+/* Loads the parameters from a file of exactly rtgb_denoiser_param_count()
+ * little-endian BF16 values (ray_tracing_gb300/weights/denoiser_unet.bf16). */
+rtgb_status rtgb_load_denoiser_file(rtgb_handle handle, const char* path);
 
 /* Number of network parameters rtgb_set_denoiser_params expects. */
 int64_t rtgb_denoiser_param_count(void);

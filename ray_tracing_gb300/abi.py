@@ -85,6 +85,12 @@ class OpenPbrMaterial(C.Structure):
         return m
 
 
+class DeviceInfo(C.Structure):
+    _fields_ = [("name", C.c_char * 256), ("device", C.c_int32), ("major", C.c_int32), ("minor", C.c_int32),
+                ("multiprocessors", C.c_int32), ("driver_version", C.c_int32), ("runtime_version", C.c_int32),
+                ("total_bytes", C.c_uint64), ("used_bytes", C.c_uint64)]
+
+
 class Sphere(C.Structure):
     _fields_ = [("center", f3), ("radius", C.c_float), ("material_index", C.c_int32)]
 
@@ -237,6 +243,8 @@ SIGNATURES = {
     "rtgb_default_rig": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, P(CameraRig)]),
     "rtgb_profile_preset": (C.c_int, [C.c_char_p, P(RenderProfile)]),
     "rtgb_denoiser_param_count": (C.c_int64, []),
+    "rtgb_load_denoiser_file": (C.c_int, [Handle, C.c_char_p]),
+    "rtgb_device_info_get": (C.c_int, [Handle, C.c_void_p]),
     "rtgb_set_denoiser_params": (C.c_int, [Handle, C.c_void_p, C.c_int64]),
     "rtgb_conv3x3_pack_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p]),
     "rtgb_conv3x3_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,

@@ -98,8 +98,29 @@ def build_oracle() -> Path:
     return ORACLE_LIB
 
 
+CLI_SRC = CSRC / "cli" / "render_realtime.cpp"
+CLI = PKG / "_bin" / "render_realtime"
+
+
+def build_cli() -> Path:
+    """The render_realtime CLI (C++23 over the C ABI), linked against librtgb.so."""
+    CLI.parent.mkdir(exist_ok=True)
+    deps = [CLI_SRC, CSRC / "cli" / "benchmark_report.h", CSRC / "cli" / "png_writer.h", INCLUDE / "rtgb.h", LIB]
+    if _stale(CLI, deps):
+        rev = "unknown"
+        try:
+            rev = subprocess.run(["git", "-C", str(ROOT), "rev-parse", "HEAD"], capture_output=True, text=True,
+                                 timeout=10).stdout.strip() or "unknown"
+        except (OSError, subprocess.SubprocessError):
+            pass
+        _run(["g++", *CXX_FLAGS, f"-DRTGB_SOURCE_REVISION=\"{rev}\"", "-I", str(INCLUDE), "-I", str(CSRC / "cli"),
+              str(CLI_SRC), "-L", str(LIB_DIR), "-lrtgb", "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(CLI)])
+    return CLI
+
+
 def build_all(verbose: bool = False) -> None:
     build_product(verbose=verbose)
+    build_cli()
     build_oracle()
 
 

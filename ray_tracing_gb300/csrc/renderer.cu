@@ -8,6 +8,7 @@
 // once as a CUDA graph and replayed.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -990,8 +991,9 @@ struct rtgb_renderer {
         float dn = 0.0f;
         if (last_denoised) RTGB_CHECK(cudaEventElapsedTime(&dn, ev_dn0, ev_dn1));
         last_denoise_ms = dn;
+        // per camera, the reference's RadianceTiming: render and denoise are separate stages
         for (int c = 0; c < out->camera_count; ++c) {
-            out->cameras[c].render_ms = ms;
+            out->cameras[c].render_ms = ms - dn;
             out->cameras[c].denoise_ms = dn;
         }
         const Counters& k = *h_counters;
@@ -1201,6 +1203,51 @@ rtgb_status rtgb_set_denoiser_params(rtgb_handle h, const float* params, int64_t
 
 int64_t rtgb_denoiser_param_count(void) { return rtgb::unet_param_count(); }
 
+rtgb_status rtgb_load_denoiser_file(rtgb_handle h, const char* path) {
+    if (!h || !path) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        FILE* f = std::fopen(path, "rb");
+        if (!f) throw Invalid{std::string("cannot open denoiser weights: ") + path};
+        const long long n = rtgb::unet_param_count();
+        std::vector<uint16_t> bits(static_cast<size_t>(n));
+        const size_t got = std::fread(bits.data(), 2, bits.size(), f);
+        const int extra = std::fgetc(f);
+        std::fclose(f);
+        if (got != bits.size() || extra != EOF) {
+            throw Invalid{std::string("denoiser weights must hold exactly ") + std::to_string(n) + " BF16 values: " + path};
+        }
+        std::vector<float> params(bits.size());
+        for (size_t i = 0; i < bits.size(); ++i) {
+            const uint32_t u = static_cast<uint32_t>(bits[i]) << 16;
+            std::memcpy(&params[i], &u, 4);
+        }
+        h->set_denoiser(params.data(), n);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_device_info_get(rtgb_handle h, rtgb_device_info* out) {
+    if (!h || !out) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        *out = rtgb_device_info{};
+        RTGB_CHECK(cudaSetDevice(h->device));
+        cudaDeviceProp prop{};
+        RTGB_CHECK(cudaGetDeviceProperties(&prop, h->device));
+        std::snprintf(out->name, sizeof out->name, "%s", prop.name);
+        out->device = h->device;
+        out->major = prop.major;
+        out->minor = prop.minor;
+        out->multiprocessors = prop.multiProcessorCount;
+        RTGB_CHECK(cudaDriverGetVersion(&out->driver_version));
+        RTGB_CHECK(cudaRuntimeGetVersion(&out->runtime_version));
+        size_t free_b = 0, total_b = 0;
+        RTGB_CHECK(cudaMemGetInfo(&free_b, &total_b));
+        out->total_bytes = total_b;
+        out->used_bytes = total_b - free_b;
+        return RTGB_OK;
+    });
+}
+
 rtgb_status rtgb_download_reservoirs(rtgb_handle h, int32_t c, void* host, size_t bytes) {
     if (!h || !host) return RTGB_INVALID_ARGUMENT;
     return guarded(h, [&] {
@@ -1267,8 +1314,8 @@ rtgb_status rtgb_tonemap_rgba8(rtgb_handle h, int32_t c, uint8_t* host) {
         h->check_camera(c);
         const size_t n = static_cast<size_t>(h->last_w[c]) * h->last_h[c];
         h->debug_rgba.ensure(n * 4);
-        launch_tonemap(h->frames[h->last].beauty + h->last_pixel_offset[c], h->debug_rgba.as<uint8_t>(),
-            static_cast<long long>(n), h->stream);
+        const float4* src = h->last_denoised ? h->denoised.as<float4>() : h->frames[h->last].beauty;
+        launch_tonemap(src + h->last_pixel_offset[c], h->debug_rgba.as<uint8_t>(), static_cast<long long>(n), h->stream);
         RTGB_CHECK(cudaGetLastError());
         RTGB_CHECK(cudaMemcpyAsync(host, h->debug_rgba.p, n * 4, cudaMemcpyDeviceToHost, h->stream));
         RTGB_CHECK(cudaStreamSynchronize(h->stream));

@@ -25,7 +25,9 @@ import numpy as np
 LAYERS = [  # (in, out) of the 11 convolutions, in order
     (10, 32), (32, 32), (32, 48), (48, 48), (48, 64), (64, 64), (112, 48), (48, 48), (80, 32), (32, 32), (32, 3),
 ]
-WEIGHTS = Path(__file__).resolve().parent / "weights" / "denoiser_unet.npz"
+# the trained parameters: param_count() little-endian BF16 values, layer order
+# (also read by rtgb_load_denoiser_file); training metadata beside it as JSON
+WEIGHTS = Path(__file__).resolve().parent / "weights" / "denoiser_unet.bf16"
 
 
 def param_count() -> int:
@@ -112,5 +114,15 @@ def load_weights(path: Path = WEIGHTS) -> np.ndarray | None:
     """The trained parameters shipped with the package (BF16), as float32."""
     if not path.exists():
         return None
-    with np.load(path) as d:
-        return from_bf16_bits(d["params_bf16"])
+    bits = np.fromfile(path, dtype="<u2")
+    if bits.size != param_count():
+        raise ValueError(f"{path}: {bits.size} values, expected {param_count()}")
+    return from_bf16_bits(bits)
+
+
+def save_weights(flat: np.ndarray, path: Path = WEIGHTS, meta: dict | None = None) -> None:
+    import json
+    path.parent.mkdir(parents=True, exist_ok=True)
+    to_bf16_bits(flat).astype("<u2").tofile(path)
+    if meta is not None:
+        path.with_suffix(".json").write_text(json.dumps(meta, indent=1) + "\n")

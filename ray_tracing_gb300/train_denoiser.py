@@ -10,7 +10,7 @@ The network (ray_tracing_gb300/denoiser.py) is trained on random crops with an
 L1 loss on log1p(radiance) and saved as BF16 parameters in the layer order of
 rtgb_set_denoiser_params.
 
-    python -m ray_tracing_gb300.train_denoiser --out ray_tracing_gb300/weights/denoiser_unet.npz
+    python -m ray_tracing_gb300.train_denoiser --out ray_tracing_gb300/weights/denoiser_unet.bf16
 
 Training runs on PyTorch (the optimiser and autograd are tooling); inference
 in the renderer runs on the library's tensor-core kernels.
@@ -134,10 +134,10 @@ def main(argv=None):
                 noisy = ((vx[..., 0:3] - vy) ** 2 / (vy ** 2 + 1e-2)).mean().item()
             print(f"step {step}: loss {loss.item():.4f}  valid relMSE {rel:.5f} (noisy {noisy:.5f})", flush=True)
     flat = denoiser.flatten(model)
-    args.out.parent.mkdir(parents=True, exist_ok=True)
-    np.savez_compressed(args.out, params_bf16=denoiser.to_bf16_bits(flat),
-                        train_scenes=np.array([f"{n}/{s}/{d}" for n, s, d in TRAIN_SCENES]),
-                        target_spp=np.array(args.target_spp), steps=np.array(args.steps))
+    denoiser.save_weights(flat, args.out, {
+        "train_scenes": [f"{n}/{s}/{d}" for n, s, d in TRAIN_SCENES], "valid_scene": "/".join(map(str, VALID_SCENE)),
+        "target_spp": args.target_spp, "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
+        "valid_relmse": rel, "valid_noisy_relmse": noisy})
     print(f"saved {args.out} ({time.time() - t0:.1f} s)")
 
 

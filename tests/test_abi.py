@@ -35,7 +35,7 @@ STRUCTS = {
     "rtgb_render_profile": abi.RenderProfile, "rtgb_create_info": abi.CreateInfo,
     "rtgb_camera_frame_view": abi.CameraFrameView, "rtgb_frame_views": abi.FrameViews,
     "rtgb_restir_stats": abi.RestirDiagnostics, "rtgb_acceleration_info": abi.AccelerationInfo,
-    "rtgb_openpbr_material": abi.OpenPbrMaterial,
+    "rtgb_openpbr_material": abi.OpenPbrMaterial, "rtgb_device_info": abi.DeviceInfo,
 }
 
 
