@@ -366,6 +366,12 @@ typedef struct rtgb_acceleration_info {
     int32_t analytic_bvh_light_count; /* finite, non-point analytic lights in the light BVH */
     float build_ms;               /* device build time (Morton, sort, hierarchy, bounds) */
     int32_t traversal_stack_overflows; /* count since the last prepare; always reported, never silent */
+    /* AccelerationUpdateKind of the last rtgb_prepare_scene (gpu_scene_acceleration.cpp:247-295):
+     * 0 reuse (nothing changed), 1 update (non-geometry data changed),
+     * 2 refit (same primitive counts, geometry changed: node boxes refitted
+     * over the kept hierarchy), 3 rebuild */
+    int32_t update_kind;
+    int32_t generation;           /* incremented by every update, refit and rebuild */
 } rtgb_acceleration_info;
 
 /* Replaces OptixRenderer::OptixRenderer + RendererPool(int) (optix_renderer.cpp:104-109,
@@ -488,6 +494,12 @@ rtgb_status rtgb_download_path_records(rtgb_handle handle, int32_t camera_index,
  * primitive_count-1 respectively. */
 rtgb_status rtgb_download_lbvh(rtgb_handle handle, uint32_t* sorted_morton,
     int32_t* sorted_primitive, int32_t* node_children /* 2 per node */);
+
+/* The internal nodes' child boxes, 12 floats per node (left lo.xyz, left
+ * hi.xyz, right lo.xyz, right hi.xyz), primitive_count-1 nodes: what a refit
+ * (rtgb_acceleration_info::update_kind 2) rewrites
+ * (GpuSceneAcceleration::refit, gpu_scene_acceleration.cpp:347-365). */
+rtgb_status rtgb_download_lbvh_boxes(rtgb_handle handle, float* child_boxes);
 
 /* ------------------------------------------------------------------------ */
 /* Host-side authoring helpers (C++23 host code in the same library).        */

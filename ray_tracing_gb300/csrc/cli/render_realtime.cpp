@@ -372,11 +372,12 @@ int run(const Args& a) {
         report.gpu_scheduling.task_submission_count = static_cast<uint64_t>(a.warmup_frames + a.frames);
         report.gpu_scheduling.launch_parameter_allocation_count = 1;
         report.gpu_scheduling.launch_parameter_upload_count = static_cast<uint64_t>(a.warmup_frames + a.frames);
-        report.gpu_scheduling.acceleration_update_kind = "rebuild";
+        static const char* const kKinds[4] = {"reuse", "update", "refit", "rebuild"};
+        report.gpu_scheduling.acceleration_update_kind = kKinds[acc.update_kind >= 0 && acc.update_kind < 4 ? acc.update_kind : 3];
         report.gpu_scheduling.acceleration_update_ms = acc.build_ms;
         report.gpu_scheduling.acceleration_node_count = acc.node_count;
         report.gpu_scheduling.acceleration_reference_count = acc.primitive_count;
-        report.gpu_scheduling.acceleration_generation = 1;
+        report.gpu_scheduling.acceleration_generation = static_cast<uint64_t>(acc.generation);
         report.aggregate = rtgb::report::aggregate_of(report.frames);
         const auto csv = out_dir / "benchmark_frames.csv";
         const auto json = out_dir / "benchmark_summary.json";

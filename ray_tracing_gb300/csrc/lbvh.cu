@@ -310,4 +310,14 @@ cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals,
     return cudaGetLastError();
 }
 
+cudaError_t lbvh_refit(LbvhScratch& s, int n, const int* sorted_vals, const int* children, const int* parent,
+    BvhNode* nodes, cudaStream_t stream) {
+    if (n < 2) return cudaErrorInvalidValue;
+    const int threads = 256;
+    cudaMemsetAsync(s.flags, 0, static_cast<size_t>(n) * sizeof(int), stream);
+    k_bounds<<<(n + threads - 1) / threads, threads, 0, stream>>>(s.aabb_lo, s.aabb_hi, sorted_vals, n, children,
+        parent, s.flags, s.node_lo, s.node_hi, nodes);
+    return cudaGetLastError();
+}
+
 }  // namespace rtgb

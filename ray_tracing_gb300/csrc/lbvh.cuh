@@ -32,6 +32,14 @@ LbvhScratch lbvh_carve(void* base, int n);
 cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals, uint32_t** sorted_keys,
     cudaStream_t stream);
 
+// Refits the node boxes of an existing hierarchy (children/parent of an
+// earlier lbvh_build over the same primitive count, leaf order `sorted_vals`)
+// to the boxes now in s.aabb_lo/hi: the bottom-up bounds pass of the build
+// without Morton codes, sort or hierarchy (GpuSceneAcceleration::refit,
+// src/realtime/gpu/gpu_scene_acceleration.cpp:347-365).
+cudaError_t lbvh_refit(LbvhScratch& s, int n, const int* sorted_vals, const int* children, const int* parent,
+    BvhNode* nodes, cudaStream_t stream);
+
 // Morton code of a centroid inside the centroid bounds, 10 bits per axis.
 // The CPU restatement in oracle/lbvh_oracle.cpp follows it operation for operation.
 RTGB_HD uint32_t expand_bits10(uint32_t v) {

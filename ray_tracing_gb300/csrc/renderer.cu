@@ -137,6 +137,30 @@ struct DevBuf {
     }
 };
 
+// A build-time scratch buffer freed when it leaves scope (cudaFree waits for
+// the work that uses it), also when the build throws.
+struct ScopedBuf : DevBuf {
+    ScopedBuf() = default;
+    ScopedBuf(const ScopedBuf&) = delete;
+    ScopedBuf& operator=(const ScopedBuf&) = delete;
+    ~ScopedBuf() { release(); }
+};
+
+// Timing events destroyed on every exit path.
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        RTGB_CHECK(cudaEventCreate(&a));
+        RTGB_CHECK(cudaEventCreate(&b));
+    }
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
 template <typename T>
 T* upload(DevBuf& buf, const T* host, size_t count, cudaStream_t stream) {
     buf.ensure(std::max<size_t>(count, 1) * sizeof(T));
@@ -196,6 +220,15 @@ struct rtgb_renderer {
     int prim_count = 0;
     int analytic_bvh_count = 0;
     float build_ms = 0.0f;
+    // acceleration lifecycle (GpuSceneAcceleration, gpu_scene_acceleration.cpp:247-295):
+    // the hierarchy's children/parent survive so a geometry change with the
+    // same primitive counts refits the boxes instead of rebuilding
+    DevBuf bvh_children, bvh_parent;
+    bool accel_valid = false;
+    int accel_counts[3] = {-1, -1, -1};
+    uint64_t geometry_sig = 0, scene_sig = 0;
+    int update_kind = 3;
+    int generation = 0;
 
     // frame state
     uint32_t sample_stream = 0;
@@ -267,7 +300,7 @@ struct rtgb_renderer {
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_nrm, &denoised};
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_nrm, &denoised, &bvh_children, &bvh_parent};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -368,16 +401,99 @@ struct rtgb_renderer {
         if (surfaces >= (1ll << 28)) throw Invalid{"scene exceeds 2^28 surface primitives"};
     }
 
+    // FNV-1a over 64-bit words, the tail byte by byte. It detects changes the
+    // way the geometry and scene signatures of gpu_scene_acceleration.cpp:116-135
+    // do, eight bytes per step: each step is a bijection of the running hash,
+    // so inputs differing in one word always hash differently.
+    static uint64_t fnv_words(uint64_t h, const void* data, size_t bytes) {
+        constexpr uint64_t kPrime = 1099511628211ull;
+        const unsigned char* p = static_cast<const unsigned char*>(data);
+        size_t i = 0;
+        for (; i + 8 <= bytes; i += 8) {
+            uint64_t w;
+            std::memcpy(&w, p + i, 8);
+            h = (h ^ w) * kPrime;
+        }
+        for (; i < bytes; ++i) h = (h ^ p[i]) * kPrime;
+        return h;
+    }
+
+    template <typename T>
+    static uint64_t fnv_array(uint64_t h, const T* data, long long count) {
+        const long long n = count > 0 && data ? count : 0;
+        h = fnv_words(h, &n, sizeof n);
+        return n > 0 ? fnv_words(h, data, static_cast<size_t>(n) * sizeof(T)) : h;
+    }
+
+    static uint64_t geometry_signature(const rtgb_scene& s) {
+        uint64_t h = 14695981039346656037ull;
+        h = fnv_array(h, s.spheres, s.sphere_count);
+        h = fnv_array(h, s.quads, s.quad_count);
+        return fnv_array(h, s.triangles, s.triangle_count);
+    }
+
+    // Everything prepare uploads besides geometry (the packed light list is a
+    // function of geometry and materials, so it needs no hash of its own).
+    static uint64_t scene_signature(const rtgb_scene& s, uint64_t geometry) {
+        uint64_t h = fnv_words(geometry, s.background, sizeof s.background);
+        h = fnv_array(h, s.media, s.medium_count);
+        h = fnv_array(h, s.textures, s.texture_count);
+        h = fnv_array(h, s.image_texels, 3ll * s.image_texel_count);
+        h = fnv_array(h, s.materials, s.material_count);
+        h = fnv_array(h, s.openpbr_materials, s.openpbr_material_count);
+        return fnv_array(h, s.analytic_lights, s.analytic_light_count);
+    }
+
+    // GpuSceneAcceleration::update + use_prepared_scene: reuse when nothing
+    // changed, update (re-upload, keep the hierarchy) when only non-geometry
+    // data changed, refit when the primitive counts are unchanged, else
+    // rebuild. Every kind restarts the sample stream and drops history.
     void prepare(const rtgb_scene& s) {
         validate_scene(s);
         RTGB_CHECK(cudaSetDevice(device));
         RTGB_CHECK(cudaStreamSynchronize(stream));
-        drop_graph();
-        prepared = false;
-        DeviceScene d{};
-        d.spheres = upload(spheres, s.spheres, static_cast<size_t>(s.sphere_count), stream);
-        d.quads = upload(quads, s.quads, static_cast<size_t>(s.quad_count), stream);
-        d.triangles = upload(triangles, s.triangles, static_cast<size_t>(s.triangle_count), stream);
+        const uint64_t geo = geometry_signature(s);
+        const uint64_t sig = scene_signature(s, geo);
+        const bool topology_changed = accel_counts[0] != s.sphere_count || accel_counts[1] != s.quad_count
+                                      || accel_counts[2] != s.triangle_count;
+        int kind = 0;
+        if (topology_changed || !accel_valid || !prepared) kind = 3;
+        else if (geo != geometry_sig) kind = 2;
+        else if (sig != scene_sig) kind = 1;
+        if (kind != 0) {
+            drop_graph();
+            prepared = false;
+            accel_valid = false;
+            upload_scene(s, kind);
+            accel_valid = true;
+            accel_counts[0] = s.sphere_count;
+            accel_counts[1] = s.quad_count;
+            accel_counts[2] = s.triangle_count;
+            geometry_sig = geo;
+            scene_sig = sig;
+            ++generation;
+        } else {
+            build_ms = 0.0f;
+        }
+        update_kind = kind;
+        prepared = true;
+        // use_prepared_scene: the sample stream restarts and history is dropped
+        sample_stream = 0;
+        reset_accumulation();
+        std::memset(h_counters, 0, sizeof(Counters));
+        RTGB_CHECK(cudaMemsetAsync(d_counters, 0, sizeof(Counters), stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+    }
+
+    // Uploads the scene for update kind 1 (non-geometry data; the primitives,
+    // records and hierarchy stay), 2 (refit) or 3 (rebuild).
+    void upload_scene(const rtgb_scene& s, int kind) {
+        DeviceScene d = kind == 1 ? scene : DeviceScene{};
+        if (kind >= 2) {
+            d.spheres = upload(spheres, s.spheres, static_cast<size_t>(s.sphere_count), stream);
+            d.quads = upload(quads, s.quads, static_cast<size_t>(s.quad_count), stream);
+            d.triangles = upload(triangles, s.triangles, static_cast<size_t>(s.triangle_count), stream);
+        }
         d.media = upload(media, s.media, static_cast<size_t>(s.medium_count), stream);
         d.materials = upload(materials, s.materials, static_cast<size_t>(s.material_count), stream);
         d.openpbr = s.openpbr_material_count > 0
@@ -470,12 +586,20 @@ struct rtgb_renderer {
         d.infinite_analytic = upload(infinite_analytic, inf.data(), inf.size(), stream);
         d.infinite_analytic_count = static_cast<int>(inf.size());
 
-        cudaEvent_t b0, b1;
-        RTGB_CHECK(cudaEventCreate(&b0));
-        RTGB_CHECK(cudaEventCreate(&b1));
-        RTGB_CHECK(cudaEventRecord(b0, stream));
+        EventPair ev;
+        RTGB_CHECK(cudaEventRecord(ev.a, stream));
+        if (kind >= 2) build_scene_bvh(s, d, kind);
+        build_analytic_bvh(s, finite, d);
+        RTGB_CHECK(cudaEventRecord(ev.b, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        RTGB_CHECK(cudaGetLastError());
+        RTGB_CHECK(cudaEventElapsedTime(&build_ms, ev.a, ev.b));
+        scene = d;
+    }
 
-        // scene LBVH
+    // Scene LBVH: a full device build (kind 3) that keeps children/parent, or
+    // a refit (kind 2) of the kept hierarchy to the new primitive boxes.
+    void build_scene_bvh(const rtgb_scene& s, DeviceScene& d, int kind) {
         const int n = s.sphere_count + s.quad_count + s.triangle_count;
         float scale = 0.0f;
         for (int i = 0; i < s.sphere_count; ++i)
@@ -489,14 +613,22 @@ struct rtgb_renderer {
         const float pad = 1e-5f + 1e-5f * scale;
         d.prim_count = n;
         prim_count = n;
-        DevBuf scratch, unsorted;
+        ScopedBuf scratch, unsorted;
         unsorted.ensure(static_cast<size_t>(n) * sizeof(PrimRecord));
         scratch.ensure(lbvh_scratch_bytes(n));
         LbvhScratch ls = lbvh_carve(scratch.p, n);
         PrimRecord* recs = static_cast<PrimRecord*>(prims.ensure(static_cast<size_t>(n) * sizeof(PrimRecord)));
         launch_prim_records(d, unsorted.as<PrimRecord>(), ls.aabb_lo, ls.aabb_hi, pad, stream);
         RTGB_CHECK(cudaGetLastError());
-        if (n >= 2) {
+        if (n >= 2 && kind == 2) {
+            // same counts: the kept leaf order and hierarchy, boxes refitted bottom-up
+            BvhNode* nd = nodes.as<BvhNode>();
+            RTGB_CHECK(lbvh_refit(ls, n, sorted_vals.as<int>(), bvh_children.as<int>(), bvh_parent.as<int>(), nd, stream));
+            launch_gather_records(unsorted.as<PrimRecord>(), sorted_vals.as<int>(), recs, n, stream);
+            RTGB_CHECK(cudaGetLastError());
+            d.nodes = nd;
+            d.node_count = n - 1;
+        } else if (n >= 2) {
             BvhNode* nd = static_cast<BvhNode*>(nodes.ensure(static_cast<size_t>(n - 1) * sizeof(BvhNode)));
             int* svals = nullptr;
             uint32_t* skeys = nullptr;
@@ -505,8 +637,14 @@ struct rtgb_renderer {
             RTGB_CHECK(cudaGetLastError());
             sorted_keys.ensure(static_cast<size_t>(n) * sizeof(uint32_t));
             sorted_vals.ensure(static_cast<size_t>(n) * sizeof(int));
+            bvh_children.ensure(2 * static_cast<size_t>(n - 1) * sizeof(int));
+            bvh_parent.ensure((2 * static_cast<size_t>(n) - 1) * sizeof(int));
             RTGB_CHECK(cudaMemcpyAsync(sorted_keys.p, skeys, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToDevice, stream));
             RTGB_CHECK(cudaMemcpyAsync(sorted_vals.p, svals, static_cast<size_t>(n) * 4, cudaMemcpyDeviceToDevice, stream));
+            RTGB_CHECK(cudaMemcpyAsync(bvh_children.p, ls.children, 2 * static_cast<size_t>(n - 1) * sizeof(int),
+                cudaMemcpyDeviceToDevice, stream));
+            RTGB_CHECK(cudaMemcpyAsync(bvh_parent.p, ls.parent, (2 * static_cast<size_t>(n) - 1) * sizeof(int),
+                cudaMemcpyDeviceToDevice, stream));
             d.nodes = nd;
             d.node_count = n - 1;
         } else {
@@ -515,8 +653,11 @@ struct rtgb_renderer {
             d.node_count = 0;
         }
         d.prims = recs;
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+    }
 
-        // analytic-light BVH (host boxes, device build)
+    // Analytic-light BVH over the finite lights (host boxes, device build).
+    void build_analytic_bvh(const rtgb_scene& s, const std::vector<int>& finite, DeviceScene& d) {
         const int nf = static_cast<int>(finite.size());
         d.analytic_bvh_count = nf;
         analytic_bvh_count = nf;
@@ -547,7 +688,7 @@ struct rtgb_renderer {
             }
             std::vector<int> leaf(static_cast<size_t>(nf));
             if (nf >= 2) {
-                DevBuf ascratch;
+                ScopedBuf ascratch;
                 ascratch.ensure(lbvh_scratch_bytes(nf));
                 LbvhScratch as = lbvh_carve(ascratch.p, nf);
                 RTGB_CHECK(cudaMemcpyAsync(as.aabb_lo, lo.data(), lo.size() * sizeof(float4), cudaMemcpyHostToDevice, stream));
@@ -559,7 +700,6 @@ struct rtgb_renderer {
                 std::vector<int> order(static_cast<size_t>(nf));
                 RTGB_CHECK(cudaMemcpyAsync(order.data(), svals, order.size() * sizeof(int), cudaMemcpyDeviceToHost, stream));
                 RTGB_CHECK(cudaStreamSynchronize(stream));
-                ascratch.release();
                 for (int k = 0; k < nf; ++k) leaf[static_cast<size_t>(k)] = finite[static_cast<size_t>(order[static_cast<size_t>(k)])];
                 d.analytic_nodes = an;
                 d.analytic_node_count = nf - 1;
@@ -570,22 +710,6 @@ struct rtgb_renderer {
         } else {
             d.analytic_leaf = nullptr;
         }
-        RTGB_CHECK(cudaEventRecord(b1, stream));
-        RTGB_CHECK(cudaStreamSynchronize(stream));
-        RTGB_CHECK(cudaGetLastError());
-        RTGB_CHECK(cudaEventElapsedTime(&build_ms, b0, b1));
-        cudaEventDestroy(b0);
-        cudaEventDestroy(b1);
-        scratch.release();
-        unsorted.release();
-        scene = d;
-        prepared = true;
-        // use_prepared_scene: the sample stream restarts and history is dropped
-        sample_stream = 0;
-        reset_accumulation();
-        std::memset(h_counters, 0, sizeof(Counters));
-        RTGB_CHECK(cudaMemsetAsync(d_counters, 0, sizeof(Counters), stream));
-        RTGB_CHECK(cudaStreamSynchronize(stream));
     }
 
     void reset_accumulation() {
@@ -1332,6 +1456,8 @@ rtgb_status rtgb_acceleration_info_get(rtgb_handle h, rtgb_acceleration_info* ou
     a.analytic_bvh_light_count = h->analytic_bvh_count;
     a.build_ms = h->build_ms;
     a.traversal_stack_overflows = h->h_counters ? h->h_counters->overflow : 0;
+    a.update_kind = h->update_kind;
+    a.generation = h->generation;
     *out = a;
     return RTGB_OK;
 }
@@ -1378,6 +1504,26 @@ rtgb_status rtgb_download_lbvh(rtgb_handle h, uint32_t* sorted_morton, int32_t* 
                 std::memcpy(&c1, &nodes[static_cast<size_t>(i)].b.w, 4);
                 children[2 * i] = c0;
                 children[2 * i + 1] = c1;
+            }
+        }
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_lbvh_boxes(rtgb_handle h, float* child_boxes) {
+    if (!h || !child_boxes) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->prepared) throw Invalid{"no scene prepared"};
+        const int n = h->prim_count;
+        if (n < 2) throw Invalid{"the scene has fewer than two primitives and no hierarchy"};
+        std::vector<BvhNode> nodes(static_cast<size_t>(n - 1));
+        RTGB_CHECK(cudaMemcpy(nodes.data(), h->nodes.p, nodes.size() * sizeof(BvhNode), cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < nodes.size(); ++i) {
+            const float4 q[4] = {nodes[i].a, nodes[i].b, nodes[i].c, nodes[i].d};
+            for (int k = 0; k < 4; ++k) {
+                child_boxes[12 * i + 3 * k] = q[k].x;
+                child_boxes[12 * i + 3 * k + 1] = q[k].y;
+                child_boxes[12 * i + 3 * k + 2] = q[k].z;
             }
         }
         return RTGB_OK;

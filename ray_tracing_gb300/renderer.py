@@ -192,3 +192,10 @@ class Renderer:
         self._check(self.lib.rtgb_download_lbvh(self.h, keys.ctypes.data, order.ctypes.data, children.ctypes.data),
                     "download_lbvh")
         return keys, order, children
+
+    def lbvh_boxes(self) -> np.ndarray:
+        """(nodes, 2, 2, 3): per internal node the left and right child's (lo, hi) box."""
+        n = self.acceleration_info().primitive_count
+        boxes = np.empty((max(n - 1, 0), 2, 2, 3), np.float32)
+        self._check(self.lib.rtgb_download_lbvh_boxes(self.h, boxes.ctypes.data), "download_lbvh_boxes")
+        return boxes
