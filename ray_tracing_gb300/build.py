@@ -5,6 +5,7 @@ Everything is compiled with nvcc/g++ directly (no cmake): CUDA sources for
 libraries land next to the code that loads them:
 
 * ``ray_tracing_gb300/_lib/librtgb.so`` — the product (C ABI of ``include/rtgb.h``)
+* ``ray_tracing_gb300/_bin/``            — render_realtime and benchmark_scene_lifecycle (C ABI users)
 * ``oracle/_bin/liborc.so``             — the CPU oracle (test infrastructure)
 
 Translation units compile in parallel and are skipped when up to date.
@@ -100,10 +101,13 @@ def build_oracle() -> Path:
 
 CLI_SRC = CSRC / "cli" / "render_realtime.cpp"
 CLI = PKG / "_bin" / "render_realtime"
+LIFECYCLE_SRC = CSRC / "cli" / "benchmark_scene_lifecycle.cpp"
+LIFECYCLE = PKG / "_bin" / "benchmark_scene_lifecycle"
 
 
 def build_cli() -> Path:
-    """The render_realtime CLI (C++23 over the C ABI), linked against librtgb.so."""
+    """The render_realtime CLI and the scene-lifecycle benchmark (C++23 over the
+    C ABI), linked against librtgb.so."""
     CLI.parent.mkdir(exist_ok=True)
     deps = [CLI_SRC, CSRC / "cli" / "benchmark_report.h", CSRC / "cli" / "png_writer.h", INCLUDE / "rtgb.h", LIB]
     if _stale(CLI, deps):
@@ -115,6 +119,9 @@ def build_cli() -> Path:
             pass
         _run(["g++", *CXX_FLAGS, f"-DRTGB_SOURCE_REVISION=\"{rev}\"", "-I", str(INCLUDE), "-I", str(CSRC / "cli"),
               str(CLI_SRC), "-L", str(LIB_DIR), "-lrtgb", "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(CLI)])
+    if _stale(LIFECYCLE, [LIFECYCLE_SRC, INCLUDE / "rtgb.h", LIB]):
+        _run(["g++", *CXX_FLAGS, "-I", str(INCLUDE), str(LIFECYCLE_SRC), "-L", str(LIB_DIR), "-lrtgb",
+              "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(LIFECYCLE)])
     return CLI
 
 
