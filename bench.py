@@ -7,7 +7,7 @@ Workload (one step = one frame of every camera):
   4 pinhole32 cameras 640x480, 1 spp, depth 4, ReSTIR DI with 32 initial
   candidates, temporal reuse and 1 spatial neighbour, BASIC bias correction,
   then the BF16 U-Net denoiser on the tensor cores (when its trained weights
-  are present: ray_tracing_gb300/weights/denoiser_unet.npz).
+  are present: ray_tracing_gb300/weights/denoiser_unet.bf16).
 
 value   = rays traced (primary + extension + shadow + ReSTIR visibility) per
           second of device time, inputs resident (Mrays/s); each frame is timed
@@ -357,8 +357,9 @@ def roofline(stage_ms, frames_stats, spatial):
     traffic = None
     tpath = ROOT / "profiles" / "roofline_traffic.json"
     if tpath.exists():
+        # DRAM bytes (read + write) per launch of each slot, from one ncu capture
         rec = json.loads(tpath.read_text()).get(name)
-        traffic = rec["dram_bytes"] if rec else None
+        traffic = float(rec) if isinstance(rec, (int, float)) else None
     frame_ms = sum(v[0] for v in slots.values())
     by_kernel = {}
     for k, v in slots.items():

@@ -25,7 +25,11 @@
 //     at even coordinates), and `up` writes every output pixel to the 2 x 2
 //     block of a twice-as-large tensor (nearest upsampling into the decoder's
 //     concatenation buffer).
-// The grid is persistent (one CTA per SM); every mbarrier wait is bounded.
+// The grid is persistent and each CTA software-pipelines its tiles: two halo
+// stages in shared memory and two accumulators in TMEM, so the TMA of tile
+// j + 1 and the epilogue of tile j - 1 run while the tensor core works on
+// tile j (one stage when two do not fit in shared memory). Layers small
+// enough keep several such CTAs on one SM. Every mbarrier wait is bounded.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -49,15 +53,27 @@ constexpr int kBoxStride = 2944;                  // boxes 128-byte aligned in s
 constexpr int kRowBytes = kHaloW * 16;            // next tile row of a box
 constexpr int kMaxCout = 64;
 constexpr int kMaxCin = 128;
-constexpr uint32_t kTmemCols = 64;
 constexpr int kSpin = 1 << 22;
 // Opt-in shared-memory ceiling; a launch asks for what its layer needs
 // (conv_smem_bytes), so small layers run several CTAs per SM.
 constexpr int kConvSmem = 227 * 1024;
 
+// Halo stages of a layer: two when they fit beside its weights, else one.
+int conv_stages(int cin, int cout) {
+    return 128 + 2 * (cin / 8) * kBoxStride + 9 * cin * cout * 2 <= kConvSmem ? 2 : 1;
+}
+
 int conv_smem_bytes(int cin, int cout) {
-    const int need = 128 + (cin / 8) * kBoxStride + 9 * cin * cout * 2;
+    const int need = 128 + conv_stages(cin, cout) * (cin / 8) * kBoxStride + 9 * cin * cout * 2;
     return (need + 1023) & ~1023;
+}
+
+// TMEM columns of a CTA: two FP32 accumulators of cout columns, rounded up to
+// the power of two tcgen05.alloc takes.
+uint32_t conv_tmem_cols(int cout) {
+    uint32_t cols = 32;
+    while (cols < static_cast<uint32_t>(2 * cout)) cols <<= 1;
+    return cols;
 }
 
 struct ConvArgs {
@@ -70,6 +86,8 @@ struct ConvArgs {
     // fused epilogue variants (k_conv3x3's comment)
     __nv_bfloat16* pool;   // non-null: also write the 2x2 average of the output (dense cout channels)
     int up;                // non-zero: y is twice the input size, each output pixel written 2 x 2
+    int stages;            // halo stages in shared memory (conv_stages)
+    uint32_t tmem_cols;    // conv_tmem_cols(cout)
 };
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
@@ -77,24 +95,104 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
     return *reinterpret_cast<const uint32_t*>(&v);
 }
 
+// Epilogue of one tile: the accumulators at TMEM column `acc` (this warp's 32
+// lanes = 4 tile rows) plus bias, ReLU, BF16 store, and the fused pooling or
+// upsampling variant.
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t acc, int tile, int tiles_x, int per_image,
+    int warp, int lane) {
+    const int img = tile / per_image;
+    const int t = tile - img * per_image;
+    const int ty = t / tiles_x;
+    const int x0 = (t - ty * tiles_x) * kTileW;
+    const int y0 = ty * kTileH;
+    const int m = warp * 32 + lane;
+    const int yy = y0 + (m >> 3);
+    const int xx = x0 + (m & 7);
+    const bool inside = yy < a.h && xx < a.w;
+    const int oh = a.up ? 2 * a.h : a.h, ow = a.up ? 2 * a.w : a.w;
+    const int oy = a.up ? 2 * yy : yy, ox = a.up ? 2 * xx : xx;
+    __nv_bfloat16* out = a.y + ((static_cast<long long>(img) * oh + oy) * ow + ox) * a.y_channels + a.y_offset;
+    const int ph = (a.h + 1) >> 1, pw = (a.w + 1) >> 1;
+    for (int g = 0; g < (a.cout >> 4); ++g) {
+        uint32_t v[16];
+        tc::tmem_ld16(acc + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v);
+        tc::tmem_wait_ld();
+        uint32_t packed[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
+            float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
+            if (a.relu) {
+                lo = fmaxf(lo, 0.0f);
+                hi = fmaxf(hi, 0.0f);
+            }
+            packed[k] = pack_bf16x2(lo, hi);
+        }
+        const uint4 q0 = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        const uint4 q1 = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+        if (inside) {
+            if (a.up) {
+                for (int dy = 0; dy < 2; ++dy) {
+                    for (int dx = 0; dx < 2; ++dx) {
+                        if (oy + dy >= oh || ox + dx >= ow) continue;
+                        uint4* dst = reinterpret_cast<uint4*>(out + (static_cast<long long>(dy) * ow + dx) * a.y_channels + g * 16);
+                        dst[0] = q0;
+                        dst[1] = q1;
+                    }
+                }
+            } else {
+                uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
+                dst[0] = q0;
+                dst[1] = q1;
+            }
+        }
+        if (a.pool != nullptr) {
+            // 2x2 window: this lane, lane+1 (next column), lane+8 (next row), lane+9
+            const float cnt0 = inside ? 1.0f : 0.0f;
+            const float cnt1 = cnt0 + __shfl_down_sync(0xffffffffu, cnt0, 1);
+            const float cnt = cnt1 + __shfl_down_sync(0xffffffffu, cnt1, 8);
+            uint32_t pooled[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&packed[k]);
+                float lo = inside ? __low2float(b2) : 0.0f;
+                float hi = inside ? __high2float(b2) : 0.0f;
+                lo += __shfl_down_sync(0xffffffffu, lo, 1);
+                hi += __shfl_down_sync(0xffffffffu, hi, 1);
+                lo += __shfl_down_sync(0xffffffffu, lo, 8);
+                hi += __shfl_down_sync(0xffffffffu, hi, 8);
+                const float inv = cnt > 0.0f ? 1.0f / cnt : 0.0f;
+                pooled[k] = pack_bf16x2(lo * inv, hi * inv);
+            }
+            if (inside && ((m >> 3) & 1) == 0 && (m & 1) == 0) {
+                uint4* dst = reinterpret_cast<uint4*>(
+                    a.pool + ((static_cast<long long>(img) * ph + (yy >> 1)) * pw + (xx >> 1)) * a.cout + g * 16);
+                dst[0] = make_uint4(pooled[0], pooled[1], pooled[2], pooled[3]);
+                dst[1] = make_uint4(pooled[4], pooled[5], pooled[6], pooled[7]);
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint64_t* tma_bar = reinterpret_cast<uint64_t*>(smem);
-    uint64_t* mma_bar = tma_bar + 1;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 16);
-    uint8_t* sa = smem + 128;
+    uint64_t* full_bar = reinterpret_cast<uint64_t*>(smem);  // per halo stage: its TMA boxes landed
+    uint64_t* mma_bar = full_bar + 2;                         // per accumulator: its UMMAs completed
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 32);
     const int boxes = a.cin >> 3;
-    uint8_t* sb = sa + boxes * kBoxStride;
+    const int stages = a.stages;
+    const int stage_bytes = boxes * kBoxStride;
+    uint8_t* sa = smem + 128;
+    uint8_t* sb = sa + stages * stage_bytes;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        tc::mbar_init(tma_bar, 1);
-        tc::mbar_init(mma_bar, 1);
+        for (int i = 0; i < 4; ++i) tc::mbar_init(full_bar + i, 1);
         tc::mbar_fence_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tmem_slot, kTmemCols);
+        tc::tmem_alloc(tmem_slot, a.tmem_cols);
         tc::tmem_relinquish();
     }
     const int wvec = 9 * a.cin * a.cout * 2 / 16;
@@ -104,138 +202,102 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
+    const uint32_t acc_step = a.tmem_cols >> 1;  // accumulator 1 starts half way
 
     const int tiles_x = (a.w + kTileW - 1) / kTileW;
     const int tiles_y = (a.h + kTileH - 1) / kTileH;
     const int per_image = tiles_x * tiles_y;
     const int total = per_image * a.n;
+    // this CTA's tiles: blockIdx.x + j * gridDim.x for j < count
+    const int count = static_cast<int>(blockIdx.x) < total ? (total - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1 : 0;
     const uint32_t idesc = tc::idesc_bf16_f32(128, a.cout);
-    const uint32_t abase = tc::smem_u32(sa);
     const uint32_t bbase = tc::smem_u32(sb);
     const uint32_t bstep = static_cast<uint32_t>(a.cout) * 16u;
-    uint32_t tma_phase = 0, mma_phase = 0;
-    int failed = 0;
-    for (int tile = blockIdx.x; tile < total; tile += gridDim.x) {
+
+    // thread 0: TMA of local tile j's halo into stage j % stages
+    auto load = [&](int j) {
+        const int tile = static_cast<int>(blockIdx.x) + j * static_cast<int>(gridDim.x);
         const int img = tile / per_image;
         const int t = tile - img * per_image;
         const int ty = t / tiles_x;
         const int x0 = (t - ty * tiles_x) * kTileW;
         const int y0 = ty * kTileH;
-        if (threadIdx.x == 0) {
-            tc::mbar_arrive_expect_tx(tma_bar, static_cast<uint32_t>(boxes * kBoxBytes));
-            for (int b = 0; b < boxes; ++b) tc::tma_load_4d(sa + b * kBoxStride, &xmap, tma_bar, b * 8, x0 - 1, y0 - 1, img);
-        }
-        const bool loaded = tc::mbar_wait(tma_bar, tma_phase, kSpin);
-        tma_phase ^= 1u;
-        if (__syncthreads_or(!loaded)) {
+        const int s = j % stages;
+        uint8_t* dst = sa + s * stage_bytes;
+        tc::mbar_arrive_expect_tx(full_bar + s, static_cast<uint32_t>(boxes * kBoxBytes));
+        for (int b = 0; b < boxes; ++b) tc::tma_load_4d(dst + b * kBoxStride, &xmap, full_bar + s, b * 8, x0 - 1, y0 - 1, img);
+    };
+
+    // Software pipeline, per local tile j: wait for its halo; one thread issues
+    // its 9 x cin/16 UMMAs into accumulator j & 1; meanwhile every thread runs
+    // the epilogue of tile j - 1 from the other accumulator; once the UMMAs are
+    // done the halo stage refills with tile j + stages.
+    int next_load = count < stages ? count : stages;
+    if (threadIdx.x == 0) {
+        for (int j = 0; j < next_load; ++j) load(j);
+    }
+    int failed = 0, fail_j = 0;
+    for (int j = 0; j < count; ++j) {
+        const int s = j % stages;
+        const bool landed = tc::mbar_wait(full_bar + s, static_cast<uint32_t>(j / stages) & 1u, kSpin);
+        if (__syncthreads_or(!landed)) {
             failed = 1;
+            fail_j = j;
             break;
         }
         tc::tc_fence_after();
         if (threadIdx.x == 0) {
-            uint32_t acc = 0;
+            const uint32_t abase = tc::smem_u32(sa + s * stage_bytes);
+            const uint32_t acc = tmem + static_cast<uint32_t>(j & 1) * acc_step;
+            uint32_t accumulate = 0;
             for (int tap = 0; tap < 9; ++tap) {
                 const int dy = tap / 3;
                 const int dx = tap - dy * 3;
-                for (int s = 0; s < (boxes >> 1); ++s) {
+                for (int p = 0; p < (boxes >> 1); ++p) {
                     const uint64_t ad = tc::smem_desc(
-                        abase + static_cast<uint32_t>(2 * s * kBoxStride + dy * kRowBytes + dx * 16), kBoxStride, kRowBytes);
+                        abase + static_cast<uint32_t>(2 * p * kBoxStride + dy * kRowBytes + dx * 16), kBoxStride, kRowBytes);
                     const uint64_t bd =
-                        tc::smem_desc(bbase + static_cast<uint32_t>(tap * boxes + 2 * s) * bstep, bstep, 128);
-                    tc::umma_bf16(tmem, ad, bd, idesc, acc);
-                    acc = 1;
+                        tc::smem_desc(bbase + static_cast<uint32_t>(tap * boxes + 2 * p) * bstep, bstep, 128);
+                    tc::umma_bf16(acc, ad, bd, idesc, accumulate);
+                    accumulate = 1;
                 }
             }
-            tc::umma_commit(mma_bar);
+            tc::umma_commit(mma_bar + (j & 1));
         }
-        const bool done = tc::mbar_wait(mma_bar, mma_phase, kSpin);
-        mma_phase ^= 1u;
+        if (j > 0) {
+            conv_epilogue(a, tmem + static_cast<uint32_t>((j - 1) & 1) * acc_step,
+                static_cast<int>(blockIdx.x) + (j - 1) * static_cast<int>(gridDim.x), tiles_x, per_image, warp, lane);
+        }
+        const bool done = tc::mbar_wait(mma_bar + (j & 1), static_cast<uint32_t>(j >> 1) & 1u, kSpin);
+        tc::tc_fence_before();
         if (__syncthreads_or(!done)) {
             failed = 2;
+            fail_j = j;
             break;
         }
         tc::tc_fence_after();
-        const int m = warp * 32 + lane;
-        const int yy = y0 + (m >> 3);
-        const int xx = x0 + (m & 7);
-        const bool inside = yy < a.h && xx < a.w;
-        const int oh = a.up ? 2 * a.h : a.h, ow = a.up ? 2 * a.w : a.w;
-        const int oy = a.up ? 2 * yy : yy, ox = a.up ? 2 * xx : xx;
-        __nv_bfloat16* out =
-            a.y + ((static_cast<long long>(img) * oh + oy) * ow + ox) * a.y_channels + a.y_offset;
-        const int ph = (a.h + 1) >> 1, pw = (a.w + 1) >> 1;
-        for (int g = 0; g < (a.cout >> 4); ++g) {
-            uint32_t v[16];
-            tc::tmem_ld16(tmem + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v);
-            tc::tmem_wait_ld();
-            uint32_t packed[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
-                float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
-                if (a.relu) {
-                    lo = fmaxf(lo, 0.0f);
-                    hi = fmaxf(hi, 0.0f);
-                }
-                packed[k] = pack_bf16x2(lo, hi);
-            }
-            const uint4 q0 = make_uint4(packed[0], packed[1], packed[2], packed[3]);
-            const uint4 q1 = make_uint4(packed[4], packed[5], packed[6], packed[7]);
-            if (inside) {
-                if (a.up) {
-                    for (int dy = 0; dy < 2; ++dy) {
-                        for (int dx = 0; dx < 2; ++dx) {
-                            if (oy + dy >= oh || ox + dx >= ow) continue;
-                            uint4* dst = reinterpret_cast<uint4*>(out + (static_cast<long long>(dy) * ow + dx) * a.y_channels + g * 16);
-                            dst[0] = q0;
-                            dst[1] = q1;
-                        }
-                    }
-                } else {
-                    uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
-                    dst[0] = q0;
-                    dst[1] = q1;
-                }
-            }
-            if (a.pool != nullptr) {
-                // 2x2 window: this lane, lane+1 (next column), lane+8 (next row), lane+9
-                const float cnt0 = inside ? 1.0f : 0.0f;
-                const float cnt1 = cnt0 + __shfl_down_sync(0xffffffffu, cnt0, 1);
-                const float cnt = cnt1 + __shfl_down_sync(0xffffffffu, cnt1, 8);
-                uint32_t pooled[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const __nv_bfloat162 b2 = *reinterpret_cast<const __nv_bfloat162*>(&packed[k]);
-                    float lo = inside ? __low2float(b2) : 0.0f;
-                    float hi = inside ? __high2float(b2) : 0.0f;
-                    lo += __shfl_down_sync(0xffffffffu, lo, 1);
-                    hi += __shfl_down_sync(0xffffffffu, hi, 1);
-                    lo += __shfl_down_sync(0xffffffffu, lo, 8);
-                    hi += __shfl_down_sync(0xffffffffu, hi, 8);
-                    const float inv = cnt > 0.0f ? 1.0f / cnt : 0.0f;
-                    pooled[k] = pack_bf16x2(lo * inv, hi * inv);
-                }
-                if (inside && ((m >> 3) & 1) == 0 && (m & 1) == 0) {
-                    uint4* dst = reinterpret_cast<uint4*>(
-                        a.pool + ((static_cast<long long>(img) * ph + (yy >> 1)) * pw + (xx >> 1)) * a.cout + g * 16);
-                    dst[0] = make_uint4(pooled[0], pooled[1], pooled[2], pooled[3]);
-                    dst[1] = make_uint4(pooled[4], pooled[5], pooled[6], pooled[7]);
-                }
-            }
+        const int refill = j + stages;
+        if (refill < count) {
+            if (threadIdx.x == 0) load(refill);
+            next_load = refill + 1;
         }
-        tc::tc_fence_before();
-        __syncthreads();
     }
-    if (failed != 0) {
-        // let copies and MMAs still in flight land before the TMEM is released
-        if (failed == 1) tc::mbar_wait(tma_bar, tma_phase ^ 1u, kSpin);
-        if (failed == 2) tc::mbar_wait(mma_bar, mma_phase ^ 1u, kSpin);
-        if (threadIdx.x == 0 && a.err != nullptr) atomicExch(a.err, failed);
+    if (failed == 0 && count > 0) {
+        conv_epilogue(a, tmem + static_cast<uint32_t>((count - 1) & 1) * acc_step,
+            static_cast<int>(blockIdx.x) + (count - 1) * static_cast<int>(gridDim.x), tiles_x, per_image, warp, lane);
+    }
+    if (failed != 0 && threadIdx.x == 0) {
+        // let the UMMAs and copies still in flight land before shared memory and TMEM are released
+        if (failed == 2) tc::mbar_wait(mma_bar + (fail_j & 1), static_cast<uint32_t>(fail_j >> 1) & 1u, kSpin);
+        for (int k = failed == 1 ? fail_j : fail_j + 1; k < next_load; ++k) {
+            tc::mbar_wait(full_bar + k % stages, static_cast<uint32_t>(k / stages) & 1u, kSpin);
+        }
+        if (a.err != nullptr) atomicExch(a.err, failed);
     }
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
-    if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+    if (warp == 0) tc::tmem_dealloc(tmem, a.tmem_cols);
 }
 
 // ---- host ----------------------------------------------------------------------------------
@@ -310,12 +372,15 @@ cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin,
     const cudaError_t attr = conv_init();
     if (attr != cudaSuccess) return attr;
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
-        static_cast<__nv_bfloat16*>(y), err, static_cast<__nv_bfloat16*>(pool), up};
+        static_cast<__nv_bfloat16*>(y), err, static_cast<__nv_bfloat16*>(pool), up, conv_stages(cin, cout),
+        conv_tmem_cols(cout)};
     const int smem = conv_smem_bytes(cin, cout);
     // resident CTAs per SM: 228 KB of shared memory (1 KB reserved per CTA),
-    // 512 TMEM columns (kTmemCols each), 16 CTAs of 128 threads
+    // 512 TMEM columns (conv_tmem_cols each, so no allocation ever waits),
+    // 16 CTAs of 128 threads
     int per_sm = (228 * 1024) / (smem + 1024);
-    per_sm = per_sm < static_cast<int>(512 / kTmemCols) ? per_sm : static_cast<int>(512 / kTmemCols);
+    const int tmem_fit = static_cast<int>(512u / a.tmem_cols);
+    per_sm = per_sm < tmem_fit ? per_sm : tmem_fit;
     per_sm = per_sm < 16 ? per_sm : 16;
     per_sm = per_sm > 1 ? per_sm : 1;
     const long long tiles = static_cast<long long>((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * n;
