@@ -572,10 +572,13 @@ rtgb_status rtgb_set_denoiser_params(rtgb_handle handle, const float* params, in
 rtgb_status rtgb_conv3x3_pack_weights(const float* weight_oihw, int32_t c_out, int32_t c_in_used,
     int32_t c_in, uint16_t* packed);
 
-/* y[n, y, x, y_channel_offset + o] = act(bias[o] + sum conv3x3(x)) on the
- * tensor cores (tcgen05, TMA halo tiles, FP32 accumulation): x is NHWC BF16
- * with c_in channels (multiple of 16, <= 128), zero padding 1, stride 1;
- * c_out a multiple of 16, <= 64; y is NHWC BF16 with y_channels channels.
+/* y[n, y_channel_offset + o, y, x] = act(bias[o] + sum conv3x3(x)) on the
+ * tensor cores (tcgen05, TMA halo tiles, FP32 accumulation), zero padding 1,
+ * stride 1. Tensors are channel-blocked BF16, [n][c/8][h][w][8]: channel c of
+ * pixel (x, y) of image n at ((n * C/8 + c/8) * h + y) * w * 8 + x * 8 + c % 8.
+ * x has c_in channels (multiple of 16, <= 128); c_out a multiple of 16,
+ * <= 64; y has y_channels channels (multiple of 8) and the output starts at
+ * block y_channel_offset / 8 (offset a multiple of 8).
  * act = ReLU when relu != 0. device_error (device int, may be null) receives a
  * non-zero code if a bounded wait inside the kernel ran out. Asynchronous on
  * `stream` (a cudaStream_t). */

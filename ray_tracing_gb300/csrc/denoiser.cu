@@ -1,13 +1,16 @@
 // Denoiser convolutions on the sm_103a tensor cores.
 //
 // k_conv3x3 is an implicit-GEMM 3x3 convolution (stride 1, zero padding 1) over
-// NHWC BF16 tensors with FP32 accumulation in TMEM:
+// channel-blocked BF16 tensors, [n][c/8][h][w][8] (8 channels innermost, then
+// x, y, the channel block and the image), with FP32 accumulation in TMEM:
 //   * a CTA owns a tile of 8 x 16 output pixels (the GEMM's M = 128 rows) and
 //     every output channel (N = C_out <= 64);
-//   * the 10 x 18 input halo of the tile arrives by TMA, one box of 8 channels
-//     (16 bytes) per load, so each box lands as a dense [18][10][8] block: the
-//     image border is the TMA's zero fill, which is exactly the convolution's
-//     zero padding;
+//   * the 10 x 18 input halo of the tile arrives by TMA, one box per 8-channel
+//     block: in the blocked layout a halo row of one block (10 pixels x 8
+//     channels) is 160 contiguous bytes, so the tensor map's innermost
+//     dimension is a whole image row of that block and a box is 18 rows of 160
+//     bytes, landing as a dense [18][10][8] block; the image border is the
+//     TMA's zero fill, which is exactly the convolution's zero padding;
 //   * the packed weights of all nine taps stay resident in shared memory;
 //   * one thread issues, per tap and per 16 input channels, a
 //     tcgen05.mma.kind::f16 (BF16 x BF16 -> FP32) whose A operand is the halo
@@ -17,7 +20,8 @@
 //     apart, so no im2col copy exists;
 //   * the epilogue reads the accumulators with tcgen05.ld (warp w owns TMEM
 //     lanes 32w..32w+31, i.e. tile rows 4w..4w+3), adds the bias, applies ReLU
-//     and stores BF16 into an NHWC tensor at a channel offset, so encoder
+//     and stores BF16 into a blocked tensor at a channel offset (the eight
+//     lanes of a tile row write 128 contiguous bytes per block), so encoder
 //     outputs land directly in the decoder's concatenation buffers;
 //   * two fused epilogues serve the U-Net: `pool` also writes the 2 x 2
 //     average of the (BF16-rounded) output at half resolution, the four pixels
@@ -25,11 +29,13 @@
 //     at even coordinates), and `up` writes every output pixel to the 2 x 2
 //     block of a twice-as-large tensor (nearest upsampling into the decoder's
 //     concatenation buffer).
-// The grid is persistent and each CTA software-pipelines its tiles: two halo
-// stages in shared memory and two accumulators in TMEM, so the TMA of tile
-// j + 1 and the epilogue of tile j - 1 run while the tensor core works on
-// tile j (one stage when two do not fit in shared memory). Layers small
-// enough keep several such CTAs on one SM. Every mbarrier wait is bounded.
+// The grid is persistent and each CTA is warp-specialised: a producer warp
+// streams halos through up to four shared-memory stages (as many as fit
+// beside the weights), two issuer warps alternate tiles (a single issuing
+// thread reaches about half the tensor core's rate on these small-N UMMAs),
+// and four epilogue warps drain four TMEM accumulators, all linked by
+// mbarriers. Layers small enough keep several such CTAs on one SM. Every
+// mbarrier wait is bounded and a failed role stops the others.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -58,21 +64,32 @@ constexpr int kSpin = 1 << 22;
 // (conv_smem_bytes), so small layers run several CTAs per SM.
 constexpr int kConvSmem = 227 * 1024;
 
-// Halo stages of a layer: two when they fit beside its weights, else one.
+constexpr int kMaxStages = 4;
+
+// Halo stages of a layer: the most (<= kMaxStages, >= 2) that still let two
+// CTAs share an SM (two sets of issuer warps keep the tensor core busier than
+// a deeper ring), else as many as fit beside the weights.
 int conv_stages(int cin, int cout) {
-    return 128 + 2 * (cin / 8) * kBoxStride + 9 * cin * cout * 2 <= kConvSmem ? 2 : 1;
+    const int stage = (cin / 8) * kBoxStride;
+    const int fixed = 256 + 9 * cin * cout * 2;
+    for (int s = kMaxStages; s >= 2; --s) {
+        const int bytes = (fixed + s * stage + 1023) & ~1023;
+        if (2 * (bytes + 1024) <= 228 * 1024) return s;
+    }
+    const int room = (kConvSmem - fixed) / stage;
+    return room < 1 ? 1 : (room > kMaxStages ? kMaxStages : room);
 }
 
 int conv_smem_bytes(int cin, int cout) {
-    const int need = 128 + conv_stages(cin, cout) * (cin / 8) * kBoxStride + 9 * cin * cout * 2;
+    const int need = 256 + conv_stages(cin, cout) * (cin / 8) * kBoxStride + 9 * cin * cout * 2;
     return (need + 1023) & ~1023;
 }
 
-// TMEM columns of a CTA: two FP32 accumulators of cout columns, rounded up to
-// the power of two tcgen05.alloc takes.
+// TMEM columns of a CTA: four FP32 accumulators of at least cout (and at
+// least 32) columns each, a power of two as tcgen05.alloc takes.
 uint32_t conv_tmem_cols(int cout) {
-    uint32_t cols = 32;
-    while (cols < static_cast<uint32_t>(2 * cout)) cols <<= 1;
+    uint32_t cols = 128;
+    while (cols < static_cast<uint32_t>(4 * cout)) cols <<= 1;
     return cols;
 }
 
@@ -111,17 +128,28 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t acc, i
     const bool inside = yy < a.h && xx < a.w;
     const int oh = a.up ? 2 * a.h : a.h, ow = a.up ? 2 * a.w : a.w;
     const int oy = a.up ? 2 * yy : yy, ox = a.up ? 2 * xx : xx;
-    __nv_bfloat16* out = a.y + ((static_cast<long long>(img) * oh + oy) * ow + ox) * a.y_channels + a.y_offset;
+    const int ycb = a.y_channels >> 3;
+    const long long oplane = static_cast<long long>(oh) * ow * 8;  // elements of one channel block
+    // block (y_offset / 8) of this output pixel; the next block is oplane further
+    __nv_bfloat16* out = a.y + ((static_cast<long long>(img) * ycb + (a.y_offset >> 3)) * oh + oy) * ow * 8 + ox * 8;
     const int ph = (a.h + 1) >> 1, pw = (a.w + 1) >> 1;
-    for (int g = 0; g < (a.cout >> 4); ++g) {
-        uint32_t v[16];
-        tc::tmem_ld16(acc + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v);
-        tc::tmem_wait_ld();
+    const long long pplane = static_cast<long long>(ph) * pw * 8;
+    // every 16-column group of this lane's accumulator row in flight at once, one wait
+    const int groups = a.cout >> 4;
+    uint32_t v[kMaxCout / 16][16];
+#pragma unroll
+    for (int g = 0; g < kMaxCout / 16; ++g) {
+        if (g < groups) tc::tmem_ld16(acc + (static_cast<uint32_t>(warp * 32) << 16) + static_cast<uint32_t>(g * 16), v[g]);
+    }
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int g = 0; g < kMaxCout / 16; ++g) {
+        if (g >= groups) break;
         uint32_t packed[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            float lo = __uint_as_float(v[2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
-            float hi = __uint_as_float(v[2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
+            float lo = __uint_as_float(v[g][2 * k]) + __ldg(a.bias + g * 16 + 2 * k);
+            float hi = __uint_as_float(v[g][2 * k + 1]) + __ldg(a.bias + g * 16 + 2 * k + 1);
             if (a.relu) {
                 lo = fmaxf(lo, 0.0f);
                 hi = fmaxf(hi, 0.0f);
@@ -131,19 +159,19 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t acc, i
         const uint4 q0 = make_uint4(packed[0], packed[1], packed[2], packed[3]);
         const uint4 q1 = make_uint4(packed[4], packed[5], packed[6], packed[7]);
         if (inside) {
+            __nv_bfloat16* blk = out + 2 * g * oplane;  // channels 16g..16g+7 here, 16g+8.. one plane on
             if (a.up) {
                 for (int dy = 0; dy < 2; ++dy) {
                     for (int dx = 0; dx < 2; ++dx) {
                         if (oy + dy >= oh || ox + dx >= ow) continue;
-                        uint4* dst = reinterpret_cast<uint4*>(out + (static_cast<long long>(dy) * ow + dx) * a.y_channels + g * 16);
-                        dst[0] = q0;
-                        dst[1] = q1;
+                        const long long o = (static_cast<long long>(dy) * ow + dx) * 8;
+                        *reinterpret_cast<uint4*>(blk + o) = q0;
+                        *reinterpret_cast<uint4*>(blk + oplane + o) = q1;
                     }
                 }
             } else {
-                uint4* dst = reinterpret_cast<uint4*>(out + g * 16);
-                dst[0] = q0;
-                dst[1] = q1;
+                *reinterpret_cast<uint4*>(blk) = q0;
+                *reinterpret_cast<uint4*>(blk + oplane) = q1;
             }
         }
         if (a.pool != nullptr) {
@@ -165,30 +193,46 @@ __device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t acc, i
                 pooled[k] = pack_bf16x2(lo * inv, hi * inv);
             }
             if (inside && ((m >> 3) & 1) == 0 && (m & 1) == 0) {
-                uint4* dst = reinterpret_cast<uint4*>(
-                    a.pool + ((static_cast<long long>(img) * ph + (yy >> 1)) * pw + (xx >> 1)) * a.cout + g * 16);
-                dst[0] = make_uint4(pooled[0], pooled[1], pooled[2], pooled[3]);
-                dst[1] = make_uint4(pooled[4], pooled[5], pooled[6], pooled[7]);
+                // dense cout-channel blocked tensor at half resolution
+                __nv_bfloat16* pblk = a.pool + ((static_cast<long long>(img) * (a.cout >> 3) + 2 * g) * ph + (yy >> 1)) * pw * 8 +
+                                      (xx >> 1) * 8;
+                *reinterpret_cast<uint4*>(pblk) = make_uint4(pooled[0], pooled[1], pooled[2], pooled[3]);
+                *reinterpret_cast<uint4*>(pblk + pplane) = make_uint4(pooled[4], pooled[5], pooled[6], pooled[7]);
             }
         }
     }
 }
 
-__global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
+// Warp roles of k_conv3x3 (kConvThreads = 224): warp 0 is the TMA producer,
+// warps 1 and 2 issue the UMMAs of alternating tiles (one issuing thread
+// cannot keep the tensor core busy: two reach its rate), warps 3..6 run the
+// epilogue, warp w reading TMEM lanes 32 (w % 4) .. + 31. (A second group of
+// epilogue warps measured slower: it takes issue slots from the issuers.)
+constexpr int kConvThreads = 224;
+constexpr int kIssuers = 2;
+constexpr int kEpilogueGroups = 1;
+constexpr int kAccs = 4;          // accumulators in TMEM: tile j uses j % kAccs, issued by warp 1 + j % kIssuers
+
+__global__ void __launch_bounds__(kConvThreads, 2) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint64_t* full_bar = reinterpret_cast<uint64_t*>(smem);  // per halo stage: its TMA boxes landed
-    uint64_t* mma_bar = full_bar + 2;                         // per accumulator: its UMMAs completed
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 32);
+    uint64_t* full_bar = reinterpret_cast<uint64_t*>(smem);   // [kMaxStages] halo stage landed (TMA bytes)
+    uint64_t* empty_bar = full_bar + kMaxStages;               // [kMaxStages] halo stage consumed (UMMA commit)
+    uint64_t* acc_full = empty_bar + kMaxStages;               // [kAccs] accumulator written (UMMA commit)
+    uint64_t* acc_empty = acc_full + kAccs;                    // [kAccs] accumulator read (4 epilogue warps)
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 128);
+    volatile int* stop = reinterpret_cast<volatile int*>(smem + 136);
     const int boxes = a.cin >> 3;
     const int stages = a.stages;
     const int stage_bytes = boxes * kBoxStride;
-    uint8_t* sa = smem + 128;
+    uint8_t* sa = smem + 256;
     uint8_t* sb = sa + stages * stage_bytes;
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 4; ++i) tc::mbar_init(full_bar + i, 1);
+        for (int i = 0; i < 2 * kMaxStages + kAccs; ++i) tc::mbar_init(full_bar + i, 1);
+        for (int i = 0; i < kAccs; ++i) tc::mbar_init(acc_empty + i, 4);
+        *stop = 0;
         tc::mbar_fence_init();
     }
     if (warp == 0) {
@@ -202,7 +246,7 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t acc_step = a.tmem_cols >> 1;  // accumulator 1 starts half way
+    const uint32_t acc_cols = a.tmem_cols / kAccs;
 
     const int tiles_x = (a.w + kTileW - 1) / kTileW;
     const int tiles_y = (a.h + kTileH - 1) / kTileH;
@@ -210,89 +254,108 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
     const int total = per_image * a.n;
     // this CTA's tiles: blockIdx.x + j * gridDim.x for j < count
     const int count = static_cast<int>(blockIdx.x) < total ? (total - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1 : 0;
-    const uint32_t idesc = tc::idesc_bf16_f32(128, a.cout);
-    const uint32_t bbase = tc::smem_u32(sb);
-    const uint32_t bstep = static_cast<uint32_t>(a.cout) * 16u;
-
-    // thread 0: TMA of local tile j's halo into stage j % stages
-    auto load = [&](int j) {
-        const int tile = static_cast<int>(blockIdx.x) + j * static_cast<int>(gridDim.x);
-        const int img = tile / per_image;
-        const int t = tile - img * per_image;
-        const int ty = t / tiles_x;
-        const int x0 = (t - ty * tiles_x) * kTileW;
-        const int y0 = ty * kTileH;
-        const int s = j % stages;
-        uint8_t* dst = sa + s * stage_bytes;
-        tc::mbar_arrive_expect_tx(full_bar + s, static_cast<uint32_t>(boxes * kBoxBytes));
-        for (int b = 0; b < boxes; ++b) tc::tma_load_4d(dst + b * kBoxStride, &xmap, full_bar + s, b * 8, x0 - 1, y0 - 1, img);
+    auto tile_of = [&](int j) { return static_cast<int>(blockIdx.x) + j * static_cast<int>(gridDim.x); };
+    auto fail = [&](int code) {
+        *stop = 1;
+        if (a.err != nullptr) atomicExch(a.err, code);
     };
 
-    // Software pipeline, per local tile j: wait for its halo; one thread issues
-    // its 9 x cin/16 UMMAs into accumulator j & 1; meanwhile every thread runs
-    // the epilogue of tile j - 1 from the other accumulator; once the UMMAs are
-    // done the halo stage refills with tile j + stages.
-    int next_load = count < stages ? count : stages;
-    if (threadIdx.x == 0) {
-        for (int j = 0; j < next_load; ++j) load(j);
-    }
-    int failed = 0, fail_j = 0;
-    for (int j = 0; j < count; ++j) {
-        const int s = j % stages;
-        const bool landed = tc::mbar_wait(full_bar + s, static_cast<uint32_t>(j / stages) & 1u, kSpin);
-        if (__syncthreads_or(!landed)) {
-            failed = 1;
-            fail_j = j;
-            break;
-        }
-        tc::tc_fence_after();
-        if (threadIdx.x == 0) {
-            const uint32_t abase = tc::smem_u32(sa + s * stage_bytes);
-            const uint32_t acc = tmem + static_cast<uint32_t>(j & 1) * acc_step;
-            uint32_t accumulate = 0;
-            for (int tap = 0; tap < 9; ++tap) {
-                const int dy = tap / 3;
-                const int dx = tap - dy * 3;
-                for (int p = 0; p < (boxes >> 1); ++p) {
-                    const uint64_t ad = tc::smem_desc(
-                        abase + static_cast<uint32_t>(2 * p * kBoxStride + dy * kRowBytes + dx * 16), kBoxStride, kRowBytes);
-                    const uint64_t bd =
-                        tc::smem_desc(bbase + static_cast<uint32_t>(tap * boxes + 2 * p) * bstep, bstep, 128);
-                    tc::umma_bf16(acc, ad, bd, idesc, accumulate);
-                    accumulate = 1;
+    if (warp == 0) {
+        // ---- producer: halo of tile j into stage j % stages once tile j - stages has left it
+        int issued = 0;
+        if (lane == 0) {
+            for (int j = 0; j < count; ++j) {
+                const int s = j % stages;
+                if (j >= stages &&
+                    !tc::mbar_wait_or_abort(empty_bar + s, static_cast<uint32_t>(j / stages - 1) & 1u, kSpin, stop)) {
+                    fail(1);
+                    break;
                 }
+                const int tile = tile_of(j);
+                const int img = tile / per_image;
+                const int t = tile - img * per_image;
+                const int ty = t / tiles_x;
+                const int x0 = (t - ty * tiles_x) * kTileW;
+                const int y0 = ty * kTileH;
+                uint8_t* dst = sa + s * stage_bytes;
+                tc::mbar_arrive_expect_tx(full_bar + s, static_cast<uint32_t>(boxes * kBoxBytes));
+                for (int b = 0; b < boxes; ++b) {
+                    tc::tma_load_3d(dst + b * kBoxStride, &xmap, full_bar + s, 8 * (x0 - 1), y0 - 1, img * boxes + b);
+                }
+                issued = j + 1;
             }
-            tc::umma_commit(mma_bar + (j & 1));
+            // the last load of every stage has landed before shared memory is released
+            for (int j = issued - stages > 0 ? issued - stages : 0; j < issued; ++j) {
+                tc::mbar_wait(full_bar + j % stages, static_cast<uint32_t>(j / stages) & 1u, kSpin);
+            }
         }
-        if (j > 0) {
-            conv_epilogue(a, tmem + static_cast<uint32_t>((j - 1) & 1) * acc_step,
-                static_cast<int>(blockIdx.x) + (j - 1) * static_cast<int>(gridDim.x), tiles_x, per_image, warp, lane);
+        __syncwarp();
+    } else if (warp <= kIssuers) {
+        // ---- issuers: tile j (j % kIssuers == warp - 1) from stage j % stages into accumulator j % kAccs.
+        // Descriptors are built once and advanced by constant deltas (their address field is the
+        // shared-memory address / 16 and every address stays inside this CTA's window, so the adds
+        // never carry out of it).
+        if (lane == 0) {
+            const uint32_t idesc = tc::idesc_bf16_f32(128, a.cout);
+            const uint32_t bstep = static_cast<uint32_t>(a.cout) * 16u;
+            const uint64_t b_first = tc::smem_desc(tc::smem_u32(sb), bstep, 128);
+            const uint64_t b_step = static_cast<uint64_t>((2u * bstep) >> 4);      // next 16 input channels of a tap
+            const uint64_t a_step = static_cast<uint64_t>((2 * kBoxStride) >> 4);  // next two channel boxes
+            const int ksteps = boxes >> 1;
+            int last = -1;
+            for (int j = warp - 1; j < count; j += kIssuers) {
+                const int s = j % stages;
+                const int b = j % kAccs;
+                if (!tc::mbar_wait_or_abort(full_bar + s, static_cast<uint32_t>(j / stages) & 1u, kSpin, stop)) {
+                    fail(2);
+                    break;
+                }
+                if (j >= kAccs &&
+                    !tc::mbar_wait_or_abort(acc_empty + b, static_cast<uint32_t>(j / kAccs - 1) & 1u, kSpin, stop)) {
+                    fail(3);
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint64_t a_first = tc::smem_desc(tc::smem_u32(sa + s * stage_bytes), kBoxStride, kRowBytes);
+                const uint32_t acc = tmem + static_cast<uint32_t>(b) * acc_cols;
+                uint64_t bd = b_first;
+                uint32_t accumulate = 0;
+#pragma unroll
+                for (int tap = 0; tap < 9; ++tap) {
+                    // the tap's window: dy rows (kRowBytes each) and dx pixels (16 bytes each) into the halo
+                    uint64_t ad = a_first + static_cast<uint64_t>(((tap / 3) * kRowBytes + (tap % 3) * 16) >> 4);
+                    for (int p = 0; p < ksteps; ++p) {
+                        tc::umma_bf16(acc, ad, bd, idesc, accumulate);
+                        accumulate = 1;
+                        ad += a_step;
+                        bd += b_step;
+                    }
+                }
+                tc::umma_commit(empty_bar + s);   // the halo stage is free once these UMMAs complete
+                tc::umma_commit(acc_full + b);    // and the accumulator is ready for the epilogue
+                last = j;
+            }
+            // every UMMA this thread issued has completed before TMEM is released
+            if (last >= 0) tc::mbar_wait(acc_full + last % kAccs, static_cast<uint32_t>(last / kAccs) & 1u, kSpin);
         }
-        const bool done = tc::mbar_wait(mma_bar + (j & 1), static_cast<uint32_t>(j >> 1) & 1u, kSpin);
-        tc::tc_fence_before();
-        if (__syncthreads_or(!done)) {
-            failed = 2;
-            fail_j = j;
-            break;
+        __syncwarp();
+    } else {
+        // ---- epilogue: group (warp - 3) / 4 takes every kEpilogueGroups-th tile, this warp the
+        // quarter of the accumulator's lanes its warp index selects
+        const int quarter = warp & 3;
+        for (int j = (warp - 1 - kIssuers) / 4; j < count; j += kEpilogueGroups) {
+            const int b = j % kAccs;
+            const bool ready = tc::mbar_wait_or_abort(acc_full + b, static_cast<uint32_t>(j / kAccs) & 1u, kSpin, stop);
+            if (!__all_sync(0xffffffffu, ready)) {
+                if (lane == 0) fail(4);
+                break;
+            }
+            tc::tc_fence_after();
+            conv_epilogue(a, tmem + static_cast<uint32_t>(b) * acc_cols, tile_of(j), tiles_x, per_image, quarter, lane);
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(acc_empty + b);
         }
-        tc::tc_fence_after();
-        const int refill = j + stages;
-        if (refill < count) {
-            if (threadIdx.x == 0) load(refill);
-            next_load = refill + 1;
-        }
-    }
-    if (failed == 0 && count > 0) {
-        conv_epilogue(a, tmem + static_cast<uint32_t>((count - 1) & 1) * acc_step,
-            static_cast<int>(blockIdx.x) + (count - 1) * static_cast<int>(gridDim.x), tiles_x, per_image, warp, lane);
-    }
-    if (failed != 0 && threadIdx.x == 0) {
-        // let the UMMAs and copies still in flight land before shared memory and TMEM are released
-        if (failed == 2) tc::mbar_wait(mma_bar + (fail_j & 1), static_cast<uint32_t>(fail_j >> 1) & 1u, kSpin);
-        for (int k = failed == 1 ? fail_j : fail_j + 1; k < next_load; ++k) {
-            tc::mbar_wait(full_bar + k % stages, static_cast<uint32_t>(k / stages) & 1u, kSpin);
-        }
-        if (a.err != nullptr) atomicExch(a.err, failed);
     }
     tc::tc_fence_before();
     __syncthreads();
@@ -335,23 +398,28 @@ uint16_t to_bf16(float f) {
 
 }  // namespace
 
-// Encodes the TMA map of an NHWC BF16 tensor for k_conv3x3's halo boxes.
+// Encodes the TMA map of a channel-blocked BF16 tensor ([n][c/8][h][w][8]) for
+// k_conv3x3's halo boxes: dimension 0 is one image row of a channel block
+// (w x 8 elements), then rows, then (image, block) planes; a box is 10 pixels
+// x 8 channels by 18 rows. Pixels left of 0 or right of w - 1 fall outside
+// dimension 0 and read as zero, like rows outside [0, h).
 bool conv_input_map(CUtensorMap* map, const void* x, int n, int h, int w, int c) {
     EncodeTiled enc = encode_tiled();
     if (enc == nullptr) return false;
-    const cuuint64_t dims[4] = {static_cast<cuuint64_t>(c), static_cast<cuuint64_t>(w), static_cast<cuuint64_t>(h),
-        static_cast<cuuint64_t>(n)};
-    const cuuint64_t strides[3] = {static_cast<cuuint64_t>(c) * 2, static_cast<cuuint64_t>(w) * c * 2,
-        static_cast<cuuint64_t>(h) * w * c * 2};
-    const cuuint32_t box[4] = {8, kHaloW, kHaloH, 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, estr,
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(w) * 8, static_cast<cuuint64_t>(h),
+        static_cast<cuuint64_t>(n) * static_cast<cuuint64_t>(c / 8)};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(w) * 16, static_cast<cuuint64_t>(h) * w * 16};
+    const cuuint32_t box[3] = {8 * kHaloW, kHaloH, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(x), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Opts k_conv3x3 into its shared-memory size (once per process; call it
 // outside stream capture).
+int g_conv_regs = 0;  // registers per thread of k_conv3x3 (set by conv_init)
+
 cudaError_t conv_init() {
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
@@ -361,6 +429,9 @@ cudaError_t conv_init() {
             attr = cudaFuncSetAttribute(k_conv3x3, cudaFuncAttributePreferredSharedMemoryCarveout,
                 cudaSharedmemCarveoutMaxShared);
         }
+        cudaFuncAttributes fa{};
+        if (attr == cudaSuccess) attr = cudaFuncGetAttributes(&fa, k_conv3x3);
+        if (attr == cudaSuccess) g_conv_regs = fa.numRegs;
     });
     return attr;
 }
@@ -377,16 +448,18 @@ cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin,
     const int smem = conv_smem_bytes(cin, cout);
     // resident CTAs per SM: 228 KB of shared memory (1 KB reserved per CTA),
     // 512 TMEM columns (conv_tmem_cols each, so no allocation ever waits),
-    // 16 CTAs of 128 threads
+    // 2048 threads and 64 K registers
     int per_sm = (228 * 1024) / (smem + 1024);
     const int tmem_fit = static_cast<int>(512u / a.tmem_cols);
+    const int reg_fit = 65536 / ((g_conv_regs > 0 ? g_conv_regs : 255) * kConvThreads);
     per_sm = per_sm < tmem_fit ? per_sm : tmem_fit;
-    per_sm = per_sm < 16 ? per_sm : 16;
+    per_sm = per_sm < reg_fit ? per_sm : reg_fit;
+    per_sm = per_sm < 2048 / kConvThreads ? per_sm : 2048 / kConvThreads;
     per_sm = per_sm > 1 ? per_sm : 1;
     const long long tiles = static_cast<long long>((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * n;
     const long long cap = static_cast<long long>(grid_limit) * per_sm;
     const int grid = static_cast<int>(tiles < cap ? tiles : cap);
-    k_conv3x3<<<grid > 0 ? grid : 1, 128, smem, stream>>>(map, a);
+    k_conv3x3<<<grid > 0 ? grid : 1, kConvThreads, smem, stream>>>(map, a);
     return cudaGetLastError();
 }
 
@@ -483,8 +556,9 @@ constexpr int kInChannels = 16;
 
 __device__ __forceinline__ __nv_bfloat16 bf(float v) { return __float2bfloat16_rn(v); }
 
-// Network input: log1p(radiance), albedo, camera-space normal, log1p(depth), 6 zeros.
-__global__ void k_dn_pack(const FrameParams* __restrict__ fpp, long long offset, long long count,
+// Network input: log1p(radiance), albedo, camera-space normal, log1p(depth), 6
+// zeros, as two channel blocks of the blocked layout (`hw` pixels per image).
+__global__ void k_dn_pack(const FrameParams* __restrict__ fpp, long long offset, long long count, long long hw,
     __nv_bfloat16* __restrict__ out) {
     const FrameBufs f = fpp->cur;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
@@ -507,77 +581,42 @@ __global__ void k_dn_pack(const FrameParams* __restrict__ fpp, long long offset,
         v[9] = bf(log1pf(fmaxf(d, 0.0f)));
 #pragma unroll
         for (int k = 10; k < 16; ++k) v[k] = bf(0.0f);
-        uint4* dst = reinterpret_cast<uint4*>(out + i * kInChannels);
-        dst[0] = reinterpret_cast<const uint4*>(v)[0];
-        dst[1] = reinterpret_cast<const uint4*>(v)[1];
+        const long long img = i / hw, px = i - img * hw;
+        __nv_bfloat16* blk = out + (img * (kInChannels / 8) * hw + px) * 8;
+        *reinterpret_cast<uint4*>(blk) = reinterpret_cast<const uint4*>(v)[0];
+        *reinterpret_cast<uint4*>(blk + hw * 8) = reinterpret_cast<const uint4*>(v)[1];
     }
 }
 
-// 2x2 average pooling of channels [0, c) of a `cs`-channel tensor into a dense
-// c-channel tensor at half resolution (windows clipped at odd borders).
-__global__ void k_dn_pool(const __nv_bfloat16* __restrict__ in, int n, int h, int w, int cs, int c,
-    __nv_bfloat16* __restrict__ out) {
-    const int ho = (h + 1) >> 1, wo = (w + 1) >> 1;
-    const int groups = c >> 3;
-    const long long total = static_cast<long long>(n) * ho * wo * groups;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int g = static_cast<int>(i % groups);
-        long long r = i / groups;
-        const int x = static_cast<int>(r % wo);
-        r /= wo;
-        const int y = static_cast<int>(r % ho);
-        const int img = static_cast<int>(r / ho);
-        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        int cnt = 0;
-        for (int dy = 0; dy < 2; ++dy) {
-            const int yy = 2 * y + dy;
-            if (yy >= h) continue;
-            for (int dx = 0; dx < 2; ++dx) {
-                const int xx = 2 * x + dx;
-                if (xx >= w) continue;
-                const uint4 q = *reinterpret_cast<const uint4*>(in + ((static_cast<long long>(img) * h + yy) * w + xx) * cs + g * 8);
-                const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) acc[k] += __bfloat162float(e[k]);
-                ++cnt;
-            }
-        }
-        const float inv = 1.0f / static_cast<float>(cnt);
-        __align__(16) __nv_bfloat16 v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = bf(acc[k] * inv);
-        *reinterpret_cast<uint4*>(out + ((static_cast<long long>(img) * ho + y) * wo + x) * c + g * 8) =
-            *reinterpret_cast<const uint4*>(v);
-    }
-}
-
-// Nearest 2x upsampling of a dense c-channel tensor (h2 x w2) into channels
-// [off, off + c) of a cs-channel tensor of size h x w.
+// Nearest 2x upsampling of a dense c-channel blocked tensor (h2 x w2) into
+// channels [off, off + c) of a cs-channel blocked tensor of size h x w (the
+// fallback for sizes that do not double exactly).
 __global__ void k_dn_upsample(const __nv_bfloat16* __restrict__ in, int n, int h, int w, int c,
     __nv_bfloat16* __restrict__ out, int cs, int off) {
     const int h2 = (h + 1) >> 1, w2 = (w + 1) >> 1;
     const int groups = c >> 3;
-    const long long total = static_cast<long long>(n) * h * w * groups;
+    const long long total = static_cast<long long>(n) * groups * h * w;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int g = static_cast<int>(i % groups);
-        long long r = i / groups;
-        const int x = static_cast<int>(r % w);
-        r /= w;
+        const int x = static_cast<int>(i % w);
+        long long r = i / w;
         const int y = static_cast<int>(r % h);
-        const int img = static_cast<int>(r / h);
-        const uint4 q =
-            *reinterpret_cast<const uint4*>(in + ((static_cast<long long>(img) * h2 + (y >> 1)) * w2 + (x >> 1)) * c + g * 8);
-        *reinterpret_cast<uint4*>(out + ((static_cast<long long>(img) * h + y) * w + x) * cs + off + g * 8) = q;
+        r /= h;
+        const int g = static_cast<int>(r % groups);
+        const int img = static_cast<int>(r / groups);
+        const uint4 q = *reinterpret_cast<const uint4*>(
+            in + ((static_cast<long long>(img) * groups + g) * h2 + (y >> 1)) * w2 * 8 + (x >> 1) * 8);
+        *reinterpret_cast<uint4*>(out + ((static_cast<long long>(img) * (cs >> 3) + (off >> 3) + g) * h + y) * w * 8 + x * 8) = q;
     }
 }
 
-// Network output (channels 0..2 of a 16-channel tensor, log1p radiance) to float4.
-__global__ void k_dn_unpack(const __nv_bfloat16* __restrict__ in, long long count, float4* __restrict__ out) {
+// Network output (channels 0..2 of a 16-channel blocked tensor, log1p
+// radiance; `hw` pixels per image) to float4.
+__global__ void k_dn_unpack(const __nv_bfloat16* __restrict__ in, long long count, long long hw, float4* __restrict__ out) {
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const uint2 q = *reinterpret_cast<const uint2*>(in + i * 16);
+        const long long img = i / hw, px = i - img * hw;
+        const uint2 q = *reinterpret_cast<const uint2*>(in + (img * 2 * hw + px) * 8);
         const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&q);
         out[i] = make_float4(expm1f(fmaxf(__bfloat162float(e[0]), 0.0f)), expm1f(fmaxf(__bfloat162float(e[1]), 0.0f)),
             expm1f(fmaxf(__bfloat162float(e[2]), 0.0f)), 1.0f);
@@ -753,7 +792,8 @@ cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, 
             l.cout, l.relu, y, ych, yoff, err, sms, stream, pool, up);
     };
     cudaError_t e;
-    k_dn_pack<<<grid_for(full, sms), 256, 0, stream>>>(fp, pixel_offset, full, net->in16);
+    const long long hw = static_cast<long long>(h) * w;
+    k_dn_pack<<<grid_for(full, sms), 256, 0, stream>>>(fp, pixel_offset, full, hw, net->in16);
     if ((e = conv(0, h, w, net->t1, 32, 0)) != cudaSuccess) return e;
     // the encoder's second convolutions also write the pooled tensor; the
     // decoder inputs' upsampled halves are written by the layer below them
@@ -777,7 +817,7 @@ cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, 
     if ((e = conv(8, h, w, net->t5, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(9, h, w, net->t6, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(10, h, w, net->out16, 16, 0)) != cudaSuccess) return e;
-    k_dn_unpack<<<grid_for(full, sms), 256, 0, stream>>>(net->out16, full, out + pixel_offset);
+    k_dn_unpack<<<grid_for(full, sms), 256, 0, stream>>>(net->out16, full, hw, out + pixel_offset);
     return cudaGetLastError();
 }
 

@@ -63,10 +63,12 @@ def test_conv3x3_matches_torch(n, h, w, cin, cout, relu, ych, yoff):
     wt = rng.standard_normal((cout, cin, 3, 3)).astype(np.float32) * (1.0 / np.sqrt(9 * cin))
     bias = rng.standard_normal(cout).astype(np.float32) * 0.1
     packed = _pack(wt, cin)
-    xt = torch.from_numpy(x).to(dev).to(torch.bfloat16).contiguous()
+    # channel-blocked [n][c/8][h][w][8] as the kernel reads it
+    xb = np.ascontiguousarray(x.reshape(n, h, w, cin // 8, 8).transpose(0, 3, 1, 2, 4))
+    xt = torch.from_numpy(xb).to(dev).to(torch.bfloat16).contiguous()
     pw = torch.from_numpy(packed.view(np.int16)).to(dev)
     bt = torch.from_numpy(bias).to(dev)
-    y = torch.full((n, h, w, ych), 7.0, dtype=torch.bfloat16, device=dev)
+    y = torch.full((n, ych // 8, h, w, 8), 7.0, dtype=torch.bfloat16, device=dev)
     err = torch.zeros(1, dtype=torch.int32, device=dev)
     msg = C.create_string_buffer(256)
     stream = torch.cuda.current_stream(dev)
@@ -82,7 +84,7 @@ def test_conv3x3_matches_torch(n, h, w, cin, cout, relu, ych, yoff):
     if relu:
         ref = torch.relu(ref)
     ref = ref.permute(0, 2, 3, 1).cpu().numpy()
-    got = y.float().cpu().numpy()
+    got = y.float().cpu().numpy().transpose(0, 2, 3, 1, 4).reshape(n, h, w, ych)
     out = got[..., yoff:yoff + cout]
     scale = max(1.0, float(np.abs(ref).max()))
     bad = np.abs(out - ref) > 1e-2 * np.maximum(np.abs(ref), 1e-2 * scale)
