@@ -308,6 +308,8 @@ struct BvhNode {
     float4 a, b, c, d;
 };
 
+constexpr int kAnalyticHot = 5;
+
 struct DeviceScene {
     const PrimRecord* prims;      // leaf order
     const BvhNode* nodes;
@@ -329,7 +331,12 @@ struct DeviceScene {
     const int* quad_light;
     const int* triangle_light;
     const rtgb_analytic_light* analytic;
-    const float4* analytic_nrm;     // analytic_light_normal of every light, computed once at prepare
+    // per light, kAnalyticHot float4 built once at prepare with the fields the
+    // light sampler reads (one aligned 16-byte load each instead of scalar
+    // loads of the 108-byte rtgb_analytic_light): (position, selection_pdf),
+    // (basis_x, width or radius), (basis_y, height or length),
+    // (radiance, world_area), (analytic_light_normal, type as int bits)
+    const float4* analytic_hot;
     const float* analytic_cdf;
     int analytic_count;
     const BvhNode* analytic_nodes;  // BVH over finite, non-point analytic lights

@@ -206,7 +206,7 @@ struct rtgb_renderer {
     // scene
     bool prepared = false;
     DeviceScene scene{};
-    DevBuf openpbr, analytic_nrm;
+    DevBuf openpbr, analytic_hot;
     // learned denoiser (replaces OptixDenoiserWrapper, denoiser.cpp:111-185)
     UNet* unet = nullptr;
     DevBuf denoised;          // float4 per pixel of the last denoised frame
@@ -300,7 +300,7 @@ struct rtgb_renderer {
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_nrm, &denoised, &bvh_children, &bvh_parent};
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -570,9 +570,10 @@ struct rtgb_renderer {
         const int na = s.analytic_light_count;
         d.analytic = upload(analytic, s.analytic_lights, static_cast<size_t>(na), stream);
         d.analytic_count = na;
-        d.analytic_nrm = na > 0 ? static_cast<const float4*>(analytic_nrm.ensure(static_cast<size_t>(na) * sizeof(float4)))
+        d.analytic_hot = na > 0 ? static_cast<const float4*>(
+                                      analytic_hot.ensure(static_cast<size_t>(na) * kAnalyticHot * sizeof(float4)))
                                 : nullptr;
-        launch_analytic_normals(d, const_cast<float4*>(d.analytic_nrm), stream);
+        launch_analytic_hot(d, const_cast<float4*>(d.analytic_hot), stream);
         RTGB_CHECK(cudaGetLastError());
         std::vector<float> acdf(static_cast<size_t>(na));
         std::vector<int> inf, finite;

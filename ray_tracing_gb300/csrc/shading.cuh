@@ -812,11 +812,42 @@ RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t&
 }
 
 // sample_analytic_direct_light_candidate, programs.cu:1234-1346
+// Disk and rect lights (the common case) read only the light's hot record
+// (DeviceScene::analytic_hot); the other types read the full light.
 RTGB_D LightSample analytic_candidate(const DeviceScene& s, const float3& sp, int li, float u0, float u1) {
     LightSample smp = empty_sample();
     if (li < 0 || li >= s.analytic_count) return smp;
+    const float4* hot = s.analytic_hot + static_cast<long long>(kAnalyticHot) * li;
+    const float4 h0 = __ldg(hot);
+    const float4 h3 = __ldg(hot + 3);
+    const float4 h4 = __ldg(hot + 4);
+    if (h0.w <= 0.0f) return smp;  // selection_pdf
+    const int type = __float_as_int(h4.w);
+    if (type == 1 || type == 2) {
+        const float4 h1 = __ldg(hot + 1);
+        const float4 h2 = __ldg(hot + 2);
+        smp.light_index = li;
+        smp.emission = xyz(h3);
+        const float3 center = xyz(h0);
+        if (type == 1) {
+            const float radial = h1.w * sqrtf(u0);  // radius
+            const float phi = 2.0f * kPi * u1;
+            smp.position = add(center, add(mul(xyz(h1), radial * cosf(phi)), mul(xyz(h2), radial * sinf(phi))));
+        } else {
+            smp.position = add(center, add(mul(xyz(h1), (u0 - 0.5f) * h1.w), mul(xyz(h2), (u1 - 0.5f) * h2.w)));
+        }
+        smp.normal = xyz(h4);
+        const float3 tl = sub(smp.position, sp);
+        const float d2 = len_sq(tl);
+        if (d2 <= 1e-12f) return empty_sample();
+        smp.distance = sqrtf(d2);
+        smp.direction = divs(tl, smp.distance);
+        const float ac = dot(smp.normal, mul(smp.direction, -1.0f));
+        smp.pdf = h0.w * area_pdf(h3.w, d2, ac);
+        smp.valid = smp.pdf > 0.0f && max_comp(smp.emission) > 0.0f;
+        return smp;
+    }
     const rtgb_analytic_light& l = s.analytic[li];
-    if (l.selection_pdf <= 0.0f) return smp;
     smp.light_index = li;
     smp.emission = ld3(l.radiance);
     if (l.type == 5) {
@@ -866,15 +897,7 @@ RTGB_D LightSample analytic_candidate(const DeviceScene& s, const float3& sp, in
         smp.valid = smp.pdf > 0.0f && max_comp(smp.emission) > 0.0f;
         return smp;
     }
-    if (l.type == 1) {
-        const float radial = l.radius * sqrtf(u0);
-        const float phi = 2.0f * kPi * u1;
-        smp.position = add(center, add(mul(ld3(l.basis_x), radial * cosf(phi)), mul(ld3(l.basis_y), radial * sinf(phi))));
-        smp.normal = xyz(s.analytic_nrm[li]);
-    } else if (l.type == 2) {
-        smp.position = add(center, add(mul(ld3(l.basis_x), (u0 - 0.5f) * l.width), mul(ld3(l.basis_y), (u1 - 0.5f) * l.height)));
-        smp.normal = xyz(s.analytic_nrm[li]);
-    } else if (l.type == 3) {
+    if (l.type == 3) {
         const float phi = 2.0f * kPi * u0;
         const float rx = l.radius * cosf(phi);
         const float ry = l.radius * sinf(phi);

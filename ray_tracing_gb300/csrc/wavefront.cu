@@ -309,17 +309,26 @@ __global__ void k_tonemap(const float4* __restrict__ beauty, uint8_t* rgba, long
 
 }  // namespace
 
-// analytic_light_normal (programs.cu:661-666) of every analytic light, once per
-// scene: the same device function the candidates would run, so the table holds
-// exactly the values they would compute.
-__global__ void k_analytic_normals(DeviceScene s, float4* out) {
+// The light sampler's per-light records (DeviceScene::analytic_hot), once per
+// scene. The normal is analytic_light_normal (programs.cu:661-666), the same
+// device function the candidates would run, so the table holds exactly the
+// values they would compute; the other fields are copies.
+__global__ void k_analytic_hot(DeviceScene s, float4* out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < s.analytic_count) out[i] = f4(analytic_normal(s.analytic[i]), 0.0f);
+    if (i >= s.analytic_count) return;
+    const rtgb_analytic_light& l = s.analytic[i];
+    const bool rect = l.type == 2;
+    float4* o = out + static_cast<long long>(kAnalyticHot) * i;
+    o[0] = make_float4(l.position[0], l.position[1], l.position[2], l.selection_pdf);
+    o[1] = make_float4(l.basis_x[0], l.basis_x[1], l.basis_x[2], rect ? l.width : l.radius);
+    o[2] = make_float4(l.basis_y[0], l.basis_y[1], l.basis_y[2], rect ? l.height : l.length);
+    o[3] = make_float4(l.radiance[0], l.radiance[1], l.radiance[2], l.world_area);
+    o[4] = f4(analytic_normal(l), __int_as_float(l.type));
 }
 
-void launch_analytic_normals(DeviceScene scene, float4* out, cudaStream_t stream) {
+void launch_analytic_hot(DeviceScene scene, float4* out, cudaStream_t stream) {
     if (scene.analytic_count <= 0) return;
-    k_analytic_normals<<<(scene.analytic_count + 255) / 256, 256, 0, stream>>>(scene, out);
+    k_analytic_hot<<<(scene.analytic_count + 255) / 256, 256, 0, stream>>>(scene, out);
 }
 
 void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream) {

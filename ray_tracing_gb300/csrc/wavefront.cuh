@@ -97,7 +97,7 @@ struct LaunchShape {
 };
 
 // Kernel launchers (wavefront.cu). All are asynchronous on `stream`.
-void launch_analytic_normals(DeviceScene scene, float4* out, cudaStream_t stream);
+void launch_analytic_hot(DeviceScene scene, float4* out, cudaStream_t stream);
 void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream);
 void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
 void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
