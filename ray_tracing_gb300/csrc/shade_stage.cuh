@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
         bool deferred = false;
         if (alight >= 0) {
             AnalyticHit ah;
-            ah.hit = hit_analytic(s.analytic[alight], st.o, st.d, kRayEpsilon, kRayFar, ah);
+            ah.hit = hit_analytic_at(s, alight, st.o, st.d, kRayEpsilon, kRayFar, ah);
             ah.light = alight;
             const float w = analytic_emission_mis(s, st, ah);
             st.rad = add(st.rad, mul(st.thr, mul(ld3(s.analytic[alight].radiance), w)));

@@ -395,9 +395,8 @@ RTGB_D float3 analytic_normal(const rtgb_analytic_light& l) {
     return normalize(mul(cross(ld3(l.basis_x), ld3(l.basis_y)), -1.0f));
 }
 
-RTGB_D bool plane_coords(const rtgb_analytic_light& l, const float3& p, float& lx, float& ly) {
-    const float3 bx = ld3(l.basis_x), by = ld3(l.basis_y);
-    const float3 local = sub(p, ld3(l.position));
+RTGB_D bool plane_coords(const float3& bx, const float3& by, const float3& center, const float3& p, float& lx, float& ly) {
+    const float3 local = sub(p, center);
     const float xx = dot(bx, bx), xy = dot(bx, by), yy = dot(by, by);
     const float det = xx * yy - xy * xy;
     if (det <= 1e-16f) return false;
@@ -439,7 +438,7 @@ RTGB_D bool hit_analytic(const rtgb_analytic_light& l, const float3& ro, const f
         if (t <= tmin || t >= tmax) return false;
         const float3 pos = add(ro, mul(rd, t));
         float lx = 0.0f, ly = 0.0f;
-        if (!plane_coords(l, pos, lx, ly)) return false;
+        if (!plane_coords(ld3(l.basis_x), ld3(l.basis_y), center, pos, lx, ly)) return false;
         const bool inside = l.type == 1 ? lx * lx + ly * ly <= l.radius * l.radius
                                         : fabsf(lx) <= 0.5f * l.width && fabsf(ly) <= 0.5f * l.height;
         if (!inside) return false;
@@ -482,6 +481,34 @@ RTGB_D bool hit_analytic(const rtgb_analytic_light& l, const float3& ro, const f
     return true;
 }
 
+// hit_analytic of light li; disk and rect lights read only its hot record
+// (the normal there is analytic_light_normal, computed once per scene).
+RTGB_D bool hit_analytic_at(const DeviceScene& s, int li, const float3& ro, const float3& rd, float tmin, float tmax,
+    AnalyticHit& h) {
+    const float4* hot = s.analytic_hot + static_cast<long long>(kAnalyticHot) * li;
+    const float4 h4 = __ldg(hot + 4);
+    const int type = __float_as_int(h4.w);
+    if (type != 1 && type != 2) return hit_analytic(s.analytic[li], ro, rd, tmin, tmax, h);
+    const float3 n = xyz(h4);
+    const float den = dot(rd, n);
+    if (den >= -1e-8f) return false;
+    const float3 center = xyz(__ldg(hot));
+    const float t = dot(sub(center, ro), n) / den;
+    if (t <= tmin || t >= tmax) return false;
+    const float4 h1 = __ldg(hot + 1), h2 = __ldg(hot + 2);
+    const float3 pos = add(ro, mul(rd, t));
+    float lx = 0.0f, ly = 0.0f;
+    if (!plane_coords(xyz(h1), xyz(h2), center, pos, lx, ly)) return false;
+    const bool inside = type == 1 ? lx * lx + ly * ly <= h1.w * h1.w
+                                  : fabsf(lx) <= 0.5f * h1.w && fabsf(ly) <= 0.5f * h2.w;
+    if (!inside) return false;
+    h.hit = true;
+    h.t = t;
+    h.pos = pos;
+    h.normal = n;
+    return true;
+}
+
 // Closest analytic-light hit below `tmax` (intersect_analytic_lights,
 // programs.cu:795-813) over the light BVH; returns the light index or -1.
 RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3& d, float tmin, float tmax, float& t_hit) {
@@ -492,7 +519,7 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
         const int li = s.analytic_leaf[slot];
         AnalyticHit h;
         h.hit = false;
-        if (hit_analytic(s.analytic[li], o, d, tmin, closest, h)) {
+        if (hit_analytic_at(s, li, o, d, tmin, closest, h)) {
             closest = h.t;
             best = li;
         }
