@@ -8,6 +8,7 @@
 // child boxes inline) is this project's own.
 #pragma once
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -310,11 +311,24 @@ struct BvhNode {
 
 constexpr int kAnalyticHot = 5;
 
+// Wide (4-ary) BVH node, 128 bytes = 8 float4, collapsed from the binary LBVH
+// (every BVH4 node is a binary node at even depth, its children the binary
+// node's children or grandchildren) and numbered breadth-first, so the top
+// levels are a prefix of the array that kernels can stage in shared memory:
+//   q[0..2] = lo.x, lo.y, lo.z of children 0..3, q[3..5] = hi.x, hi.y, hi.z,
+//   q[6] = child indices as int bits (>= 0 a BVH4 node, < 0 the leaf of sorted
+//   slot ~c, kEmptyChild unused), q[7] unused.
+constexpr int kNode4 = 8;                 // float4 per BVH4 node
+constexpr int kEmptyChild = INT_MIN;
+constexpr int kStagedNodes4 = 64;         // BVH4 nodes the trace kernels keep in shared memory (8 KB)
+
 struct DeviceScene {
     const PrimRecord* prims;      // leaf order
-    const BvhNode* nodes;
+    const BvhNode* nodes;         // binary LBVH (build, refit, parity downloads)
     int prim_count;
     int node_count;
+    const float4* nodes4;         // wide BVH traversed by every ray (kNode4 float4 per node)
+    int node4_count;
     const rtgb_sphere* spheres;
     const rtgb_quad* quads;
     const rtgb_triangle* triangles;
@@ -616,11 +630,50 @@ RTGB_D RayInv ray_inv(const float3& o, const float3& d) {
     return r;
 }
 
-// Closest hit over the scene BVH: strict t < closest like the reference, so
-// equal-t primitives keep the first one traversed. Returns the code or -1.
-// `overflow` counts subtrees dropped by a full stack (never silently).
+RTGB_D float lane4(const float4& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+// The node's eight float4, from the shared-memory copy of the first `staged`
+// nodes when it is there, else through the read-only cache.
+RTGB_D void load_node4(const DeviceScene& s, const float4* staged, int staged_count, int node, float4 (&q)[kNode4]) {
+    if (node < staged_count) {
+        const float4* src = staged + static_cast<long long>(kNode4) * node;
+#pragma unroll
+        for (int k = 0; k < kNode4 - 1; ++k) q[k] = src[k];
+    } else {
+        const float4* src = s.nodes4 + static_cast<long long>(kNode4) * node;
+#pragma unroll
+        for (int k = 0; k < kNode4 - 1; ++k) q[k] = __ldg(src + k);
+    }
+}
+
+// Inserts (t, c) into the ascending list (t0, c0) .. (t3, c3) (INF-padded);
+// equal t keeps the earlier child first.
+RTGB_D void insert4(float t, int c, float& t0, int& c0, float& t1, int& c1, float& t2, int& c2, float& t3, int& c3) {
+    if (!(t < t3)) return;
+    t3 = t;
+    c3 = c;
+    if (t3 < t2) {
+        const float tt = t2; t2 = t3; t3 = tt;
+        const int cc = c2; c2 = c3; c3 = cc;
+    }
+    if (t2 < t1) {
+        const float tt = t1; t1 = t2; t2 = tt;
+        const int cc = c1; c1 = c2; c2 = cc;
+    }
+    if (t1 < t0) {
+        const float tt = t0; t0 = t1; t1 = tt;
+        const int cc = c0; c0 = c1; c1 = cc;
+    }
+}
+
+// Closest hit over the scene's wide BVH: strict t < closest like the
+// reference, so equal-t primitives keep the first one traversed. Leaves are
+// tested as soon as their box is hit; internal children are visited nearest
+// first. Returns the code or -1. `overflow` counts subtrees dropped by a full
+// stack (never silently). `staged` / `staged_count`: a shared-memory copy of
+// the first nodes (or null / 0).
 RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3& d, float tmin, float& closest,
-    int& overflow) {
+    int& overflow, const float4* staged = nullptr, int staged_count = 0) {
     int best = -1;
     if (s.prim_count <= 0) return -1;
     if (s.prim_count == 1) {
@@ -636,44 +689,47 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
     int stack[kTraversalStack];
     int sp = 0;
     int node = 0;
+    const float kInf = __int_as_float(0x7f800000);
     for (int guard = 0; guard < (1 << 24); ++guard) {
-        const float4* np = reinterpret_cast<const float4*>(s.nodes + node);
-        const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
-        const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
-        float t0, t1;
-        bool h0 = box_hit(xyz(a), xyz(b), ri.inv, ri.oinv, tmin, closest, t0);
-        bool h1 = box_hit(xyz(c), xyz(e), ri.inv, ri.oinv, tmin, closest, t1);
-        if (h0 && c0 < 0) {
-            const PrimRecord p = load_prim(s.prims, ~c0);
-            float t;
-            if (prim_hit(p, o, d, tmin, closest, t)) {
-                closest = t;
-                best = prim_code(p);
+        float4 q[kNode4];
+        load_node4(s, staged, staged_count, node, q);
+        float t0 = kInf, t1 = kInf, t2 = kInf, t3 = kInf;
+        int c0 = -1, c1 = -1, c2 = -1, c3 = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = __float_as_int(lane4(q[6], k));
+            if (c == kEmptyChild) continue;
+            float tn;
+            if (!box_hit(f3(lane4(q[0], k), lane4(q[1], k), lane4(q[2], k)), f3(lane4(q[3], k), lane4(q[4], k), lane4(q[5], k)),
+                    ri.inv, ri.oinv, tmin, closest, tn)) {
+                continue;
             }
-            h0 = false;
-        }
-        if (h1 && c1 < 0) {
-            const PrimRecord p = load_prim(s.prims, ~c1);
-            float t;
-            if (prim_hit(p, o, d, tmin, closest, t)) {
-                closest = t;
-                best = prim_code(p);
+            if (c < 0) {
+                const PrimRecord p = load_prim(s.prims, ~c);
+                float t;
+                if (prim_hit(p, o, d, tmin, closest, t)) {
+                    closest = t;
+                    best = prim_code(p);
+                }
+            } else {
+                insert4(tn, c, t0, c0, t1, c1, t2, c2, t3, c3);
             }
-            h1 = false;
         }
-        if (h0 && h1) {
-            const bool first0 = t0 <= t1;
-            if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
-            else ++overflow;
-            node = first0 ? c0 : c1;
-            continue;
-        }
-        if (h0) {
+        if (t0 < kInf) {
+            // farthest first onto the stack, continue with the nearest
+            if (t3 < kInf) {
+                if (sp < kTraversalStack) stack[sp++] = c3;
+                else ++overflow;
+            }
+            if (t2 < kInf) {
+                if (sp < kTraversalStack) stack[sp++] = c2;
+                else ++overflow;
+            }
+            if (t1 < kInf) {
+                if (sp < kTraversalStack) stack[sp++] = c1;
+                else ++overflow;
+            }
             node = c0;
-            continue;
-        }
-        if (h1) {
-            node = c1;
             continue;
         }
         if (sp == 0) break;
@@ -685,7 +741,8 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
 // Any hit in (tmin, tmax): the reference's occlusion test is a closest-hit
 // query whose `hit` flag alone is used (programs.cu:1759-1762), so the first
 // hit found gives the same answer.
-RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d, float tmin, float tmax, int& overflow) {
+RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d, float tmin, float tmax, int& overflow,
+    const float4* staged = nullptr, int staged_count = 0) {
     if (s.prim_count <= 0) return false;
     if (s.prim_count == 1) {
         float t;
@@ -696,33 +753,31 @@ RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d,
     int sp = 0;
     int node = 0;
     for (int guard = 0; guard < (1 << 24); ++guard) {
-        const float4* np = reinterpret_cast<const float4*>(s.nodes + node);
-        const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
-        const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
-        float t0, t1, t;
-        bool h0 = box_hit(xyz(a), xyz(b), ri.inv, ri.oinv, tmin, tmax, t0);
-        bool h1 = box_hit(xyz(c), xyz(e), ri.inv, ri.oinv, tmin, tmax, t1);
-        if (h0 && c0 < 0) {
-            if (prim_hit(load_prim(s.prims, ~c0), o, d, tmin, tmax, t)) return true;
-            h0 = false;
+        float4 q[kNode4];
+        load_node4(s, staged, staged_count, node, q);
+        int next = -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = __float_as_int(lane4(q[6], k));
+            if (c == kEmptyChild) continue;
+            float tn;
+            if (!box_hit(f3(lane4(q[0], k), lane4(q[1], k), lane4(q[2], k)), f3(lane4(q[3], k), lane4(q[4], k), lane4(q[5], k)),
+                    ri.inv, ri.oinv, tmin, tmax, tn)) {
+                continue;
+            }
+            if (c < 0) {
+                float t;
+                if (prim_hit(load_prim(s.prims, ~c), o, d, tmin, tmax, t)) return true;
+            } else if (next < 0) {
+                next = c;
+            } else if (sp < kTraversalStack) {
+                stack[sp++] = c;
+            } else {
+                ++overflow;
+            }
         }
-        if (h1 && c1 < 0) {
-            if (prim_hit(load_prim(s.prims, ~c1), o, d, tmin, tmax, t)) return true;
-            h1 = false;
-        }
-        if (h0 && h1) {
-            const bool first0 = t0 <= t1;
-            if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
-            else ++overflow;
-            node = first0 ? c0 : c1;
-            continue;
-        }
-        if (h0) {
-            node = c0;
-            continue;
-        }
-        if (h1) {
-            node = c1;
+        if (next >= 0) {
+            node = next;
             continue;
         }
         if (sp == 0) break;

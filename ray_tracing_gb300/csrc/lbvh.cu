@@ -310,6 +310,81 @@ cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals,
     return cudaGetLastError();
 }
 
+int collapse_bvh4(const int* children, int n, std::vector<int>& child4, std::vector<int>& ref4) {
+    child4.clear();
+    ref4.clear();
+    if (n < 2) return 0;
+    std::vector<int> source(1, 0);  // binary node behind each BVH4 node, breadth-first
+    source.reserve(static_cast<size_t>(n));
+    for (size_t i = 0; i < source.size(); ++i) {
+        const int p = source[i];
+        int slot = 0;
+        int c4[4] = {kEmptyChild, kEmptyChild, kEmptyChild, kEmptyChild};
+        int r4[4] = {-1, -1, -1, -1};
+        for (int k = 0; k < 2; ++k) {
+            const int ck = children[2 * p + k];
+            if (ck >= 0) {  // internal: its two children become this node's
+                for (int kk = 0; kk < 2; ++kk) {
+                    const int g = children[2 * ck + kk];
+                    r4[slot] = 2 * ck + kk;
+                    if (g >= 0) {
+                        c4[slot] = static_cast<int>(source.size());
+                        source.push_back(g);
+                    } else {
+                        c4[slot] = g;
+                    }
+                    ++slot;
+                }
+            } else {
+                r4[slot] = 2 * p + k;
+                c4[slot] = ck;
+                ++slot;
+            }
+        }
+        child4.insert(child4.end(), c4, c4 + 4);
+        ref4.insert(ref4.end(), r4, r4 + 4);
+    }
+    return static_cast<int>(source.size());
+}
+
+namespace {
+
+__global__ void k_fill_bvh4(const BvhNode* __restrict__ nodes2, const int* __restrict__ child4,
+    const int* __restrict__ ref4, int n4, float4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n4) return;
+    float lo[3][4], hi[3][4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int r = ref4[4 * i + k];
+        float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+        if (r >= 0) {
+            const BvhNode& nd = nodes2[r >> 1];
+            a = (r & 1) ? nd.c : nd.a;
+            b = (r & 1) ? nd.d : nd.b;
+        }
+        lo[0][k] = a.x; lo[1][k] = a.y; lo[2][k] = a.z;
+        hi[0][k] = b.x; hi[1][k] = b.y; hi[2][k] = b.z;
+    }
+    float4* o = out + static_cast<long long>(kNode4) * i;
+    for (int ax = 0; ax < 3; ++ax) {
+        o[ax] = make_float4(lo[ax][0], lo[ax][1], lo[ax][2], lo[ax][3]);
+        o[3 + ax] = make_float4(hi[ax][0], hi[ax][1], hi[ax][2], hi[ax][3]);
+    }
+    o[6] = make_float4(__int_as_float(child4[4 * i]), __int_as_float(child4[4 * i + 1]), __int_as_float(child4[4 * i + 2]),
+        __int_as_float(child4[4 * i + 3]));
+    o[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+}  // namespace
+
+cudaError_t fill_bvh4(const BvhNode* nodes2, const int* child4, const int* ref4, int n4, float4* nodes4,
+    cudaStream_t stream) {
+    if (n4 <= 0) return cudaSuccess;
+    k_fill_bvh4<<<(n4 + 127) / 128, 128, 0, stream>>>(nodes2, child4, ref4, n4, nodes4);
+    return cudaGetLastError();
+}
+
 cudaError_t lbvh_refit(LbvhScratch& s, int n, const int* sorted_vals, const int* children, const int* parent,
     BvhNode* nodes, cudaStream_t stream) {
     if (n < 2) return cudaErrorInvalidValue;

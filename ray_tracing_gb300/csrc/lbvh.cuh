@@ -4,6 +4,8 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "device_common.cuh"
 
 namespace rtgb {
@@ -39,6 +41,19 @@ cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals,
 // src/realtime/gpu/gpu_scene_acceleration.cpp:347-365).
 cudaError_t lbvh_refit(LbvhScratch& s, int n, const int* sorted_vals, const int* children, const int* parent,
     BvhNode* nodes, cudaStream_t stream);
+
+// Collapses the binary hierarchy into the wide BVH of DeviceScene::nodes4 (host
+// side, breadth-first): `children` holds the binary children (2 per internal
+// node, a negative child c the leaf of sorted slot ~c); per BVH4 node it
+// writes 4 child indices (BVH4 node, ~slot or kEmptyChild) and 4 box
+// references (2 * binary node + which child, whose inline box is the child's
+// box; -1 unused). Returns the BVH4 node count.
+int collapse_bvh4(const int* children, int n, std::vector<int>& child4, std::vector<int>& ref4);
+
+// Writes the wide BVH's nodes from the binary nodes' inline child boxes (after
+// every build and refit).
+cudaError_t fill_bvh4(const BvhNode* nodes2, const int* child4, const int* ref4, int n4, float4* nodes4,
+    cudaStream_t stream);
 
 // Morton code of a centroid inside the centroid bounds, 10 bits per axis.
 // The CPU restatement in oracle/lbvh_oracle.cpp follows it operation for operation.

@@ -224,6 +224,10 @@ struct rtgb_renderer {
     // the hierarchy's children/parent survive so a geometry change with the
     // same primitive counts refits the boxes instead of rebuilding
     DevBuf bvh_children, bvh_parent;
+    // wide BVH traversed by every ray: nodes and the collapse (children, box
+    // references into the binary nodes) kept for refits
+    DevBuf nodes4, child4, ref4;
+    int node4_count = 0;
     bool accel_valid = false;
     int accel_counts[3] = {-1, -1, -1};
     uint64_t geometry_sig = 0, scene_sig = 0;
@@ -300,7 +304,7 @@ struct rtgb_renderer {
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent};
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -627,6 +631,7 @@ struct rtgb_renderer {
             RTGB_CHECK(lbvh_refit(ls, n, sorted_vals.as<int>(), bvh_children.as<int>(), bvh_parent.as<int>(), nd, stream));
             launch_gather_records(unsorted.as<PrimRecord>(), sorted_vals.as<int>(), recs, n, stream);
             RTGB_CHECK(cudaGetLastError());
+            RTGB_CHECK(fill_bvh4(nd, child4.as<int>(), ref4.as<int>(), node4_count, nodes4.as<float4>(), stream));
             d.nodes = nd;
             d.node_count = n - 1;
         } else if (n >= 2) {
@@ -646,13 +651,29 @@ struct rtgb_renderer {
                 cudaMemcpyDeviceToDevice, stream));
             RTGB_CHECK(cudaMemcpyAsync(bvh_parent.p, ls.parent, (2 * static_cast<size_t>(n) - 1) * sizeof(int),
                 cudaMemcpyDeviceToDevice, stream));
+            // the wide BVH: collapse the binary hierarchy on the host, boxes filled on the device
+            std::vector<int> children2(2 * static_cast<size_t>(n - 1)), c4, r4;
+            RTGB_CHECK(cudaMemcpyAsync(children2.data(), ls.children, children2.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                stream));
+            RTGB_CHECK(cudaStreamSynchronize(stream));
+            node4_count = collapse_bvh4(children2.data(), n, c4, r4);
+            RTGB_CHECK(cudaMemcpyAsync(child4.ensure(c4.size() * sizeof(int)), c4.data(), c4.size() * sizeof(int),
+                cudaMemcpyHostToDevice, stream));
+            RTGB_CHECK(cudaMemcpyAsync(ref4.ensure(r4.size() * sizeof(int)), r4.data(), r4.size() * sizeof(int),
+                cudaMemcpyHostToDevice, stream));
+            nodes4.ensure(static_cast<size_t>(node4_count) * kNode4 * sizeof(float4));
+            RTGB_CHECK(fill_bvh4(nd, child4.as<int>(), ref4.as<int>(), node4_count, nodes4.as<float4>(), stream));
+            RTGB_CHECK(cudaStreamSynchronize(stream));  // the host vectors leave scope
             d.nodes = nd;
             d.node_count = n - 1;
         } else {
             RTGB_CHECK(cudaMemcpyAsync(recs, unsorted.p, sizeof(PrimRecord), cudaMemcpyDeviceToDevice, stream));
             d.nodes = nullptr;
             d.node_count = 0;
+            node4_count = 0;
         }
+        d.nodes4 = node4_count > 0 ? nodes4.as<float4>() : nullptr;
+        d.node4_count = node4_count;
         d.prims = recs;
         RTGB_CHECK(cudaStreamSynchronize(stream));
     }

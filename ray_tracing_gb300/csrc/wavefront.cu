@@ -86,9 +86,22 @@ __global__ void __launch_bounds__(256) k_raygen(const FrameParams* __restrict__ 
     }
 }
 
+// The first kStagedNodes4 wide-BVH nodes (the top levels: nodes are numbered
+// breadth-first) into this block's shared memory; returns how many.
+RTGB_D int stage_nodes4(const DeviceScene& s, float4* smem4) {
+    const int staged = s.node4_count < kStagedNodes4 ? s.node4_count : kStagedNodes4;
+    for (int k = threadIdx.x; k < staged * kNode4; k += blockDim.x) smem4[k] = __ldg(s.nodes4 + k);
+    __syncthreads();
+    return staged;
+}
+
+constexpr int kStagedBytes = kStagedNodes4 * kNode4 * static_cast<int>(sizeof(float4));
+
 // intersect_scene (programs.cu:1654-1757) + intersect_analytic_lights (:795-813)
 __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
+    extern __shared__ float4 smem4[];
+    const int staged = stage_nodes4(s, smem4);
     const int in = bounce & 1;
     const int count = counters->active[in];
     if (blockIdx.x == 0 && threadIdx.x == 0 && bounce < 64) counters->bounce_active[bounce] = count;
@@ -99,7 +112,7 @@ __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ f
         const float3 o = xyz(P.ray_o[path]);
         const float3 d = xyz(P.ray_d[path]);
         float closest = kRayFar;
-        int code = traverse_closest(s, o, d, kRayEpsilon, closest, overflow);
+        int code = traverse_closest(s, o, d, kRayEpsilon, closest, overflow, smem4, staged);
         ++traced;
         if (s.medium_count > 0) {
             uint32_t rng = P.rng[path];
@@ -135,6 +148,8 @@ __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ f
 // contributions are added in slot order (emissive geometry, then analytic).
 __global__ void __launch_bounds__(128) k_shadow(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
+    extern __shared__ float4 smem4[];
+    const int staged = stage_nodes4(s, smem4);
     const FrameParams& fp = *fpp;
     const int count = counters->shadow;
     int overflow = 0;
@@ -149,7 +164,7 @@ __global__ void __launch_bounds__(128) k_shadow(const FrameParams* __restrict__ 
             const float4 o = P.sh_o[k][path];
             const float4 d = P.sh_d[k][path];
             ++traced;
-            if (!traverse_any(s, xyz(o), xyz(d), kRayEpsilon, o.w, overflow)) {
+            if (!traverse_any(s, xyz(o), xyz(d), kRayEpsilon, o.w, overflow, smem4, staged)) {
                 rad = add(rad, xyz(c));
                 visible |= 1 << k;  // kDecisionNeeEmissive, kDecisionNeeAnalytic
             }
@@ -343,7 +358,7 @@ void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, Launc
 
 void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream) {
-    k_trace<<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_trace<<<shape.grid, 128, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
@@ -357,7 +372,7 @@ void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
 
 void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream) {
-    k_shadow<<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_shadow<<<shape.grid, 128, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
@@ -383,11 +398,11 @@ void query_launch_shapes(int sm_count, LaunchShape* shapes) {
     int blocks = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_raygen, 256, 0);
     shapes[0] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 256};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace, 128, kStagedBytes);
     shapes[1] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false>, 128, 0);
     shapes[2] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shadow, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shadow, 128, kStagedBytes);
     shapes[3] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_finalize, 256, 0);
     shapes[4] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 256};
