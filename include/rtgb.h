@@ -372,6 +372,7 @@ typedef struct rtgb_acceleration_info {
      * over the kept hierarchy), 3 rebuild */
     int32_t update_kind;
     int32_t generation;           /* incremented by every update, refit and rebuild */
+    int32_t wide_node_count;      /* nodes of the 4-wide BVH the rays traverse (rtgb_download_bvh4) */
 } rtgb_acceleration_info;
 
 /* Replaces OptixRenderer::OptixRenderer + RendererPool(int) (optix_renderer.cpp:104-109,
@@ -500,6 +501,13 @@ rtgb_status rtgb_download_lbvh(rtgb_handle handle, uint32_t* sorted_morton,
  * (rtgb_acceleration_info::update_kind 2) rewrites
  * (GpuSceneAcceleration::refit, gpu_scene_acceleration.cpp:347-365). */
 rtgb_status rtgb_download_lbvh_boxes(rtgb_handle handle, float* child_boxes);
+
+/* The 4-wide BVH every ray traverses, collapsed breadth-first from the binary
+ * LBVH (same leaves): per node 4 child indices (>= 0 a node, < 0 the leaf of
+ * sorted slot ~c, INT32_MIN unused) and 24 floats of child boxes (lo.x[4],
+ * lo.y[4], lo.z[4], hi.x[4], hi.y[4], hi.z[4]); wide_node_count nodes, node 0
+ * the root. No counterpart in the reference (its BVH is binary). */
+rtgb_status rtgb_download_bvh4(rtgb_handle handle, int32_t* children, float* child_boxes);
 
 /* ------------------------------------------------------------------------ */
 /* Host-side authoring helpers (C++23 host code in the same library).        */

@@ -194,7 +194,7 @@ class AccelerationInfo(C.Structure):
     _fields_ = [("primitive_count", C.c_int32), ("node_count", C.c_int32),
                 ("analytic_light_node_count", C.c_int32), ("analytic_bvh_light_count", C.c_int32),
                 ("build_ms", C.c_float), ("traversal_stack_overflows", C.c_int32),
-                ("update_kind", C.c_int32), ("generation", C.c_int32)]
+                ("update_kind", C.c_int32), ("generation", C.c_int32), ("wide_node_count", C.c_int32)]
 
 # AccelerationUpdateKind (gpu_scene_acceleration.cpp:247-295)
 UPDATE_KINDS = ("reuse", "update", "refit", "rebuild")
@@ -239,6 +239,7 @@ SIGNATURES = {
                                              C.c_int64]),
     "rtgb_download_lbvh": (C.c_int, [Handle, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtgb_download_lbvh_boxes": (C.c_int, [Handle, C.c_void_p]),
+    "rtgb_download_bvh4": (C.c_int, [Handle, C.c_void_p, C.c_void_p]),
     "rtgb_host_scene_create": (C.c_int, [C.c_char_p, C.c_uint32, C.c_int64, P(C.c_void_p)]),
     "rtgb_host_scene_destroy": (None, [C.c_void_p]),
     "rtgb_host_scene_view": (C.c_int, [C.c_void_p, P(Scene)]),

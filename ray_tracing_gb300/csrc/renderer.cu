@@ -1480,6 +1480,7 @@ rtgb_status rtgb_acceleration_info_get(rtgb_handle h, rtgb_acceleration_info* ou
     a.traversal_stack_overflows = h->h_counters ? h->h_counters->overflow : 0;
     a.update_kind = h->update_kind;
     a.generation = h->generation;
+    a.wide_node_count = h->scene.node4_count;
     *out = a;
     return RTGB_OK;
 }
@@ -1527,6 +1528,27 @@ rtgb_status rtgb_download_lbvh(rtgb_handle h, uint32_t* sorted_morton, int32_t* 
                 children[2 * i] = c0;
                 children[2 * i + 1] = c1;
             }
+        }
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_bvh4(rtgb_handle h, int32_t* children, float* child_boxes) {
+    if (!h || !children || !child_boxes) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->prepared) throw Invalid{"no scene prepared"};
+        const int n4 = h->scene.node4_count;
+        if (n4 <= 0) throw Invalid{"the scene has fewer than two primitives and no hierarchy"};
+        std::vector<float4> q(static_cast<size_t>(n4) * kNode4);
+        RTGB_CHECK(cudaMemcpy(q.data(), h->scene.nodes4, q.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n4; ++i) {
+            const float4* n = q.data() + static_cast<size_t>(i) * kNode4;
+            for (int k = 0; k < 6; ++k) {
+                const float v[4] = {n[k].x, n[k].y, n[k].z, n[k].w};
+                for (int c = 0; c < 4; ++c) child_boxes[24 * static_cast<size_t>(i) + 4 * k + c] = v[c];
+            }
+            const float w[4] = {n[6].x, n[6].y, n[6].z, n[6].w};
+            std::memcpy(children + 4 * static_cast<size_t>(i), w, sizeof w);
         }
         return RTGB_OK;
     });

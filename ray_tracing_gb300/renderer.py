@@ -193,6 +193,14 @@ class Renderer:
                     "download_lbvh")
         return keys, order, children
 
+    def bvh4(self):
+        """(children (nodes, 4) int32, boxes (nodes, 2, 3, 4) float32: lo/hi, axis, child)."""
+        n = self.acceleration_info().wide_node_count
+        children = np.empty((n, 4), np.int32)
+        boxes = np.empty((n, 2, 3, 4), np.float32)
+        self._check(self.lib.rtgb_download_bvh4(self.h, children.ctypes.data, boxes.ctypes.data), "download_bvh4")
+        return children, boxes
+
     def lbvh_boxes(self) -> np.ndarray:
         """(nodes, 2, 2, 3): per internal node the left and right child's (lo, hi) box."""
         n = self.acceleration_info().primitive_count

@@ -10,7 +10,9 @@ only the node boxes, so it is checked three ways: every node box equals the
 union of the (new) primitive boxes below it, the paths traced through the
 refitted hierarchy match the oracle on the moved scene, and they match a
 renderer that rebuilt from scratch, bit for bit wherever the two hit the same
-primitives.
+primitives. The 4-wide BVH the rays traverse (collapsed from the binary one)
+is checked after builds and refits: every leaf once, every node reached once,
+every child box the exact union of the primitive boxes below it.
 """
 import numpy as np
 import pytest
@@ -179,3 +181,61 @@ def test_refit_boxes_paths_and_rebuilt_equivalence(amplitude):
         diverged, max_err, bad = compare_paths(gc, gr, oc, orad)
         assert diverged <= 2e-3 and bad == 0, (cam, diverged, max_err, bad)
     assert r.acceleration_info().traversal_stack_overflows == 0
+
+
+def _check_bvh4(r, view):
+    """Every leaf slot once, every node reached once from the root, every child
+    box the exact union of the primitive boxes below it."""
+    from oracle.lbvh import primitive_boxes
+    _, order, _ = r.lbvh()
+    children, boxes = r.bvh4()
+    lo, hi = primitive_boxes(view)
+    leaf_lo, leaf_hi = lo[order], hi[order]
+    n4 = children.shape[0]
+    empty = np.iinfo(np.int32).min
+    seen_leaves = np.zeros(len(order), np.int32)
+    seen_nodes = np.zeros(n4, np.int32)
+    seen_nodes[0] = 1
+    for i in range(n4):
+        for k in range(4):
+            c = int(children[i, k])
+            if c == empty:
+                continue
+            if c >= 0:
+                assert c > i, "children follow their parent (breadth-first)"
+                seen_nodes[c] += 1
+            else:
+                seen_leaves[~c] += 1
+    assert np.all(seen_leaves == 1) and np.all(seen_nodes == 1)
+    # subtree unions, children before parents (reverse breadth-first order)
+    ulo = np.zeros((n4, 3), np.float32)
+    uhi = np.zeros((n4, 3), np.float32)
+    for i in range(n4 - 1, -1, -1):
+        cl, ch = [], []
+        for k in range(4):
+            c = int(children[i, k])
+            if c == empty:
+                continue
+            blo, bhi = (ulo[c], uhi[c]) if c >= 0 else (leaf_lo[~c], leaf_hi[~c])
+            assert np.array_equal(boxes[i, 0, :, k], blo) and np.array_equal(boxes[i, 1, :, k], bhi), (i, k)
+            cl.append(blo)
+            ch.append(bhi)
+        ulo[i] = np.min(cl, axis=0)
+        uhi[i] = np.max(ch, axis=0)
+    return n4
+
+
+@pytest.mark.parametrize("name,detail", [("random_spheres", 256), ("triangle_terrain", 20000), ("cornell_box", 0)])
+def test_wide_bvh_structure_after_build_and_refit(name, detail):
+    from ray_tracing_gb300.renderer import Renderer
+    sc = scenes.HostScene(name, detail=detail)
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    n = sc.view.sphere_count + sc.view.quad_count + sc.view.triangle_count
+    n4 = _check_bvh4(r, sc.view)
+    assert (n - 1) // 3 <= n4 <= n - 1
+    if sc.view.sphere_count:
+        _move_spheres(sc.view, 0.3)
+        r.prepare_scene(sc.view)
+        assert _kind(r)[0] == REFIT
+        assert _check_bvh4(r, sc.view) == n4
