@@ -595,6 +595,18 @@ rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, int32_t w, in
     int32_t y_channels, int32_t y_channel_offset, int32_t* device_error, void* stream,
     char* message, size_t message_size);
 
+/* Weight and bias gradients of rtgb_conv3x3_bf16 (the training backward pass;
+ * the input gradient is rtgb_conv3x3_bf16 itself with the weights flipped and
+ * transposed): dweight[o][i][dy][dx] = sum over pixels of dy[o] * x[i] at the
+ * offset (dy - 1, dx - 1) with zero padding, dbias[o] = sum of dy[o]; both
+ * FP32 and overwritten. x (c_in channels, multiple of 16, <= 128) and dy
+ * (c_out channels, multiple of 16, <= 64) are channel-blocked BF16 of the
+ * same n x h x w. Tensor cores (tcgen05, MN-major operands straight from the
+ * blocked tiles), FP32 accumulation. Asynchronous on `stream`. */
+rtgb_status rtgb_conv3x3_wgrad_bf16(const void* x, int32_t n, int32_t h, int32_t w, int32_t c_in,
+    const void* dy, int32_t c_out, float* dweight, float* dbias, int32_t* device_error, void* stream,
+    char* message, size_t message_size);
+
 /* ------------------------------------------------------------------------ */
 /* Allocation-free LBVH build. No counterpart in the reference.              */
 /* ------------------------------------------------------------------------ */

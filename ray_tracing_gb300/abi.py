@@ -240,6 +240,9 @@ SIGNATURES = {
     "rtgb_download_lbvh": (C.c_int, [Handle, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtgb_download_lbvh_boxes": (C.c_int, [Handle, C.c_void_p]),
     "rtgb_download_bvh4": (C.c_int, [Handle, C.c_void_p, C.c_void_p]),
+    "rtgb_conv3x3_wgrad_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                           C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_char_p, C.c_size_t]),
     "rtgb_host_scene_create": (C.c_int, [C.c_char_p, C.c_uint32, C.c_int64, P(C.c_void_p)]),
     "rtgb_host_scene_destroy": (None, [C.c_void_p]),
     "rtgb_host_scene_view": (C.c_int, [C.c_void_p, P(Scene)]),

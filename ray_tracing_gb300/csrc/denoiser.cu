@@ -44,6 +44,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "denoiser.cuh"
 #include "rtgb.h"
 #include "tc_primitives.cuh"
 
@@ -404,12 +405,16 @@ uint16_t to_bf16(float f) {
 // x 8 channels by 18 rows. Pixels left of 0 or right of w - 1 fall outside
 // dimension 0 and read as zero, like rows outside [0, h).
 bool conv_input_map(CUtensorMap* map, const void* x, int n, int h, int w, int c) {
+    return blocked_tensor_map(map, x, n, h, w, c, kHaloW, kHaloH);
+}
+
+bool blocked_tensor_map(CUtensorMap* map, const void* x, int n, int h, int w, int c, int box_pixels, int box_rows) {
     EncodeTiled enc = encode_tiled();
     if (enc == nullptr) return false;
     const cuuint64_t dims[3] = {static_cast<cuuint64_t>(w) * 8, static_cast<cuuint64_t>(h),
         static_cast<cuuint64_t>(n) * static_cast<cuuint64_t>(c / 8)};
     const cuuint64_t strides[2] = {static_cast<cuuint64_t>(w) * 16, static_cast<cuuint64_t>(h) * w * 16};
-    const cuuint32_t box[3] = {8 * kHaloW, kHaloH, 1};
+    const cuuint32_t box[3] = {static_cast<cuuint32_t>(8 * box_pixels), static_cast<cuuint32_t>(box_rows), 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(x), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -536,7 +541,6 @@ extern "C" rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, in
 #include <string>
 #include <vector>
 
-#include "denoiser.cuh"
 
 namespace rtgb {
 namespace {

@@ -18,7 +18,15 @@
 
 #include "wavefront.cuh"
 
+#include <cuda.h>
+
 namespace rtgb {
+
+// TMA map of a channel-blocked BF16 tensor ([n][c/8][h][w][8]) whose box is
+// `box_pixels` pixels x 8 channels by `box_rows` rows of one channel block
+// (the innermost dimension is an image row of a block; pixels outside the
+// image read as zero).
+bool blocked_tensor_map(CUtensorMap* map, const void* x, int n, int h, int w, int c, int box_pixels, int box_rows);
 
 struct UNet;
 
