@@ -607,6 +607,27 @@ rtgb_status rtgb_conv3x3_wgrad_bf16(const void* x, int32_t n, int32_t h, int32_t
     const void* dy, int32_t c_out, float* dweight, float* dbias, int32_t* device_error, void* stream,
     char* message, size_t message_size);
 
+/* Native training of the denoiser U-Net (the reference's denoiser is closed
+ * and has no training): forward, log-space L1 loss, backward (input
+ * gradients by rtgb_conv3x3_bf16's kernel with flipped, transposed weights,
+ * weight gradients by rtgb_conv3x3_wgrad_bf16's) and Adam (beta 0.9 / 0.999,
+ * eps 1e-8) on FP32 master parameters, for batches of n crops of h x w (h, w
+ * multiples of 4). Parameters in rtgb_set_denoiser_params order. */
+typedef struct rtgb_trainer_s* rtgb_trainer;
+rtgb_status rtgb_trainer_create(int32_t n, int32_t h, int32_t w, const float* params, int64_t count,
+    rtgb_trainer* out_trainer);
+void rtgb_trainer_destroy(rtgb_trainer trainer);
+/* input: device, channel-blocked BF16, 16 channels (the network input of
+ * denoiser.py's make_input, channels 10..15 zero); target: device FP32
+ * n x h x w x 3, log1p radiance. learning_rate 0 computes the gradients only.
+ * *loss (host, may be null) receives the mean L1 loss of the forward pass. */
+rtgb_status rtgb_trainer_step(rtgb_trainer trainer, const void* input, const float* target, float learning_rate,
+    float* loss);
+/* Parameter gradients of the last step and the current parameters (host, count values). */
+rtgb_status rtgb_trainer_gradients(rtgb_trainer trainer, float* grads);
+rtgb_status rtgb_trainer_params(rtgb_trainer trainer, float* params);
+const char* rtgb_trainer_last_error(rtgb_trainer trainer);
+
 /* ------------------------------------------------------------------------ */
 /* Allocation-free LBVH build. No counterpart in the reference.              */
 /* ------------------------------------------------------------------------ */

@@ -240,6 +240,12 @@ SIGNATURES = {
     "rtgb_download_lbvh": (C.c_int, [Handle, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtgb_download_lbvh_boxes": (C.c_int, [Handle, C.c_void_p]),
     "rtgb_download_bvh4": (C.c_int, [Handle, C.c_void_p, C.c_void_p]),
+    "rtgb_trainer_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, P(C.c_void_p)]),
+    "rtgb_trainer_destroy": (None, [C.c_void_p]),
+    "rtgb_trainer_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float, P(C.c_float)]),
+    "rtgb_trainer_gradients": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rtgb_trainer_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rtgb_trainer_last_error": (C.c_char_p, [C.c_void_p]),
     "rtgb_conv3x3_wgrad_bf16": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                            C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_char_p, C.c_size_t]),

@@ -444,7 +444,7 @@ cudaError_t conv_init() {
 // Launches k_conv3x3; `map` must describe x (conv_input_map).
 cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
     int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream,
-    void* pool = nullptr, int up = 0) {
+    void* pool, int up) {
     const cudaError_t attr = conv_init();
     if (attr != cudaSuccess) return attr;
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
@@ -545,17 +545,6 @@ extern "C" rtgb_status rtgb_conv3x3_bf16(const void* x, int32_t n, int32_t h, in
 namespace rtgb {
 namespace {
 
-struct LayerSpec {
-    int cin_used, cin, cout_used, cout, relu;
-};
-
-// in order: e1a e1b e2a e2b e3a e3b d2a d2b d1a d1b head
-constexpr LayerSpec kLayers[] = {
-    {10, 16, 32, 32, 1}, {32, 32, 32, 32, 1}, {32, 32, 48, 48, 1}, {48, 48, 48, 48, 1}, {48, 48, 64, 64, 1},
-    {64, 64, 64, 64, 1}, {112, 112, 48, 48, 1}, {48, 48, 48, 48, 1}, {80, 80, 32, 32, 1}, {32, 32, 32, 32, 1},
-    {32, 32, 3, 16, 0},
-};
-constexpr int kLayerCount = sizeof(kLayers) / sizeof(kLayers[0]);
 constexpr int kInChannels = 16;
 
 __device__ __forceinline__ __nv_bfloat16 bf(float v) { return __float2bfloat16_rn(v); }

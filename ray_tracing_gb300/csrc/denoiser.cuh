@@ -28,6 +28,36 @@ namespace rtgb {
 // image read as zero).
 bool blocked_tensor_map(CUtensorMap* map, const void* x, int n, int h, int w, int c, int box_pixels, int box_rows);
 
+// Layers of the U-Net in order (e1a e1b e2a e2b e3a e3b d2a d2b d1a d1b head):
+// input channels used / padded to a multiple of 16, output channels used /
+// padded, ReLU.
+struct LayerSpec {
+    int cin_used, cin, cout_used, cout, relu;
+};
+inline constexpr LayerSpec kLayers[] = {
+    {10, 16, 32, 32, 1}, {32, 32, 32, 32, 1}, {32, 32, 48, 48, 1}, {48, 48, 48, 48, 1}, {48, 48, 64, 64, 1},
+    {64, 64, 64, 64, 1}, {112, 112, 48, 48, 1}, {48, 48, 48, 48, 1}, {80, 80, 32, 32, 1}, {32, 32, 32, 32, 1},
+    {32, 32, 3, 16, 0},
+};
+inline constexpr int kLayerCount = sizeof(kLayers) / sizeof(kLayers[0]);
+
+// TMA map of a k_conv3x3 input (halo boxes of 10 x 18 pixels).
+bool conv_input_map(CUtensorMap* map, const void* x, int n, int h, int w, int c);
+// Opts k_conv3x3 into its shared memory (once; call outside stream capture).
+cudaError_t conv_init();
+// k_conv3x3 over an (n, h, w) batch of the blocked tensor `map` describes:
+// weights packed as rtgb_conv3x3_pack_weights, output written at channel
+// y_offset of a y_channels tensor (twice the size when `up`), and the 2 x 2
+// average of the output into `pool` when it is non-null.
+cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
+    int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream,
+    void* pool = nullptr, int up = 0);
+// Weight (cout x cin x 3 x 3, FP32) and bias gradients of a k_conv3x3 layer
+// (denoiser_train.cu); `partial` holds wgrad_partial_bytes(sms, cout).
+cudaError_t launch_conv3x3_wgrad(const void* x, int n, int h, int w, int cin, const void* dy, int cout, float* dweight,
+    float* dbias, int* err, int sms, cudaStream_t stream, float* partial, size_t partial_bytes);
+size_t wgrad_partial_bytes(int sms, int cout);
+
 struct UNet;
 
 UNet* unet_create();
