@@ -25,6 +25,9 @@ equal_relmse: the headline comparison. A 4096-spp plain render of the same
 roofline: the launch with the largest share of the frame, per-unit algorithmic
           bytes (SoA stream bytes per ray / path segment / pixel) over its CUDA-event durations, against the measured
           HBM copy bandwidth.
+training: native training steps of the U-Net (rtgb_trainer_step: tcgen05
+          forward, input- and weight-gradient convolutions, Adam) on 16 crops
+          of 256 x 256, ms per step and algorithmic TFLOP/s.
 cpu_baseline / --impl reference: the CPU oracle (restatement of the reference's
           radiance kernel, with the reference's median-split BVH) on all host
           threads, over a band of rows of the same workload.
@@ -322,6 +325,61 @@ def denoiser_record(denoise_ms):
             "frac": achieved / peak, "peak_source": note, "flops_per_frame": flops}
 
 
+TRAIN_BATCH, TRAIN_CROP = 16, 256     # the learned-denoiser training shape (16 crops of 256 x 256)
+
+
+def training_flops(n: int, h: int, w: int) -> float:
+    """Algorithmic FLOPs of one native training step: each convolution's forward,
+    weight gradient and (all but the first layer) input gradient, real channel
+    counts."""
+    from ray_tracing_gb300 import denoiser
+    full = float(n * h * w)
+    res = [full, full, full / 4, full / 4, full / 16, full / 16, full / 4, full / 4, full, full, full]
+    return sum(2.0 * px * ci * co * 9 * (2 if li == 0 else 3)
+               for li, (px, (ci, co)) in enumerate(zip(res, denoiser.LAYERS)))
+
+
+def training_record(steps: int = 10, warmup: int = 3):
+    """Native training steps of the U-Net (rtgb_trainer_step: forward, loss,
+    backward, Adam) on a resident synthetic batch; wall time per step (each
+    step ends with the loss read back) and algorithmic TFLOP/s against the
+    measured dense BF16 burst rate."""
+    import ctypes as C
+    import torch
+    from ray_tracing_gb300 import abi, denoiser
+    torch.manual_seed(0)
+    flat = denoiser.flatten(denoiser.build_model()).astype(np.float32)
+    n, hw = TRAIN_BATCH, TRAIN_CROP
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.rand((n, 10, hw, hw), device="cuda", generator=gen)
+    xb = denoiser.blocked_input(x)
+    target = torch.rand((n, hw, hw, 3), device="cuda", generator=gen).contiguous()
+    lib = abi.load()
+    tr = C.c_void_p()
+    if lib.rtgb_trainer_create(n, hw, hw, flat.ctypes.data, flat.size, C.byref(tr)) != 0:
+        return {"unavailable": "rtgb_trainer_create failed"}
+    try:
+        loss = C.c_float()
+        for i in range(warmup + steps):
+            if i == warmup:
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+            if lib.rtgb_trainer_step(tr, C.c_void_p(xb.data_ptr()), C.c_void_p(target.data_ptr()), 1e-4,
+                                     C.byref(loss)) != 0:
+                return {"unavailable": lib.rtgb_trainer_last_error(tr).decode()}
+        ms = 1000.0 * (time.perf_counter() - t0) / steps
+    finally:
+        lib.rtgb_trainer_destroy(tr)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("bf16_tflops") or 1900.0
+    flops = training_flops(n, hw, hw)
+    achieved = flops / (ms * 1e-3) / 1e12
+    return {"batch": f"{n} x {hw}x{hw} crops, 10 input channels", "optimizer": "Adam", "ms_per_step": ms,
+            "steps": steps, "flops_per_step": flops, "achieved_tflops": achieved, "peak_tflops": peak,
+            "frac": achieved / peak, "peak_source": "of measured (burst)" if peaks.get("bf16_tflops") else "of fallback",
+            "final_loss": float(loss.value)}
+
+
 def roofline(stage_ms, frames_stats, spatial):
     """Roofline record of the launch slot (kernel at a bounce) with the largest
     average time per frame; per-unit algorithmic bytes over its
@@ -477,6 +535,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches_per_frame * args.steps,
         "denoiser": denoiser_record(denoise_ms) if weights is not None else None,
     }
+    if world == 1 and not args.no_training:
+        line["training"] = training_record()
     if world == 1 and not args.no_relmse:
         line["equal_relmse"] = equal_relmse(sc, rig, prof)
     if world == 1 and not args.no_cpu_baseline:
@@ -493,6 +553,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
+    ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

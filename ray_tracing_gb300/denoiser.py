@@ -45,6 +45,16 @@ def make_input(beauty: np.ndarray | "torch.Tensor", albedo, dnormal, depth, xp=n
     return xp.cat([lb, albedo[..., :3], dnormal[..., :3], ld], dim=-1).permute(0, 3, 1, 2)
 
 
+def blocked_input(x):
+    """Network input (N, 10, H, W) torch tensor -> the native path's layout:
+    16 channels (6 zero), channel-blocked (N, 2, H, W, 8), BF16, contiguous."""
+    import torch
+    n, c, h, w = x.shape
+    x16 = torch.zeros((n, 16, h, w), dtype=torch.float32, device=x.device)
+    x16[:, :c] = x
+    return x16.reshape(n, 2, 8, h, w).permute(0, 1, 3, 4, 2).to(torch.bfloat16).contiguous()
+
+
 def build_model():
     import torch
     import torch.nn.functional as F

@@ -12,8 +12,11 @@ rtgb_set_denoiser_params.
 
     python -m ray_tracing_gb300.train_denoiser --out ray_tracing_gb300/weights/denoiser_unet.bf16
 
-Training runs on PyTorch (the optimiser and autograd are tooling); inference
-in the renderer runs on the library's tensor-core kernels.
+By default the optimisation runs on PyTorch (autograd and Adam as tooling);
+with --native every training step runs on the library's own kernels
+(rtgb_trainer_*: tcgen05 forward, input- and weight-gradient convolutions,
+Adam), PyTorch only holding the rendered data and evaluating the validation
+relMSE. Inference in the renderer always runs on the library's kernels.
 """
 from __future__ import annotations
 
@@ -85,6 +88,7 @@ def main(argv=None):
     ap.add_argument("--crop", type=int, default=128)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--native", action="store_true", help="train with the library's kernels (rtgb_trainer_*)")
     args = ap.parse_args(argv)
 
     import torch
@@ -110,6 +114,16 @@ def main(argv=None):
     opt = torch.optim.Adam(model.parameters(), lr=args.lr)
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, args.steps)
     cs = args.crop
+    native = None
+    if args.native:
+        import ctypes as C
+        import math
+        from . import abi
+        lib = abi.load()
+        flat0 = denoiser.flatten(model)
+        native = C.c_void_p()
+        if lib.rtgb_trainer_create(args.batch, cs, cs, flat0.ctypes.data, flat0.size, C.byref(native)) != 0:
+            raise RuntimeError("rtgb_trainer_create failed")
     for step in range(args.steps):
         xs, ys = [], []
         for _ in range(args.batch):
@@ -121,20 +135,37 @@ def main(argv=None):
             xs.append(inputs[si][fi, yy:yy + cs, xx:xx + cs])
             ys.append(targets[si][yy:yy + cs, xx:xx + cs])
         x = prep(torch.stack(xs))
-        y = torch.log1p(torch.stack(ys).clamp_min(0)).permute(0, 3, 1, 2)
-        loss = torch.nn.functional.l1_loss(model(x), y)
-        opt.zero_grad(set_to_none=True)
-        loss.backward()
-        opt.step()
-        sched.step()
+        if native is not None:
+            # cosine schedule as CosineAnnealingLR, the step on the library's kernels
+            lr = 0.5 * args.lr * (1.0 + math.cos(math.pi * step / args.steps))
+            xb = denoiser.blocked_input(x)
+            yt = torch.log1p(torch.stack(ys).clamp_min(0)).contiguous()
+            lv = C.c_float()
+            if lib.rtgb_trainer_step(native, C.c_void_p(xb.data_ptr()), C.c_void_p(yt.data_ptr()), lr, C.byref(lv)) != 0:
+                raise RuntimeError(lib.rtgb_trainer_last_error(native).decode())
+            loss = torch.tensor(lv.value)
+            if step % 500 == 0 or step == args.steps - 1:
+                cur = np.empty(denoiser.param_count(), np.float32)
+                lib.rtgb_trainer_params(native, cur.ctypes.data)
+                denoiser.unflatten(model, cur)
+        else:
+            y = torch.log1p(torch.stack(ys).clamp_min(0)).permute(0, 3, 1, 2)
+            loss = torch.nn.functional.l1_loss(model(x), y)
+            opt.zero_grad(set_to_none=True)
+            loss.backward()
+            opt.step()
+            sched.step()
         if step % 500 == 0 or step == args.steps - 1:
             with torch.no_grad():
                 pred = torch.expm1(model(prep(vx)).clamp_min(0)).permute(0, 2, 3, 1)
                 rel = ((pred - vy) ** 2 / (vy ** 2 + 1e-2)).mean().item()
                 noisy = ((vx[..., 0:3] - vy) ** 2 / (vy ** 2 + 1e-2)).mean().item()
             print(f"step {step}: loss {loss.item():.4f}  valid relMSE {rel:.5f} (noisy {noisy:.5f})", flush=True)
+    if native is not None:
+        lib.rtgb_trainer_destroy(native)
     flat = denoiser.flatten(model)
     denoiser.save_weights(flat, args.out, {
+        "trainer": "native (rtgb_trainer_*)" if args.native else "pytorch",
         "train_scenes": [f"{n}/{s}/{d}" for n, s, d in TRAIN_SCENES], "valid_scene": "/".join(map(str, VALID_SCENE)),
         "target_spp": args.target_spp, "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
         "valid_relmse": rel, "valid_noisy_relmse": noisy})

@@ -42,3 +42,11 @@ def test_denoiser_flops_match_the_network():
     quarter = (48 * 64 + 64 * 64) * 160 * 120
     assert bench.denoiser_flops(640, 480, 4) == pytest.approx(2 * 9 * 4 * (full + half + quarter))
     assert len(denoiser.LAYERS) == 11
+
+
+def test_training_flops_count_forward_and_both_gradients():
+    from ray_tracing_gb300 import denoiser
+    n, h, w = 2, 64, 32
+    fwd = bench.denoiser_flops(w, h, n)
+    first = 2.0 * n * h * w * denoiser.LAYERS[0][0] * denoiser.LAYERS[0][1] * 9
+    assert bench.training_flops(n, h, w) == pytest.approx(3 * fwd - first)
