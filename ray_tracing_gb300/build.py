@@ -5,7 +5,8 @@ Everything is compiled with nvcc/g++ directly (no cmake): CUDA sources for
 libraries land next to the code that loads them:
 
 * ``ray_tracing_gb300/_lib/librtgb.so`` — the product (C ABI of ``include/rtgb.h``)
-* ``ray_tracing_gb300/_bin/``            — render_realtime and benchmark_scene_lifecycle (C ABI users)
+* ``ray_tracing_gb300/_bin/``            — render_realtime, render_restir_acceptance and
+  benchmark_scene_lifecycle (C ABI users)
 * ``oracle/_bin/liborc.so``             — the CPU oracle (test infrastructure)
 
 Translation units compile in parallel and are skipped when up to date.
@@ -103,6 +104,8 @@ CLI_SRC = CSRC / "cli" / "render_realtime.cpp"
 CLI = PKG / "_bin" / "render_realtime"
 LIFECYCLE_SRC = CSRC / "cli" / "benchmark_scene_lifecycle.cpp"
 LIFECYCLE = PKG / "_bin" / "benchmark_scene_lifecycle"
+ACCEPTANCE_SRC = CSRC / "cli" / "render_restir_acceptance.cpp"
+ACCEPTANCE = PKG / "_bin" / "render_restir_acceptance"
 
 
 def build_cli() -> Path:
@@ -119,6 +122,10 @@ def build_cli() -> Path:
             pass
         _run(["g++", *CXX_FLAGS, f"-DRTGB_SOURCE_REVISION=\"{rev}\"", "-I", str(INCLUDE), "-I", str(CSRC / "cli"),
               str(CLI_SRC), "-L", str(LIB_DIR), "-lrtgb", "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(CLI)])
+    if _stale(ACCEPTANCE, [ACCEPTANCE_SRC, CSRC / "cli" / "png_reader.h", CSRC / "cli" / "png_writer.h", INCLUDE / "rtgb.h",
+                           LIB]):
+        _run(["g++", *CXX_FLAGS, "-I", str(INCLUDE), "-I", str(CSRC / "cli"), str(ACCEPTANCE_SRC), "-L", str(LIB_DIR),
+              "-lrtgb", "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(ACCEPTANCE)])
     if _stale(LIFECYCLE, [LIFECYCLE_SRC, INCLUDE / "rtgb.h", LIB]):
         _run(["g++", *CXX_FLAGS, "-I", str(INCLUDE), str(LIFECYCLE_SRC), "-L", str(LIB_DIR), "-lrtgb",
               "-Wl,-rpath,$ORIGIN/../_lib", "-o", str(LIFECYCLE)])
