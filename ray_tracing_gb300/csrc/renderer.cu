@@ -917,24 +917,32 @@ struct rtgb_renderer {
                 stage_events.push_back(e);
             }
         }
+        // Grids: the persistent size (SMs x resident blocks), but no more blocks
+        // than the frame's paths need (small frames then launch few, cheap blocks).
+        LaunchShape sh[kLaunchShapes];
+        for (int i = 0; i < kLaunchShapes; ++i) {
+            sh[i] = shapes[i];
+            const long long need = (total_paths + sh[i].block - 1) / (sh[i].block > 0 ? sh[i].block : 1);
+            if (need > 0 && need < sh[i].grid) sh[i].grid = static_cast<int>(need);
+        }
         int k = 0;
         mark(k);
-        launch_raygen(d_fp, paths, d_counters, shapes[0], stream);
+        launch_raygen(d_fp, paths, d_counters, sh[0], stream);
         mark(k);
         for (int b = 0; b < mb; ++b) {
-            launch_trace(d_fp, scene, paths, d_counters, b, shapes[1], stream);
+            launch_trace(d_fp, scene, paths, d_counters, b, sh[1], stream);
             mark(k);
             launch_reset_counters(d_counters, b, stream);
             const bool pbr_scene = scene.openpbr_count > 0;
-            launch_shade(d_fp, scene, paths, d_counters, b, shapes[pbr_scene ? 7 : 2], stream);
-            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, shapes, stream);
+            launch_shade(d_fp, scene, paths, d_counters, b, sh[pbr_scene ? 7 : 2], stream);
+            if (b == 0) launch_restir(d_fp, scene, paths, d_counters, sh, stream);
             mark(k);
-            launch_shadow(d_fp, scene, paths, d_counters, b, shapes[3], stream);
+            launch_shadow(d_fp, scene, paths, d_counters, b, sh[3], stream);
             mark(k);
         }
-        launch_finalize(d_fp, paths, d_counters, shapes[4], stream);
+        launch_finalize(d_fp, paths, d_counters, sh[4], stream);
         mark(k);
-        launch_resolve(d_fp, shapes[5], stream);
+        launch_resolve(d_fp, sh[5], stream);
         mark(k);
         stage_count = stage_timing ? k - 1 : 0;
         if (denoise_this_frame) enqueue_denoise();
