@@ -28,6 +28,9 @@ roofline: the launch with the largest share of the frame, per-unit algorithmic
 training: native training steps of the U-Net (rtgb_trainer_step: tcgen05
           forward, input- and weight-gradient convolutions, Adam) on 16 crops
           of 256 x 256, ms per step and algorithmic TFLOP/s.
+workloads: the protocol's C1 (Cornell box, with the CPU oracle on the same
+          full frame) and C3 (1 M triangles, OpenPBR, mixed pinhole / fisheye
+          rig) configurations, ms per frame and Mrays/s.
 cpu_baseline / --impl reference: the CPU oracle (restatement of the reference's
           radiance kernel, with the reference's median-split BVH) on all host
           threads, over a band of rows of the same workload.
@@ -242,7 +245,7 @@ class ClockSampler:
 
 # ---- CPU oracle (baseline / reference arm) ----------------------------------------
 
-def oracle_frames(sc, rig, prof, stride, frames, threads=0):
+def oracle_frames(sc, rig, prof, stride, frames, threads=0, cameras=CAMERAS):
     """Renders `frames` frames of every `stride`-th row on the CPU oracle;
     returns (rays traced in the last frame, seconds of the last frame)."""
     from oracle.binding import OracleRenderer
@@ -251,11 +254,63 @@ def oracle_frames(sc, rig, prof, stride, frames, threads=0):
     rays = secs = 0.0
     for _ in range(frames):
         t0 = time.perf_counter()
-        orc.render_frame(rig, prof, CAMERAS, row_stride=stride)
+        orc.render_frame(rig, prof, cameras, row_stride=stride)
         secs = time.perf_counter() - t0
-        rays = sum(orc.rays(c) for c in range(CAMERAS))
+        rays = sum(orc.rays(c) for c in range(cameras))
     orc.close()
     return rays, secs
+
+
+def gpu_frames(sc, rig, prof, cameras, warmup, frames):
+    """Prepares the scene and renders warm-up then timed frames on the GPU;
+    returns (prepare ms, ms per frame, Mrays/s) from the frames' CUDA events."""
+    from ray_tracing_gb300.renderer import Renderer
+    r = Renderer()
+    t0 = time.perf_counter()
+    r.prepare_scene(sc.view)
+    prep_ms = 1000.0 * (time.perf_counter() - t0)
+    r.reset_sequence(SEED)
+    for _ in range(warmup):
+        r.render_frame(rig, prof, cameras)
+    ms = rays = 0.0
+    for _ in range(frames):
+        v = r.render_frame(rig, prof, cameras)
+        ms += v.frame_render_ms
+        rays += v.rays_traced
+    r.close()
+    return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
+
+
+def workload_records():
+    """The other configurations of the reference protocol, measured beside the
+    headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
+    on all host threads renders the same full frame) and C3 (1 M triangles with
+    200 icosphere instances, constant OpenPBR materials, 256 emissive
+    triangles; 2 x pinhole32 640x480 + 2 x equi62_lut1d 1280x1024 fisheye in one
+    launch; 1 spp, depth 4, ReSTIR DI on; no analytic lights, so emissive NEE
+    carries the direct light)."""
+    from ray_tracing_gb300 import scenes
+    out = {}
+    sc = scenes.HostScene("cornell_box")
+    rig = scenes.default_rig("cornell_box", 1)
+    prof = scenes.profile("quality", samples_per_pixel=64, max_bounces=8, enable_denoise=0, enable_restir_di=0)
+    prep, ms, mrays = gpu_frames(sc, rig, prof, 1, 2, 5)
+    cores = os.cpu_count() or 1
+    rays, secs = oracle_frames(sc, rig, prof, 1, 1, threads=cores, cameras=1)
+    out["C1_cornell_256x256_64spp_d8"] = {
+        "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep,
+        "cpu_oracle": {"ms_per_frame": 1000.0 * secs, "mrays_per_s": rays / secs / 1e6, "cores": cores,
+                       "sample": "the full frame, reference BVH"},
+        "gpu_over_cpu": (1000.0 * secs) / ms if ms > 0 else None}
+    sc.close()
+    sc = scenes.HostScene("triangle_terrain_pbr", detail=1000000)
+    rig = scenes.default_rig("triangle_terrain_pbr", 4)
+    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1)
+    prep, ms, mrays = gpu_frames(sc, rig, prof, 4, 3, 10)
+    out["C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280"] = {
+        "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
+    sc.close()
+    return out
 
 
 def cpu_baseline(sc, rig, prof):
@@ -537,6 +592,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if world == 1 and not args.no_training:
         line["training"] = training_record()
+    if world == 1 and not args.no_workloads:
+        line["workloads"] = workload_records()
     if world == 1 and not args.no_relmse:
         line["equal_relmse"] = equal_relmse(sc, rig, prof)
     if world == 1 and not args.no_cpu_baseline:
@@ -554,6 +611,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
+    ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 workload records")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

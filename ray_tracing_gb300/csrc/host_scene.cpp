@@ -612,7 +612,11 @@ void build_openpbr_gallery(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
 // instances, constant per-object materials, and `emissive` emissive
 // triangles (a fraction of the icosphere faces). The triangle budget is
 // `detail` (default 1,000,000).
-void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
+// The 1 M-triangle terrain with 200 icosphere instances and 256 emissive
+// triangles; with `pbr` every non-emissive surface is an OpenPBR material
+// with constant parameters (the instances: base colour U(0,1)^3, specular
+// roughness U(0.05,1), metalness Bernoulli(0.3), specular IOR 1.5).
+void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail, bool pbr = false) {
     Builder b(s);
     SplitMix rng(0x7e77a1000ull ^ seed);
     const int64_t budget = detail > 0 ? detail : 1000000;
@@ -659,7 +663,15 @@ void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
         return 0.8 * std::sin(0.21 * x + phase[0]) * std::cos(0.17 * z + phase[1])
                + 0.35 * std::sin(0.57 * x + 0.31 * z + phase[2]) + 0.12 * std::cos(1.3 * z - 0.7 * x + phase[3]);
     };
-    const int terrain = b.diffuse({0.45, 0.42, 0.38});
+    auto pbr_material = [&](const Vec3& color, double roughness, double metalness) {
+        rtgb_openpbr_material om = openpbr_defaults();
+        for (int k = 0; k < 3; ++k) om.base_color[k] = static_cast<float>(color[k]);
+        om.specular_roughness = static_cast<float>(roughness);
+        om.base_metalness = static_cast<float>(metalness);
+        om.specular_ior = 1.5f;
+        return b.openpbr(om);
+    };
+    const int terrain = pbr ? pbr_material({0.45, 0.42, 0.38}, 0.6, 0.0) : b.diffuse({0.45, 0.42, 0.38});
     for (int j = 0; j < n; ++j) {
         for (int i = 0; i < n; ++i) {
             const double x0 = -extent + 2.0 * extent * i / n, x1 = -extent + 2.0 * extent * (i + 1) / n;
@@ -676,7 +688,8 @@ void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
         const double r = rng.uniform(0.3, 1.2);
         const double cx = rng.uniform(-extent * 0.8, extent * 0.8), cz = rng.uniform(-extent * 0.8, extent * 0.8);
         const Vec3 center {cx, height(cx, cz) + r * 1.05, cz};
-        const int m = b.diffuse({rng.uniform(), rng.uniform(), rng.uniform()});
+        const Vec3 color {rng.uniform(), rng.uniform(), rng.uniform()};
+        const int m = pbr ? pbr_material(color, rng.uniform(0.05, 1.0), rng.uniform() < 0.3 ? 1.0 : 0.0) : b.diffuse(color);
         const bool is_light_host = k % 25 == 0;
         const int light_m = is_light_host ? b.emissive({8.0, 7.0, 6.0}) : -1;
         for (size_t f = 0; f < faces.size(); ++f) {
@@ -808,6 +821,7 @@ rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t deta
     else if (n == "restir_acceptance") build_restir_acceptance(*s);
     else if (n == "random_spheres") build_random_spheres(*s, seed, detail);
     else if (n == "triangle_terrain") build_triangle_terrain(*s, seed, detail);
+    else if (n == "triangle_terrain_pbr") build_triangle_terrain(*s, seed, detail, true);
     else if (n == "openpbr_gallery") build_openpbr_gallery(*s, seed, detail);
     else {
         delete s;
@@ -908,7 +922,7 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
         for (int i = 0; i < camera_count; ++i) rig->cameras[i] = c;
         return RTGB_OK;
     }
-    if (n == "triangle_terrain") {
+    if (n == "triangle_terrain" || n == "triangle_terrain_pbr") {
         // mixed rig: 2x pinhole32 640x480 (hfov 90) + 2x equi62_lut1d 1280x1024 (180 deg)
         for (int i = 0; i < camera_count; ++i) {
             const bool equi = i >= 2;
