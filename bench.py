@@ -281,7 +281,7 @@ def gpu_frames(sc, rig, prof, cameras, warmup, frames):
     return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
 
 
-def workload_records():
+def workload_records(names=("c1", "c3"), c3_steps=10, c3_warmup=3):
     """The other configurations of the reference protocol, measured beside the
     headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
     on all host threads renders the same full frame) and C3 (1 M triangles with
@@ -291,25 +291,30 @@ def workload_records():
     carries the direct light)."""
     from ray_tracing_gb300 import scenes
     out = {}
-    sc = scenes.HostScene("cornell_box")
-    rig = scenes.default_rig("cornell_box", 1)
-    prof = scenes.profile("quality", samples_per_pixel=64, max_bounces=8, enable_denoise=0, enable_restir_di=0)
-    prep, ms, mrays = gpu_frames(sc, rig, prof, 1, 2, 5)
-    cores = os.cpu_count() or 1
-    rays, secs = oracle_frames(sc, rig, prof, 1, 1, threads=cores, cameras=1)
-    out["C1_cornell_256x256_64spp_d8"] = {
-        "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep,
-        "cpu_oracle": {"ms_per_frame": 1000.0 * secs, "mrays_per_s": rays / secs / 1e6, "cores": cores,
-                       "sample": "the full frame, reference BVH"},
-        "gpu_over_cpu": (1000.0 * secs) / ms if ms > 0 else None}
-    sc.close()
-    sc = scenes.HostScene("triangle_terrain_pbr", detail=1000000)
-    rig = scenes.default_rig("triangle_terrain_pbr", 4)
-    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1)
-    prep, ms, mrays = gpu_frames(sc, rig, prof, 4, 3, 10)
-    out["C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280"] = {
-        "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
-    sc.close()
+    if "c1" not in names:
+        sc = None
+    else:
+        sc = scenes.HostScene("cornell_box")
+    if sc is not None:
+        rig = scenes.default_rig("cornell_box", 1)
+        prof = scenes.profile("quality", samples_per_pixel=64, max_bounces=8, enable_denoise=0, enable_restir_di=0)
+        prep, ms, mrays = gpu_frames(sc, rig, prof, 1, 2, 5)
+        cores = os.cpu_count() or 1
+        rays, secs = oracle_frames(sc, rig, prof, 1, 1, threads=cores, cameras=1)
+        out["C1_cornell_256x256_64spp_d8"] = {
+            "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep,
+            "cpu_oracle": {"ms_per_frame": 1000.0 * secs, "mrays_per_s": rays / secs / 1e6, "cores": cores,
+                           "sample": "the full frame, reference BVH"},
+            "gpu_over_cpu": (1000.0 * secs) / ms if ms > 0 else None}
+        sc.close()
+    if "c3" in names:
+        sc = scenes.HostScene("triangle_terrain_pbr", detail=1000000)
+        rig = scenes.default_rig("triangle_terrain_pbr", 4)
+        prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1)
+        prep, ms, mrays = gpu_frames(sc, rig, prof, 4, c3_warmup, c3_steps)
+        out["C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280"] = {
+            "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
+        sc.close()
     return out
 
 
@@ -612,11 +617,17 @@ def main():
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
     ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 workload records")
+    ap.add_argument("--workload", choices=["c1", "c3"], default=None,
+                    help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload is not None:
+        if rank == 0:
+            print(json.dumps({"workloads": workload_records((args.workload,), args.steps, args.warmup)}), flush=True)
+        return 0
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
