@@ -489,6 +489,20 @@ def roofline(stage_ms, frames_stats, spatial):
             "stage_ms_per_frame": by_kernel}
 
 
+def replica_reduce(value: float, op: str, device="cpu") -> float:
+    """`value` combined over the replicas of the process group ("max": the
+    slowest rank's time, "sum": whole-job totals); unchanged without a group.
+    `device` is where the collective's tensor lives (cuda:N under NCCL, cpu
+    under gloo)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -542,13 +556,8 @@ def run_ours(args, rank, world, local_rank):
     clocks = sampler.stop()
     rays = float(np.sum(r.ray_totals() - rays0))
     total_ms = float(sum(frame_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        rt = torch.tensor([rays], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(rt, op=dist.ReduceOp.SUM)
-        rays = float(rt.item())
+    total_ms = replica_reduce(total_ms, "max", f"cuda:{local_rank}")
+    rays = replica_reduce(rays, "sum", f"cuda:{local_rank}")
     value = rays / (total_ms * 1e-3) / 1e6
 
     # e2e: public API with host buffers (pinned), wall clock per step
@@ -575,10 +584,7 @@ def run_ours(args, rank, world, local_rank):
     e2e = {"value": e2e_rays / e2e_secs / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d // e2e_steps),
            "d2h_bytes_per_step": CAMERAS * pixels * (16 * 3 + 4), "steps": e2e_steps,
            "ms_per_step": 1000.0 * e2e_secs / e2e_steps}
-    if world > 1:
-        t = torch.tensor([e2e["value"]], dtype=torch.float64, device=f"cuda:{local_rank}")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e["value"] = float(t.item())
+    e2e["value"] = replica_reduce(e2e["value"], "sum", f"cuda:{local_rank}")
 
     if rank != 0:
         return 0
