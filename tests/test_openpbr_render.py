@@ -98,3 +98,23 @@ def test_gallery_gpu_matches_oracle(restir):
     g = gpu.download(0).beauty_rgba[..., :3].astype(np.float64)
     o = orc.buffer(0, "beauty")[..., :3].astype(np.float64)
     assert abs(g.mean() - o.mean()) <= 2e-2 * o.mean(), (g.mean(), o.mean())
+
+
+@pytest.mark.gpu
+def test_c3_terrain_openpbr_mixed_cameras_match_oracle():
+    """The C3 configuration's path at a size the oracle finishes quickly:
+    OpenPBR (constant parameters, metal and dielectric) on triangles with
+    emissive triangles, seen by a pinhole and a distorted 180-degree equi62
+    fisheye camera in one launch."""
+    from helpers import equi, look_at, pinhole, rig_of
+    cams = [pinhole(64, 48, 90.0), equi(80, 64, 180.0, radial=(0.01, -0.003, 0.0008, -0.0002, 5e-5, -1e-5),
+                                         tangential=(0.0007, -0.0005))]
+    for i, c in enumerate(cams):
+        ang = np.radians(90.0 * i + 30.0)
+        look_at(c, (0.0, 4.0, 0.0), (np.sin(ang), 3.6, np.cos(ang)), (0.0, 1.0, 0.0))
+    rig = rig_of(*cams)
+    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=0)
+    sc, gpu, orc = render_both("triangle_terrain_pbr", rig, prof, frames=2, detail=30000, oracle_bvh=True)
+    assert sc.view.openpbr_material_count > 100
+    for cam in range(2):
+        _check(gpu, orc, cam, 1, 4)
