@@ -67,22 +67,24 @@ constexpr int kConvSmem = 227 * 1024;
 
 constexpr int kMaxStages = 4;
 
-// Halo stages of a layer: the most (<= kMaxStages, >= 2) that still let two
-// CTAs share an SM (two sets of issuer warps keep the tensor core busier than
-// a deeper ring), else as many as fit beside the weights.
+// Halo stages of a layer, even so that two issuer warps can share the CTA:
+// 4 or 2, whichever still lets two CTAs share an SM (two sets of issuers keep
+// the tensor core busier than a deeper ring), else the larger that fits
+// beside the weights, else 1 (one issuer).
 int conv_stages(int cin, int cout) {
     const int stage = (cin / 8) * kBoxStride;
     const int fixed = 256 + 9 * cin * cout * 2;
-    for (int s = kMaxStages; s >= 2; --s) {
+    for (int s = kMaxStages; s >= 2; s -= 2) {
         const int bytes = (fixed + s * stage + 1023) & ~1023;
         if (2 * (bytes + 1024) <= 228 * 1024) return s;
     }
     const int room = (kConvSmem - fixed) / stage;
-    return room < 1 ? 1 : (room > kMaxStages ? kMaxStages : room);
+    return room >= 4 ? 4 : (room >= 2 ? 2 : 1);
 }
 
-int conv_smem_bytes(int cin, int cout) {
-    const int need = 256 + conv_stages(cin, cout) * (cin / 8) * kBoxStride + 9 * cin * cout * 2;
+// Shared memory of a CTA with `stages` halo stages (0: conv_stages).
+int conv_smem_bytes(int cin, int cout, int stages = 0) {
+    const int need = 256 + (stages > 0 ? stages : conv_stages(cin, cout)) * (cin / 8) * kBoxStride + 9 * cin * cout * 2;
     return (need + 1023) & ~1023;
 }
 
@@ -292,11 +294,16 @@ __global__ void __launch_bounds__(kConvThreads, 2) k_conv3x3(const __grid_consta
         }
         __syncwarp();
     } else if (warp <= kIssuers) {
-        // ---- issuers: tile j (j % kIssuers == warp - 1) from stage j % stages into accumulator j % kAccs.
+        // ---- issuers: tile j (j % issuers == warp - 1) from stage j % stages into accumulator j % kAccs.
+        // A parity wait on an mbarrier only tells two consecutive phases apart, so each barrier's
+        // rounds must be waited for in order by one thread: with an even stage count every tile of
+        // a stage (and of an accumulator) has the same parity of j, so two issuers can alternate;
+        // with an odd count one issuer takes every tile.
         // Descriptors are built once and advanced by constant deltas (their address field is the
         // shared-memory address / 16 and every address stays inside this CTA's window, so the adds
         // never carry out of it).
-        if (lane == 0) {
+        const int issuers = (stages & 1) == 0 ? kIssuers : 1;
+        if (lane == 0 && warp - 1 < issuers) {
             const uint32_t idesc = tc::idesc_bf16_f32(128, a.cout);
             const uint32_t bstep = static_cast<uint32_t>(a.cout) * 16u;
             const uint64_t b_first = tc::smem_desc(tc::smem_u32(sb), bstep, 128);
@@ -304,7 +311,7 @@ __global__ void __launch_bounds__(kConvThreads, 2) k_conv3x3(const __grid_consta
             const uint64_t a_step = static_cast<uint64_t>((2 * kBoxStride) >> 4);  // next two channel boxes
             const int ksteps = boxes >> 1;
             int last = -1;
-            for (int j = warp - 1; j < count; j += kIssuers) {
+            for (int j = warp - 1; j < count; j += issuers) {
                 const int s = j % stages;
                 const int b = j % kAccs;
                 if (!tc::mbar_wait_or_abort(full_bar + s, static_cast<uint32_t>(j / stages) & 1u, kSpin, stop)) {
@@ -444,13 +451,13 @@ cudaError_t conv_init() {
 // Launches k_conv3x3; `map` must describe x (conv_input_map).
 cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
     int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream,
-    void* pool, int up) {
+    void* pool, int up, int stages) {
     const cudaError_t attr = conv_init();
     if (attr != cudaSuccess) return attr;
+    if (stages <= 0 || stages > kMaxStages || conv_smem_bytes(cin, cout, stages) > kConvSmem) stages = conv_stages(cin, cout);
     ConvArgs a{n, h, w, cin, cout, y_channels, y_offset, relu, static_cast<const uint4*>(weight), bias,
-        static_cast<__nv_bfloat16*>(y), err, static_cast<__nv_bfloat16*>(pool), up, conv_stages(cin, cout),
-        conv_tmem_cols(cout)};
-    const int smem = conv_smem_bytes(cin, cout);
+        static_cast<__nv_bfloat16*>(y), err, static_cast<__nv_bfloat16*>(pool), up, stages, conv_tmem_cols(cout)};
+    const int smem = conv_smem_bytes(cin, cout, stages);
     // resident CTAs per SM: 228 KB of shared memory (1 KB reserved per CTA),
     // 512 TMEM columns (conv_tmem_cols each, so no allocation ever waits),
     // 2048 threads and 64 K registers
@@ -654,6 +661,9 @@ struct Acts {
     __nv_bfloat16 *p1 = nullptr, *t2 = nullptr, *cat2 = nullptr, *t4 = nullptr, *t4b = nullptr;
     __nv_bfloat16 *p2 = nullptr, *t3 = nullptr, *t3b = nullptr;
     CUtensorMap maps[kLayerCount];
+    int stages[kLayerCount] = {};  // halo stages per layer chosen by unet_tune (0: the conv_stages rule)
+    bool tuned = false;
+    DevMem scratch_err;            // error flag of the tuning launches
 };
 
 struct UNet {
@@ -768,8 +778,100 @@ Acts* unet_buffers(UNet* unet, int n, int h, int w) {
 
 }  // namespace
 
+namespace {
+
+// Output side of layer li in the U-Net pass over an (n, h, w) batch: its
+// input size, output tensor, channel count and offset, fused pooling and
+// upsampling (as unet_run issues it).
+struct LayerCall {
+    int hh, ww;
+    void* y;
+    int ych, yoff;
+    void* pool;
+    int up;
+};
+
+LayerCall layer_call(const Acts* a, int li, int h, int w) {
+    const int h2 = (h + 1) / 2, w2 = (w + 1) / 2, h4 = (h2 + 1) / 2, w4 = (w2 + 1) / 2;
+    const bool up2 = 2 * h4 == h2 && 2 * w4 == w2, up1 = 2 * h2 == h && 2 * w2 == w;
+    switch (li) {
+        case 0: return {h, w, a->t1, 32, 0, nullptr, 0};
+        case 1: return {h, w, a->cat1, 80, 0, a->p1, 0};
+        case 2: return {h2, w2, a->t2, 48, 0, nullptr, 0};
+        case 3: return {h2, w2, a->cat2, 112, 0, a->p2, 0};
+        case 4: return {h4, w4, a->t3, 64, 0, nullptr, 0};
+        case 5: return up2 ? LayerCall{h4, w4, a->cat2, 112, 48, nullptr, 1} : LayerCall{h4, w4, a->t3b, 64, 0, nullptr, 0};
+        case 6: return {h2, w2, a->t4, 48, 0, nullptr, 0};
+        case 7: return up1 ? LayerCall{h2, w2, a->cat1, 80, 32, nullptr, 1} : LayerCall{h2, w2, a->t4b, 48, 0, nullptr, 0};
+        case 8: return {h, w, a->t5, 32, 0, nullptr, 0};
+        case 9: return {h, w, a->t6, 32, 0, nullptr, 0};
+        default: return {h, w, a->out16, 16, 0, nullptr, 0};
+    }
+}
+
+// Picks each layer's halo-stage count for this batch shape by timing the
+// layer with every even count that fits shared memory (best of three
+// launches, on the set's own buffers; the outputs are overwritten by the
+// next pass). A layer where none fits keeps the rule (0).
+bool unet_tune(UNet* unet, Acts* a) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int* err = static_cast<int*>(a->scratch_err.ensure(sizeof(int)));
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (err == nullptr || cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return false;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    bool ok = true;
+    for (int li = 0; li < kLayerCount && ok; ++li) {
+        const LayerSpec& l = kLayers[li];
+        const LayerCall c = layer_call(a, li, a->h, a->w);
+        float best = 1e30f;
+        int best_s = 0;
+        for (int s = 2; s <= kMaxStages; s += 2) {  // even counts: two issuers per CTA
+            if (conv_smem_bytes(l.cin, l.cout, s) > kConvSmem) continue;
+            float t_min = 1e30f;
+            for (int rep = 0; rep < 3 && ok; ++rep) {
+                cudaEventRecord(e0, st);
+                ok = launch_conv3x3(a->maps[li], a->n, c.hh, c.ww, l.cin, unet->weights[li].p,
+                         static_cast<const float*>(unet->biases[li].p), l.cout, l.relu, c.y, c.ych, c.yoff, err, sms, st,
+                         c.pool, c.up, s) == cudaSuccess;
+                cudaEventRecord(e1, st);
+                ok = ok && cudaEventSynchronize(e1) == cudaSuccess;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                t_min = ms < t_min ? ms : t_min;
+            }
+            if (t_min < best) {
+                best = t_min;
+                best_s = s;
+            }
+        }
+        a->stages[li] = best_s;
+    }
+    int h_err = 0;
+    ok = ok && cudaMemcpy(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && h_err == 0;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (!ok) {
+        for (int& s : a->stages) s = 0;  // fall back to the rule
+    }
+    return ok;
+}
+
+}  // namespace
+
 bool unet_prepare(UNet* unet, int n, int h, int w) {
-    return conv_init() == cudaSuccess && unet_buffers(unet, n, h, w) != nullptr;
+    if (conv_init() != cudaSuccess) return false;
+    Acts* a = unet_buffers(unet, n, h, w);
+    if (a == nullptr) return false;
+    if (unet->ready && !a->tuned) {
+        unet_tune(unet, a);
+        a->tuned = true;
+    }
+    return true;
 }
 
 cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, int n, int h, int w, float4* out,
@@ -782,7 +884,7 @@ cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, 
     auto conv = [&](int li, int hh, int ww, void* y, int ych, int yoff, void* pool = nullptr, int up = 0) {
         const LayerSpec& l = kLayers[li];
         return launch_conv3x3(net->maps[li], n, hh, ww, l.cin, unet->weights[li].p, static_cast<const float*>(unet->biases[li].p),
-            l.cout, l.relu, y, ych, yoff, err, sms, stream, pool, up);
+            l.cout, l.relu, y, ych, yoff, err, sms, stream, pool, up, net->stages[li]);
     };
     cudaError_t e;
     const long long hw = static_cast<long long>(h) * w;

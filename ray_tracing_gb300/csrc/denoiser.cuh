@@ -49,9 +49,10 @@ cudaError_t conv_init();
 // weights packed as rtgb_conv3x3_pack_weights, output written at channel
 // y_offset of a y_channels tensor (twice the size when `up`), and the 2 x 2
 // average of the output into `pool` when it is non-null.
+// `stages`: halo stages in shared memory, 0 for the built-in rule.
 cudaError_t launch_conv3x3(const CUtensorMap& map, int n, int h, int w, int cin, const void* weight, const float* bias,
     int cout, int relu, void* y, int y_channels, int y_offset, int* err, int grid_limit, cudaStream_t stream,
-    void* pool = nullptr, int up = 0);
+    void* pool = nullptr, int up = 0, int stages = 0);
 // Weight (cout x cin x 3 x 3, FP32) and bias gradients of a k_conv3x3 layer
 // (denoiser_train.cu); `partial` holds wgrad_partial_bytes(sms, cout).
 cudaError_t launch_conv3x3_wgrad(const void* x, int n, int h, int w, int cin, const void* dy, int cout, float* dweight,
