@@ -112,7 +112,8 @@ def build_cli() -> Path:
     """The render_realtime CLI and the scene-lifecycle benchmark (C++23 over the
     C ABI), linked against librtgb.so."""
     CLI.parent.mkdir(exist_ok=True)
-    deps = [CLI_SRC, CSRC / "cli" / "benchmark_report.h", CSRC / "cli" / "png_writer.h", INCLUDE / "rtgb.h", LIB]
+    deps = [CLI_SRC, CSRC / "cli" / "benchmark_report.h", CSRC / "cli" / "png_writer.h", CSRC / "cli" / "exr_writer.h",
+            INCLUDE / "rtgb.h", LIB]
     if _stale(CLI, deps):
         rev = "unknown"
         try:

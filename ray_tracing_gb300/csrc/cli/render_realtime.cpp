@@ -1,7 +1,8 @@
 // render_realtime: the reference's realtime benchmark CLI (utils/render_realtime.cpp)
 // over this library's C ABI. Same flags, the same per-frame console lines, and
 // the same artifacts in --output-dir: frame_XXXX_cam_N.png (unless
-// --skip-image-write), benchmark_frames.csv, benchmark_summary.json (schema 3)
+// --skip-image-write; with --write-exr also frame_XXXX_cam_N.exr, the linear
+// radiance as 32-bit float B/G/R), benchmark_frames.csv, benchmark_summary.json (schema 3)
 // and benchmark_manifest.json (FNV-1a64 digests). One library handle renders
 // all cameras of a frame in one launch sequence, so the reference's
 // per-camera worker threads become one worker; render_ms is the whole frame's
@@ -9,7 +10,7 @@
 //
 // Extra flags: --width/--height (default 640 x 480, the reference's fixed
 // size), --denoiser-weights (default: the weights shipped beside the
-// library), --device.
+// library), --device, --write-exr.
 #include <sys/utsname.h>
 
 #include <chrono>
@@ -30,6 +31,7 @@
 #include <vector>
 
 #include "benchmark_report.h"
+#include "exr_writer.h"
 #include "png_writer.h"
 #include "rtgb.h"
 
@@ -65,6 +67,7 @@ struct Args {
     std::string scene = "smoke";
     std::string profile;
     bool skip_image_write = false;
+    bool write_exr = false;
     int width = 640;
     int height = 480;
     int device = 0;
@@ -76,7 +79,7 @@ void usage(FILE* out) {
         "usage: render_realtime [--camera-count N] [--frames N] [--warmup-frames N] [--seed S]\n"
         "                       [--output-dir DIR] [--scene NAME] [--profile quality|balanced|realtime]\n"
         "                       [--skip-image-write] [--width W] [--height H] [--device D]\n"
-        "                       [--denoiser-weights FILE]");
+        "                       [--denoiser-weights FILE] [--write-exr]");
 }
 
 template <class T>
@@ -104,6 +107,8 @@ std::optional<Args> parse(int argc, char** argv) {
         bool ok = true;
         if (k == "--skip-image-write") {
             a.skip_image_write = true;
+        } else if (k == "--write-exr") {
+            a.write_exr = true;
         } else if (k == "--help" || k == "-h") {
             usage(stdout);
             std::exit(EXIT_SUCCESS);
@@ -343,6 +348,10 @@ int run(const Args& a) {
                     char name[64];
                     std::snprintf(name, sizeof name, "frame_%04d_cam_%d.png", f, c);
                     rtgb::png::write_rgb(out_dir / name, a.width, a.height, rgb.data());
+                    if (a.write_exr) {
+                        std::snprintf(name, sizeof name, "frame_%04d_cam_%d.exr", f, c);
+                        rtgb::exr::write_rgba(out_dir / name, a.width, a.height, b.data());
+                    }
                     fr.image_write_ms += ms_since(t0);
                 }
                 fr.cameras.push_back(cs);

@@ -142,6 +142,31 @@ def test_direction_debug_matches_oracle():
         assert np.abs(g.astype(int) - o.astype(int)).max() <= 1   # reference contract: +-2 LSB
 
 
+def _display_u8(v: np.ndarray) -> np.ndarray:
+    """linear_to_display_u8 (src/realtime/display_transfer.h:9-15): sqrt of the
+    clamped-positive value, clamp to [0, 0.999], scale by 255 in float32, round
+    half away from zero (the values are non-negative, so floor(x + 0.5) in
+    float64 is exact)."""
+    c = np.clip(np.sqrt(np.maximum(v.astype(np.float32), np.float32(0))), np.float32(0), np.float32(0.999))
+    return np.floor((c * np.float32(255)).astype(np.float64) + 0.5).astype(np.uint8)
+
+
+def test_tonemap_matches_display_transfer():
+    from ray_tracing_gb300.renderer import Renderer
+    rig = scaled_rig(scenes.default_rig("random_spheres", 2), 0.15)
+    prof = scenes.profile("balanced", samples_per_pixel=2, max_bounces=3, enable_denoise=0)
+    sc = scenes.HostScene("random_spheres")
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    r.render_frame(rig, prof, 2)
+    for cam in range(2):
+        beauty = r.download(cam).beauty_rgba
+        got = r.tonemap_rgba8(cam)
+        assert np.array_equal(got[..., :3], _display_u8(beauty[..., :3]))
+        assert np.all(got[..., 3] == 255)
+        assert 0 < got[..., :3].mean() < 254
+
+
 def test_lbvh_morton_order_matches_cpu_restatement():
     from oracle.lbvh import lbvh_reference
     from ray_tracing_gb300.renderer import Renderer

@@ -1,10 +1,12 @@
 """The render_realtime CLI (utils/render_realtime.cpp's flags and artifacts).
 
-CPU: argument validation, and the report writer and PNG writer through a small
-harness compiled against the CLI's headers (schema-3 summary, CSV columns,
-nearest-rank percentiles, FNV-1a64 manifest digests as
-tests/test_realtime_benchmark_report.cpp of the reference checks them).
-GPU: a short run writes every artifact.
+CPU: argument validation, and the report writer, PNG writer and OpenEXR writer
+through small harnesses compiled against the CLI's headers (schema-3 summary,
+CSV columns, nearest-rank percentiles, FNV-1a64 manifest digests as
+tests/test_realtime_benchmark_report.cpp of the reference checks them; EXR
+files read back by an independent parser of the published file layout).
+GPU: a short run writes every artifact, the EXR frames holding the same linear
+radiance whose mean luminance the summary reports.
 """
 from __future__ import annotations
 
@@ -16,6 +18,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
+from _exr import read_exr
 from _png import read_png
 from ray_tracing_gb300 import build as _build
 
@@ -128,10 +131,53 @@ def test_report_and_png_writers(tmp_path):
     assert np.array_equal(img, want)
 
 
+EXR_HARNESS = r"""
+#include <cmath>
+#include "exr_writer.h"
+int main(int argc, char** argv) {
+    std::filesystem::path d = argv[1];
+    const int w = 13, h = 6;
+    std::vector<float> rgba(static_cast<size_t>(w) * h * 4);
+    for (size_t i = 0; i < rgba.size(); ++i) rgba[i] = std::ldexp(static_cast<float>(i % 97) - 20.0f, static_cast<int>(i % 7) - 3);
+    rtgb::exr::write_rgba(d / "rgb.exr", w, h, rgba.data());
+    rtgb::exr::write_rgba(d / "rgba.exr", w, h, rgba.data(), true);
+    bool threw = false;
+    try {
+        rtgb::exr::encode(w, h, {"R", "G"}, rgba.data());
+    } catch (const std::runtime_error&) {
+        threw = true;
+    }
+    (void)argc;
+    return threw ? 0 : 3;
+}
+"""
+
+
+def test_exr_writer(tmp_path):
+    src = tmp_path / "exr.cpp"
+    src.write_text(EXR_HARNESS)
+    exe = tmp_path / "exr"
+    subprocess.run(["g++", "-std=c++23", "-O1", "-I", str(CLI_DIR), str(src), "-o", str(exe)], check=True)
+    subprocess.run([str(exe), str(tmp_path)], check=True)
+    w, h = 13, 6
+    i = np.arange(w * h * 4)
+    want = np.ldexp((i % 97).astype(np.float32) - 20.0, (i % 7) - 3).astype(np.float32).reshape(h, w, 4)
+    for name, chans in (("rgb", ["B", "G", "R"]), ("rgba", ["A", "B", "G", "R"])):
+        attrs, img = read_exr(tmp_path / f"{name}.exr")
+        assert attrs["channels"] == chans
+        assert attrs["dataWindow"] == (0, 0, w - 1, h - 1) and attrs["displayWindow"] == (0, 0, w - 1, h - 1)
+        assert attrs["lineOrder"] == 0 and attrs["pixelAspectRatio"] == 1.0 and attrs["screenWindowWidth"] == 1.0
+        for k, c in enumerate("RGBA"):
+            if c in chans:
+                assert np.array_equal(img[c], want[..., k]), c
+    size = (tmp_path / "rgb.exr").stat().st_size
+    assert size > h * (8 + 8 + w * 3 * 4)
+
+
 @pytest.mark.gpu
 def test_cli_writes_all_artifacts(cli, tmp_path):
     res = subprocess.run([str(cli), "--scene", "smoke", "--camera-count", "2", "--frames", "2", "--warmup-frames", "1",
-                          "--seed", "5", "--width", "96", "--height", "72", "--output-dir", str(tmp_path)],
+                          "--seed", "5", "--width", "96", "--height", "72", "--output-dir", str(tmp_path), "--write-exr"],
                          capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr
     assert "summary profile=balanced" in res.stdout
@@ -144,3 +190,8 @@ def test_cli_writes_all_artifacts(cli, tmp_path):
         for c in range(2):
             img = read_png(tmp_path / f"frame_{f:04d}_cam_{c}.png")
             assert img.shape == (72, 96, 3) and img.max() > 0
+            _, hdr = read_exr(tmp_path / f"frame_{f:04d}_cam_{c}.exr")
+            assert hdr["R"].shape == (72, 96) and all(np.isfinite(hdr[k]).all() for k in "RGB")
+            lum = (0.2126 * hdr["R"].astype(np.float64) + 0.7152 * hdr["G"] + 0.0722 * hdr["B"]).mean()
+            rec = [r for r in summary["per-camera"] if r["frame_index"] == f and r["camera_index"] == c]
+            assert len(rec) == 1 and lum == pytest.approx(rec[0]["average_luminance"], rel=1e-5)
