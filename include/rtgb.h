@@ -531,6 +531,18 @@ void rtgb_host_scene_destroy(rtgb_host_scene* scene);
 /* A view of the scene's arrays (owned by the host scene). */
 rtgb_status rtgb_host_scene_view(const rtgb_host_scene* scene, rtgb_scene* out_view);
 
+/* Scene files: the packed arrays of a host scene (from a builtin builder or
+ * from the SceneIR v2 adapter of rtgb_scene_ir_v2.hpp) written to / read from
+ * disk, so a scene compiled once renders from any caller of this ABI. Format:
+ * "RTGBSCN1", a version word, the byte size of each record type (a file from
+ * a build with other record layouts is refused), then per array a 64-bit
+ * count and the records, all little-endian. No reference counterpart (its
+ * packed scenes live only in memory). */
+rtgb_status rtgb_host_scene_save(const rtgb_host_scene* scene, const char* path);
+rtgb_status rtgb_host_scene_load(const char* path, rtgb_host_scene** out_scene);
+/* A host scene holding copies of a view's arrays (the view is not kept). */
+rtgb_status rtgb_host_scene_from_view(const rtgb_scene* view, rtgb_host_scene** out_scene);
+
 /* make_equi62_lut1d_params (src/realtime/camera_models.cpp:228-248). */
 rtgb_status rtgb_make_equi62_lut1d(int32_t width, int32_t height, double fx, double fy,
     double cx, double cy, const double radial[6], const double tangential[2],

@@ -252,6 +252,9 @@ SIGNATURES = {
     "rtgb_host_scene_create": (C.c_int, [C.c_char_p, C.c_uint32, C.c_int64, P(C.c_void_p)]),
     "rtgb_host_scene_destroy": (None, [C.c_void_p]),
     "rtgb_host_scene_view": (C.c_int, [C.c_void_p, P(Scene)]),
+    "rtgb_host_scene_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "rtgb_host_scene_load": (C.c_int, [C.c_char_p, P(C.c_void_p)]),
+    "rtgb_host_scene_from_view": (C.c_int, [P(Scene), P(C.c_void_p)]),
     "rtgb_make_equi62_lut1d": (C.c_int, [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double,
                                          C.c_double, P(C.c_double), P(C.c_double), P(Equi62Lut1d)]),
     "rtgb_pack_camera_pose": (C.c_int, [P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_double)]),

@@ -10,24 +10,17 @@
 
 #include <algorithm>
 #include <array>
+#include <bit>
+#include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <memory>
 #include <numbers>
 #include <string>
 #include <vector>
 
-struct rtgb_host_scene {
-    std::vector<rtgb_texture> textures;
-    std::vector<float> texels;
-    std::vector<rtgb_material> materials;
-    std::vector<rtgb_sphere> spheres;
-    std::vector<rtgb_quad> quads;
-    std::vector<rtgb_triangle> triangles;
-    std::vector<rtgb_medium> media;
-    std::vector<rtgb_analytic_light> analytic;
-    std::vector<rtgb_openpbr_material> openpbr;
-    std::array<float, 3> background {0.0f, 0.0f, 0.0f};
-};
+#include "host_scene.h"
 
 namespace rtgb {
 namespace {
@@ -808,6 +801,37 @@ Vec3 rotate_about(const Vec3& v, const Vec3& axis, double deg) {
 
 using namespace rtgb;
 
+namespace {
+
+constexpr char kSceneMagic[8] = {'R', 'T', 'G', 'B', 'S', 'C', 'N', '1'};
+constexpr uint32_t kSceneVersion = 1;
+static_assert(std::endian::native == std::endian::little, "scene files are written in host byte order");
+
+// record sizes, in file order; a reader with other layouts refuses the file
+constexpr std::array<uint32_t, 9> kRecordSizes {sizeof(rtgb_texture), sizeof(float), sizeof(rtgb_material),
+    sizeof(rtgb_sphere), sizeof(rtgb_quad), sizeof(rtgb_triangle), sizeof(rtgb_medium), sizeof(rtgb_analytic_light),
+    sizeof(rtgb_openpbr_material)};
+
+template <class F>
+void for_each_array(rtgb_host_scene& s, F&& f) {
+    f(s.textures);
+    f(s.texels);
+    f(s.materials);
+    f(s.spheres);
+    f(s.quads);
+    f(s.triangles);
+    f(s.media);
+    f(s.analytic);
+    f(s.openpbr);
+}
+
+template <class T>
+void copy_array(std::vector<T>& dst, const T* src, int32_t n) {
+    dst.assign(src, src + (src && n > 0 ? n : 0));
+}
+
+}  // namespace
+
 extern "C" {
 
 rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t detail, rtgb_host_scene** out) {
@@ -855,6 +879,73 @@ rtgb_status rtgb_host_scene_view(const rtgb_host_scene* s, rtgb_scene* v) {
     v->openpbr_materials = s->openpbr.data();
     v->openpbr_material_count = static_cast<int32_t>(s->openpbr.size());
     std::memcpy(v->background, s->background.data(), sizeof v->background);
+    return RTGB_OK;
+}
+
+
+rtgb_status rtgb_host_scene_save(const rtgb_host_scene* s, const char* path) {
+    if (s == nullptr || path == nullptr) return RTGB_INVALID_ARGUMENT;
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return RTGB_INVALID_ARGUMENT;
+    bool ok = std::fwrite(kSceneMagic, 1, 8, f) == 8 && std::fwrite(&kSceneVersion, 4, 1, f) == 1 &&
+              std::fwrite(kRecordSizes.data(), 4, kRecordSizes.size(), f) == kRecordSizes.size();
+    for_each_array(const_cast<rtgb_host_scene&>(*s), [&](auto& v) {
+        const uint64_t n = v.size();
+        ok = ok && std::fwrite(&n, 8, 1, f) == 1 && (n == 0 || std::fwrite(v.data(), sizeof v[0], n, f) == n);
+    });
+    ok = ok && std::fwrite(s->background.data(), 4, 3, f) == 3;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? RTGB_OK : RTGB_INVALID_ARGUMENT;
+}
+
+rtgb_status rtgb_host_scene_load(const char* path, rtgb_host_scene** out) {
+    if (path == nullptr || out == nullptr) return RTGB_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return RTGB_INVALID_ARGUMENT;
+    auto s = std::make_unique<rtgb_host_scene>();
+    char magic[8] = {};
+    uint32_t version = 0;
+    std::array<uint32_t, 9> sizes {};
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::equal(magic, magic + 8, kSceneMagic) &&
+              std::fread(&version, 4, 1, f) == 1 && version == kSceneVersion &&
+              std::fread(sizes.data(), 4, sizes.size(), f) == sizes.size() && sizes == kRecordSizes;
+    // counts are bounded by what is left in the file before anything is allocated
+    long here = ok ? std::ftell(f) : 0;
+    std::fseek(f, 0, SEEK_END);
+    const long end = std::ftell(f);
+    std::fseek(f, here, SEEK_SET);
+    for_each_array(*s, [&](auto& v) {
+        uint64_t n = 0;
+        ok = ok && std::fread(&n, 8, 1, f) == 1;
+        here += 8;
+        ok = ok && n <= static_cast<uint64_t>(end - here) / sizeof v[0] && n <= static_cast<uint64_t>(INT32_MAX);
+        if (!ok) return;
+        v.resize(static_cast<size_t>(n));
+        ok = n == 0 || std::fread(v.data(), sizeof v[0], n, f) == n;
+        here += static_cast<long>(n * sizeof v[0]);
+    });
+    ok = ok && std::fread(s->background.data(), 4, 3, f) == 3;
+    std::fclose(f);
+    if (!ok) return RTGB_INVALID_ARGUMENT;
+    *out = s.release();
+    return RTGB_OK;
+}
+
+rtgb_status rtgb_host_scene_from_view(const rtgb_scene* v, rtgb_host_scene** out) {
+    if (v == nullptr || out == nullptr) return RTGB_INVALID_ARGUMENT;
+    auto s = std::make_unique<rtgb_host_scene>();
+    copy_array(s->textures, v->textures, v->texture_count);
+    copy_array(s->texels, v->image_texels, v->image_texel_count > 0 ? 3 * v->image_texel_count : 0);
+    copy_array(s->materials, v->materials, v->material_count);
+    copy_array(s->spheres, v->spheres, v->sphere_count);
+    copy_array(s->quads, v->quads, v->quad_count);
+    copy_array(s->triangles, v->triangles, v->triangle_count);
+    copy_array(s->media, v->media, v->medium_count);
+    copy_array(s->analytic, v->analytic_lights, v->analytic_light_count);
+    copy_array(s->openpbr, v->openpbr_materials, v->openpbr_material_count);
+    std::memcpy(s->background.data(), v->background, sizeof v->background);
+    *out = s.release();
     return RTGB_OK;
 }
 

@@ -1,0 +1,23 @@
+// The packed host scene behind the C ABI's opaque rtgb_host_scene: the arrays
+// an rtgb_scene view points into. Filled by the builtin scene builders
+// (host_scene.cpp), the SceneIR v2 adapter (scene_ir_adapter.cpp) and the
+// scene file reader (rtgb_host_scene_load).
+#pragma once
+
+#include <array>
+#include <vector>
+
+#include "rtgb.h"
+
+struct rtgb_host_scene {
+    std::vector<rtgb_texture> textures;
+    std::vector<float> texels;
+    std::vector<rtgb_material> materials;
+    std::vector<rtgb_sphere> spheres;
+    std::vector<rtgb_quad> quads;
+    std::vector<rtgb_triangle> triangles;
+    std::vector<rtgb_medium> media;
+    std::vector<rtgb_analytic_light> analytic;
+    std::vector<rtgb_openpbr_material> openpbr;
+    std::array<float, 3> background {0.0f, 0.0f, 0.0f};
+};

@@ -16,14 +16,28 @@ from . import abi
 class HostScene:
     """A builtin or procedural scene owned by the C++ host library."""
 
-    def __init__(self, name: str, seed: int = 0, detail: int = 0):
+    def __init__(self, name: str, seed: int = 0, detail: int = 0, *, path=None):
+        """A builtin scene by name, or (``path=``) a scene file written by
+        rtgb_host_scene_save, e.g. one lowered from SceneIR v2."""
         self.lib = abi.load()
-        self.name = name
         self.ptr = C.c_void_p()
-        abi.check(self.lib.rtgb_host_scene_create(name.encode(), seed, detail, C.byref(self.ptr)),
-                  what=f"rtgb_host_scene_create({name})")
+        if path is not None:
+            self.name = str(path)
+            abi.check(self.lib.rtgb_host_scene_load(str(path).encode(), C.byref(self.ptr)),
+                      what=f"rtgb_host_scene_load({path})")
+        else:
+            self.name = name
+            abi.check(self.lib.rtgb_host_scene_create(name.encode(), seed, detail, C.byref(self.ptr)),
+                      what=f"rtgb_host_scene_create({name})")
         self.view = abi.Scene()
         abi.check(self.lib.rtgb_host_scene_view(self.ptr, C.byref(self.view)), what="rtgb_host_scene_view")
+
+    @classmethod
+    def load(cls, path) -> "HostScene":
+        return cls("", path=path)
+
+    def save(self, path) -> None:
+        abi.check(self.lib.rtgb_host_scene_save(self.ptr, str(path).encode()), what=f"rtgb_host_scene_save({path})")
 
     def close(self):
         if self.ptr:

@@ -89,12 +89,14 @@ def compare_paths(gc, gr, oc, orad, rel=1e-4, floor=1e-6):
     return diverged, float(err.max() if err.size else 0.0), bad
 
 
-def render_both(scene_name, rig, profile, frames=1, seed=0, detail=0, oracle_bvh=False, active=None, records=True):
-    """Renders `frames` frames with the GPU path and the oracle; returns both."""
+def render_both(scene_name, rig, profile, frames=1, seed=0, detail=0, oracle_bvh=False, active=None, records=True,
+                scene=None):
+    """Renders `frames` frames with the GPU path and the oracle; returns both.
+    `scene` (a HostScene) replaces the builtin scene of `scene_name`."""
     from oracle.binding import OracleRenderer
     from ray_tracing_gb300.renderer import Renderer
 
-    sc = scenes.HostScene(scene_name, seed=seed, detail=detail)
+    sc = scene if scene is not None else scenes.HostScene(scene_name, seed=seed, detail=detail)
     active = active or rig.active_count
     gpu = Renderer(debug_path_records=records)
     gpu.prepare_scene(sc.view)
