@@ -315,7 +315,48 @@ def workload_records(names=("c1", "c3"), c3_steps=10, c3_warmup=3):
         out["C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280"] = {
             "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
         sc.close()
+    if "c5" in names:
+        out["C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6"] = c5_record()
     return out
+
+
+def c5_record(frames=60, warmup=3, degrees_per_frame=2.0):
+    """C5: the 4 M-triangle textured room (checker / 3D-noise OpenPBR, 600
+    icosphere props, 4096 emissive triangles), 2 x pinhole32 + 2 x
+    equi62_lut1d at 1920x1080 in one launch, the rig orbiting the room by
+    `degrees_per_frame` each of `frames` frames; 1 spp, depth 6, ReSTIR DI
+    (32 candidates, temporal + 1 spatial) and the U-Net denoiser when its
+    weights are present. Frame times are the frames' CUDA events."""
+    from ray_tracing_gb300 import scenes
+    from ray_tracing_gb300.renderer import Renderer
+    sc = scenes.HostScene("textured_room")
+    rig = scenes.default_rig("textured_room", 4)
+    weights = _weights()
+    prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=1 if weights is not None else 0,
+                          enable_restir_di=1, restir_initial_candidates=32, restir_temporal_reuse=1,
+                          restir_spatial_neighbors=1)
+    r = Renderer()
+    t0 = time.perf_counter()
+    r.prepare_scene(sc.view)
+    prep_ms = 1000.0 * (time.perf_counter() - t0)
+    if weights is not None:
+        r.set_denoiser(weights)
+    r.reset_sequence(SEED)
+    for _ in range(warmup):
+        r.render_frame(rig, prof, 4)
+    ms, dn, rays = [], [], 0
+    for f in range(frames):
+        v = r.render_frame(scenes.orbit_rig(rig, degrees_per_frame * f), prof, 4)
+        ms.append(v.frame_render_ms)
+        dn.append(v.cameras[0].denoise_ms)
+        rays += v.rays_traced
+    r.close()
+    rec = {"ms_per_frame": float(np.mean(ms)), "ms_p50": float(np.median(ms)), "ms_max": float(np.max(ms)),
+           "denoise_ms_per_frame": float(np.mean(dn)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
+           "prepare_ms": prep_ms, "triangles": sc.view.triangle_count, "frames": frames,
+           "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None}
+    sc.close()
+    return rec
 
 
 def cpu_baseline(sc, rig, prof):
@@ -623,7 +664,7 @@ def main():
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
     ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 workload records")
-    ap.add_argument("--workload", choices=["c1", "c3"], default=None,
+    ap.add_argument("--workload", choices=["c1", "c3", "c5"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

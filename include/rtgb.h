@@ -523,6 +523,10 @@ typedef struct rtgb_host_scene rtgb_host_scene;
  *   "restir_acceptance"  utils/render_restir_acceptance.cpp:41-93
  *   "random_spheres"     seeded 22x22 sphere field + emissive rect lights
  *   "triangle_terrain"   seeded displaced-grid terrain + icosphere instances
+ *   "triangle_terrain_pbr"  the same with constant OpenPBR materials
+ *   "openpbr_gallery"    one sphere per OpenPBR feature + analytic sphere lights
+ *   "textured_room"      4 M-triangle room, checker / noise textured OpenPBR,
+ *                        600 icosphere props, 4096 emissive triangles
  * `detail` scales the procedural scenes (light count / triangle budget);
  * 0 selects the default size. */
 rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t detail,

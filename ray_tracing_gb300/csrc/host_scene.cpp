@@ -601,6 +601,39 @@ void build_openpbr_gallery(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
     b.background({0.03, 0.035, 0.05});
 }
 
+// Unit icosphere subdivided twice: 162 vertices, 320 faces.
+void icosphere2(std::vector<Vec3>& verts, std::vector<std::array<int, 3>>& faces) {
+    verts.clear();
+    const double t = (1.0 + std::sqrt(5.0)) / 2.0;
+    const double v[12][3] = {{-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0}, {0, -1, t}, {0, 1, t},
+        {0, -1, -t}, {0, 1, -t}, {t, 0, -1}, {t, 0, 1}, {-t, 0, -1}, {-t, 0, 1}};
+    for (const auto& p : v) {
+        const double l = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+        verts.push_back({p[0] / l, p[1] / l, p[2] / l});
+    }
+    faces = {{0, 11, 5}, {0, 5, 1}, {0, 1, 7}, {0, 7, 10}, {0, 10, 11}, {1, 5, 9}, {5, 11, 4}, {11, 10, 2},
+        {10, 7, 6}, {7, 1, 8}, {3, 9, 4}, {3, 4, 2}, {3, 2, 6}, {3, 6, 8}, {3, 8, 9}, {4, 9, 5}, {2, 4, 11},
+        {6, 2, 10}, {8, 6, 7}, {9, 8, 1}};
+    for (int level = 0; level < 2; ++level) {
+        std::vector<std::array<int, 3>> next;
+        auto mid = [&](int i, int j) {
+            Vec3 m {(verts[i][0] + verts[j][0]) * 0.5, (verts[i][1] + verts[j][1]) * 0.5,
+                (verts[i][2] + verts[j][2]) * 0.5};
+            const double l = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+            verts.push_back({m[0] / l, m[1] / l, m[2] / l});
+            return static_cast<int>(verts.size()) - 1;
+        };
+        for (const auto& f : faces) {
+            const int a = mid(f[0], f[1]), bb = mid(f[1], f[2]), c = mid(f[2], f[0]);
+            next.push_back({f[0], a, c});
+            next.push_back({f[1], bb, a});
+            next.push_back({f[2], c, bb});
+            next.push_back({a, bb, c});
+        }
+        faces = next;
+    }
+}
+
 // Seeded procedural triangle scene: a displaced-grid terrain plus icosphere
 // instances, constant per-object materials, and `emissive` emissive
 // triangles (a fraction of the icosphere faces). The triangle budget is
@@ -617,36 +650,7 @@ void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail, b
     // icosphere subdivided twice: 320 faces
     std::vector<Vec3> verts;
     std::vector<std::array<int, 3>> faces;
-    {
-        const double t = (1.0 + std::sqrt(5.0)) / 2.0;
-        const double v[12][3] = {{-1, t, 0}, {1, t, 0}, {-1, -t, 0}, {1, -t, 0}, {0, -1, t}, {0, 1, t},
-            {0, -1, -t}, {0, 1, -t}, {t, 0, -1}, {t, 0, 1}, {-t, 0, -1}, {-t, 0, 1}};
-        for (const auto& p : v) {
-            const double l = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-            verts.push_back({p[0] / l, p[1] / l, p[2] / l});
-        }
-        faces = {{0, 11, 5}, {0, 5, 1}, {0, 1, 7}, {0, 7, 10}, {0, 10, 11}, {1, 5, 9}, {5, 11, 4}, {11, 10, 2},
-            {10, 7, 6}, {7, 1, 8}, {3, 9, 4}, {3, 4, 2}, {3, 2, 6}, {3, 6, 8}, {3, 8, 9}, {4, 9, 5}, {2, 4, 11},
-            {6, 2, 10}, {8, 6, 7}, {9, 8, 1}};
-        for (int level = 0; level < 2; ++level) {
-            std::vector<std::array<int, 3>> next;
-            auto mid = [&](int i, int j) {
-                Vec3 m {(verts[i][0] + verts[j][0]) * 0.5, (verts[i][1] + verts[j][1]) * 0.5,
-                    (verts[i][2] + verts[j][2]) * 0.5};
-                const double l = std::sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
-                verts.push_back({m[0] / l, m[1] / l, m[2] / l});
-                return static_cast<int>(verts.size()) - 1;
-            };
-            for (const auto& f : faces) {
-                const int a = mid(f[0], f[1]), bb = mid(f[1], f[2]), c = mid(f[2], f[0]);
-                next.push_back({f[0], a, c});
-                next.push_back({f[1], bb, a});
-                next.push_back({f[2], c, bb});
-                next.push_back({a, bb, c});
-            }
-            faces = next;
-        }
-    }
+    icosphere2(verts, faces);
     const int64_t sphere_tris = static_cast<int64_t>(instances) * static_cast<int64_t>(faces.size());
     const int64_t terrain_tris = std::max<int64_t>(2, budget - sphere_tris);
     const int n = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(terrain_tris) / 2.0)));
@@ -695,6 +699,88 @@ void build_triangle_terrain(rtgb_host_scene& s, uint32_t seed, int64_t detail, b
         }
     }
     b.background({0.05, 0.06, 0.09});
+}
+
+// The 4 M-triangle textured room: a 30 x 8 x 30 room whose floor, ceiling and
+// four walls are fine triangle grids (the floor gently undulating), textured
+// OpenPBR (a checker base colour on the floor, 3D noise on the walls), 600
+// icosphere props with constant OpenPBR materials, and 16 ceiling panels of
+// 256 emissive OpenPBR triangles each (4096). `detail` is the triangle budget
+// (default 4,000,000).
+void build_textured_room(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
+    Builder b(s);
+    SplitMix rng(0x7e4700ull ^ seed);
+    const int64_t budget = detail > 0 ? detail : 4000000;
+    const double hx = 15.0, hz = 15.0, top = 8.0;
+    auto pbr = [&](const Vec3& color, double roughness, double metalness) {
+        rtgb_openpbr_material om = openpbr_defaults();
+        for (int k = 0; k < 3; ++k) om.base_color[k] = static_cast<float>(color[k]);
+        om.specular_roughness = static_cast<float>(roughness);
+        om.base_metalness = static_cast<float>(metalness);
+        return om;
+    };
+    rtgb_openpbr_material floor_m = pbr({0.6, 0.6, 0.6}, 0.5, 0.0);
+    floor_m.color_texture[0] = b.checker_texture(1.5, b.constant_texture({0.75, 0.72, 0.66}), b.constant_texture({0.18, 0.2, 0.24}));
+    rtgb_openpbr_material wall_m = pbr({0.7, 0.7, 0.7}, 0.8, 0.0);
+    wall_m.color_texture[0] = b.noise_texture(1.3);
+    const int floor = b.openpbr(floor_m), wall = b.openpbr(wall_m), ceiling = b.openpbr(pbr({0.85, 0.85, 0.82}, 0.9, 0.0));
+    rtgb_openpbr_material lamp = pbr({0.0, 0.0, 0.0}, 0.5, 0.0);
+    lamp.emission_luminance = 12.0f;
+    lamp.emission_color[0] = 1.0f;
+    lamp.emission_color[1] = 0.92f;
+    lamp.emission_color[2] = 0.8f;
+    const int light = b.openpbr(lamp);
+
+    // a grid of cells x cells quads (two triangles each) spanning o + [0,1] u + [0,1] v
+    auto grid = [&](int m, const Vec3& o, const Vec3& u, const Vec3& v, int64_t tris, auto&& lift) {
+        const int cells = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(tris) / 2.0)));
+        auto P = [&](int i, int j) {
+            const double a = static_cast<double>(i) / cells, c = static_cast<double>(j) / cells;
+            Vec3 q {o[0] + a * u[0] + c * v[0], o[1] + a * u[1] + c * v[1], o[2] + a * u[2] + c * v[2]};
+            q[1] += lift(q[0], q[2]);
+            return q;
+        };
+        for (int j = 0; j < cells; ++j) {
+            for (int i = 0; i < cells; ++i) {
+                const Vec3 p00 = P(i, j), p10 = P(i + 1, j), p01 = P(i, j + 1), p11 = P(i + 1, j + 1);
+                b.triangle(m, p00, p01, p10);
+                b.triangle(m, p10, p01, p11);
+            }
+        }
+    };
+    const auto flat = [](double, double) { return 0.0; };
+    const auto bumps = [](double x, double z) { return 0.03 * std::sin(1.7 * x) * std::cos(1.3 * z); };
+
+    const int props = 600, panels = 16;
+    const int64_t prop_tris = static_cast<int64_t>(props) * 320, lamp_tris = static_cast<int64_t>(panels) * 256;
+    const int64_t rest = std::max<int64_t>(12, budget - prop_tris - lamp_tris);
+    grid(floor, {-hx, 0.0, -hz}, {2 * hx, 0.0, 0.0}, {0.0, 0.0, 2 * hz}, rest * 4 / 10, bumps);
+    grid(ceiling, {-hx, top, -hz}, {0.0, 0.0, 2 * hz}, {2 * hx, 0.0, 0.0}, rest * 2 / 10, flat);
+    grid(wall, {-hx, 0.0, -hz}, {0.0, top, 0.0}, {2 * hx, 0.0, 0.0}, rest / 10, flat);
+    grid(wall, {-hx, 0.0, hz}, {2 * hx, 0.0, 0.0}, {0.0, top, 0.0}, rest / 10, flat);
+    grid(wall, {-hx, 0.0, -hz}, {0.0, 0.0, 2 * hz}, {0.0, top, 0.0}, rest / 10, flat);
+    grid(wall, {hx, 0.0, -hz}, {0.0, top, 0.0}, {0.0, 0.0, 2 * hz}, rest / 10, flat);
+    // ceiling panels: 4 x 4 layout, each 8 x 16 quads just below the ceiling, facing down
+    for (int k = 0; k < panels; ++k) {
+        const double cx = -11.25 + 7.5 * (k % 4), cz = -11.25 + 7.5 * (k / 4);
+        grid(light, {cx - 1.5, top - 0.02, cz - 0.75}, {3.0, 0.0, 0.0}, {0.0, 0.0, 1.5}, 256, flat);
+    }
+    // icosphere props (the 320-face sphere of the terrain scene)
+    std::vector<Vec3> verts;
+    std::vector<std::array<int, 3>> faces;
+    icosphere2(verts, faces);
+    for (int k = 0; k < props; ++k) {
+        const double r = rng.uniform(0.2, 0.8);
+        const double cx = rng.uniform(-hx + 1.0, hx - 1.0), cz = rng.uniform(-hz + 1.0, hz - 1.0);
+        const Vec3 center {cx, bumps(cx, cz) + r * 1.02, cz};
+        const int m = b.openpbr(pbr({rng.uniform(), rng.uniform(), rng.uniform()}, rng.uniform(0.05, 1.0),
+            rng.uniform() < 0.3 ? 1.0 : 0.0));
+        for (const auto& f : faces) {
+            auto P = [&](int vi) { return Vec3 {center[0] + r * verts[vi][0], center[1] + r * verts[vi][1], center[2] + r * verts[vi][2]}; };
+            b.triangle(m, P(f[0]), P(f[1]), P(f[2]));
+        }
+    }
+    b.background({0.0, 0.0, 0.0});
 }
 
 // ---- cameras -----------------------------------------------------------------
@@ -847,6 +933,7 @@ rtgb_status rtgb_host_scene_create(const char* name, uint32_t seed, int64_t deta
     else if (n == "triangle_terrain") build_triangle_terrain(*s, seed, detail);
     else if (n == "triangle_terrain_pbr") build_triangle_terrain(*s, seed, detail, true);
     else if (n == "openpbr_gallery") build_openpbr_gallery(*s, seed, detail);
+    else if (n == "textured_room") build_textured_room(*s, seed, detail);
     else {
         delete s;
         return RTGB_INVALID_ARGUMENT;
@@ -1021,6 +1108,19 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
             const Vec3 eye {0.0, 4.0, 0.0};
             const Vec3 dir = rotate_about({0.0, -0.35, 1.0}, {0.0, 1.0, 0.0}, kYaw[i]);
             look_at(c, eye, {eye[0] + dir[0], eye[1] + dir[1], eye[2] + dir[2]}, {0.0, 1.0, 0.0});
+            rig->cameras[i] = c;
+        }
+        return RTGB_OK;
+    }
+    if (n == "textured_room") {
+        // mixed rig at 1920x1080: 2x pinhole32 (hfov 90) + 2x equi62_lut1d (180 deg),
+        // on a 9 m circle around the room centre, each looking across the room
+        for (int i = 0; i < camera_count; ++i) {
+            const bool equi = i % 2 == 1;
+            const int w = width > 0 ? width : 1920, h = height > 0 ? height : 1080;
+            rtgb_camera c = equi ? equi_camera(w, h, 180.0) : pinhole_camera(w, h, 90.0);
+            const Vec3 eye = rotate_about({0.0, 2.2, -9.0}, {0.0, 1.0, 0.0}, 90.0 * i);
+            look_at(c, eye, {0.0, 1.2 + 0.4 * (i % 2), 0.0}, {0.0, 1.0, 0.0});
             rig->cameras[i] = c;
         }
         return RTGB_OK;

@@ -64,6 +64,24 @@ def default_rig(scene_name: str, camera_count: int, width: int = 0, height: int 
     return rig
 
 
+def orbit_rig(rig: abi.CameraRig, degrees: float, center=(0.0, 0.0, 0.0)) -> abi.CameraRig:
+    """A copy of `rig` with every camera pose turned by `degrees` about the
+    vertical (+y) axis through `center`: R' = Ry R, t' = Ry (t - c) + c (the
+    pose rotation's columns are the camera axes in world space)."""
+    out = abi.CameraRig()
+    C.pointer(out)[0] = rig
+    a = np.radians(degrees)
+    ry = np.array([[np.cos(a), 0.0, np.sin(a)], [0.0, 1.0, 0.0], [-np.sin(a), 0.0, np.cos(a)]])
+    c = np.asarray(center, np.float64)
+    for i in range(rig.active_count):
+        cam = out.cameras[i]
+        r = np.array(cam.rotation[:], np.float64).reshape(3, 3)
+        t = np.array(cam.translation[:], np.float64)
+        cam.rotation[:] = (ry @ r).ravel().tolist()
+        cam.translation[:] = (ry @ (t - c) + c).tolist()
+    return out
+
+
 def profile(name: str, **overrides) -> abi.RenderProfile:
     p = abi.RenderProfile()
     abi.check(abi.load().rtgb_profile_preset(name.encode(), C.byref(p)), what=f"rtgb_profile_preset({name})")

@@ -597,7 +597,10 @@ static SceneMeshGeometry cube_mesh() {
 }
 
 // The GPU parity scene: every SceneIR v2 feature the realtime path lowers.
-static SceneIRv2 parity_scene(const std::string& image_path) {
+// `lights`: bit k keeps light k (sphere, rect, disk, tube, sun, dome); `textures`
+// binds the checker and image textures; `normals` authors the pentagon's normals.
+static SceneIRv2 parity_scene(const std::string& image_path, unsigned lights = 0x3f, bool textures = true,
+    bool normals = true) {
     SceneIRv2 s;
     s.add_prim(prim("/World"));
     s.add_prim(prim("/World/Tex"));
@@ -622,14 +625,14 @@ static SceneIRv2 parity_scene(const std::string& image_path) {
     s.add_prim(prim("/World/Looks"));
     SceneOpenPbrSurface floor, gold, glass, pic, emit, coat;
     floor.specular_roughness = 0.6;
-    floor.connections.push_back({"base_color", SceneMaterialValueType::color3, "/World/Tex/Check", SceneTextureChannel::rgb});
+    if (textures) floor.connections.push_back({"base_color", SceneMaterialValueType::color3, "/World/Tex/Check", SceneTextureChannel::rgb});
     gold.base_metalness = 1.0;
     gold.base_color = {1.0, 0.78, 0.34};
     gold.specular_roughness = 0.3;
     glass.transmission_weight = 1.0;
     glass.specular_roughness = 0.0;
     glass.base_color = {1.0, 1.0, 1.0};
-    pic.connections.push_back({"base_color", SceneMaterialValueType::color3, "/World/Tex/Img", SceneTextureChannel::rgb});
+    if (textures) pic.connections.push_back({"base_color", SceneMaterialValueType::color3, "/World/Tex/Img", SceneTextureChannel::rgb});
     emit.base_color = {0.0, 0.0, 0.0};
     emit.emission_luminance = 4.0;
     emit.emission_color = {1.0, 0.9, 0.7};
@@ -646,7 +649,9 @@ static SceneIRv2 parity_scene(const std::string& image_path) {
     s.add_prim(prim("/World/Proto"));
     {
         SceneMeshGeometry f;
-        f.points = {{-6.0, 0.0, -6.0}, {6.0, 0.0, -6.0}, {6.0, 0.0, 6.0}, {-6.0, 0.0, 6.0}};
+        // 1 cm below y = 0: the checker is the sign of sin(x) sin(y) sin(z), so on
+        // the plane y = 0 a hit's cell would hang on the last bit of its position
+        f.points = {{-6.0, -0.01, -6.0}, {6.0, -0.01, -6.0}, {6.0, -0.01, 6.0}, {-6.0, -0.01, 6.0}};
         f.face_vertex_counts = {4};
         f.face_vertex_indices = {0, 3, 2, 1};  // facing +y
         ScenePrimvar st;
@@ -680,7 +685,7 @@ static SceneIRv2 parity_scene(const std::string& image_path) {
         n.interpolation = ScenePrimvarInterpolation::vertex;
         n.values = std::vector<Vec3f> {{0.0f, 0.0f, 1.0f}, {0.2f, 0.0f, 1.0f}};
         n.indices = {0, 1, 0, 1, 0};
-        g.primvars = {n};
+        if (normals) g.primvars = {n};
         ScenePrim pg = prim("/World/Proto/Pentagon", ScenePrimKind::geometry_prototype);
         pg.geometry = SceneGeometry {g};
         s.add_prim(pg);
@@ -730,7 +735,7 @@ static SceneIRv2 parity_scene(const std::string& image_path) {
     sun.normalize = true;
     dome.intensity = 0.15;
     dome.color = {0.6, 0.7, 1.0};
-    s.add_prim(light_prim("/World/Lights/Sphere", sph, translate(2.5, 2.5, 2.0)));
+    if (lights & 1) s.add_prim(light_prim("/World/Lights/Sphere", sph, translate(2.5, 2.5, 2.0)));
     // rect / disk lights face -(basis_x x basis_y), local -z: a rotation about x
     // taking local -z onto world -y points them at the floor
     Mat4 down = kIdentity4;
@@ -742,21 +747,21 @@ static SceneIRv2 parity_scene(const std::string& image_path) {
     rect_xf[3] = -2.0;
     rect_xf[7] = 3.0;
     rect_xf[11] = 0.5;
-    s.add_prim(light_prim("/World/Lights/Rect", rect, rect_xf));
+    if (lights & 2) s.add_prim(light_prim("/World/Lights/Rect", rect, rect_xf));
     Mat4 disk_xf = down;
     disk_xf[3] = 1.0;
     disk_xf[7] = 3.2;
     disk_xf[11] = -1.5;
-    s.add_prim(light_prim("/World/Lights/Disk", disk, disk_xf));
-    s.add_prim(light_prim("/World/Lights/Tube", cyl, translate(0.0, 2.2, -1.8)));
+    if (lights & 4) s.add_prim(light_prim("/World/Lights/Disk", disk, disk_xf));
+    if (lights & 8) s.add_prim(light_prim("/World/Lights/Tube", cyl, translate(0.0, 2.2, -1.8)));
     Mat4 sun_xf = kIdentity4;  // tilt the sun about x
     const double a = 0.9;
     sun_xf[5] = std::cos(a);
     sun_xf[6] = -std::sin(a);
     sun_xf[9] = std::sin(a);
     sun_xf[10] = std::cos(a);
-    s.add_prim(light_prim("/World/Lights/Sun", sun, sun_xf));
-    s.add_prim(light_prim("/World/Lights/Dome", dome));
+    if (lights & 16) s.add_prim(light_prim("/World/Lights/Sun", sun, sun_xf));
+    if (lights & 32) s.add_prim(light_prim("/World/Lights/Dome", dome));
     return s;
 }
 
@@ -833,6 +838,19 @@ int main(int argc, char** argv) {
             CHECK(near3(v.triangles[26].p0, {0.5, -0.1, -3.5}, 1e-6), "time-sampled instance at the start time code");
             if (argc >= 4 && std::string(argv[2]) == "--write-scene") {
                 CHECK(rtgb_host_scene_save(h.get(), argv[3]) == RTGB_OK, "write the parity scene");
+            }
+            if (argc >= 4 && std::string(argv[2]) == "--write-variants") {
+                // one scene per feature, for locating a parity difference
+                const std::string img = (dir / "grid.png").string();
+                const auto save = [&](const SceneIRv2& ir, const std::string& name) {
+                    const HostScenePtr v2 = adapt_scene_ir_v2_to_realtime(ir);
+                    CHECK(rtgb_host_scene_save(v2.get(), (std::filesystem::path(argv[3]) / name).string().c_str()) == RTGB_OK,
+                        "write a variant");
+                };
+                for (unsigned k = 0; k < 6; ++k) save(parity_scene(img, 1u << k), "light" + std::to_string(k) + ".rtgbscene");
+                save(parity_scene(img, 0), "nolights.rtgbscene");
+                save(parity_scene(img, 0x3f, false), "notex.rtgbscene");
+                save(parity_scene(img, 0x3f, true, false), "nonormals.rtgbscene");
             }
         }
     } catch (const std::exception& e) {
