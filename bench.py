@@ -281,7 +281,7 @@ def gpu_frames(sc, rig, prof, cameras, warmup, frames):
     return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
 
 
-def workload_records(names=("c1", "c3"), c3_steps=10, c3_warmup=3):
+def workload_records(names=("c1", "c3", "c5"), c3_steps=10, c3_warmup=3):
     """The other configurations of the reference protocol, measured beside the
     headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
     on all host threads renders the same full frame) and C3 (1 M triangles with
@@ -335,7 +335,7 @@ def c5_record(frames=60, warmup=3, degrees_per_frame=2.0):
     prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=1 if weights is not None else 0,
                           enable_restir_di=1, restir_initial_candidates=32, restir_temporal_reuse=1,
                           restir_spatial_neighbors=1)
-    r = Renderer()
+    r = Renderer(stage_timing=True)
     t0 = time.perf_counter()
     r.prepare_scene(sc.view)
     prep_ms = 1000.0 * (time.perf_counter() - t0)
@@ -344,17 +344,26 @@ def c5_record(frames=60, warmup=3, degrees_per_frame=2.0):
     r.reset_sequence(SEED)
     for _ in range(warmup):
         r.render_frame(rig, prof, 4)
-    ms, dn, rays = [], [], 0
+    ms, dn, stages, rays = [], [], [], 0
     for f in range(frames):
         v = r.render_frame(scenes.orbit_rig(rig, degrees_per_frame * f), prof, 4)
         ms.append(v.frame_render_ms)
         dn.append(v.cameras[0].denoise_ms)
+        stages.append(r.stage_times())
         rays += v.rays_traced
     r.close()
+    # per-stage mean ms: raygen, (trace, shade, shadow) per bounce, finalize + resolve
+    st = np.mean(np.stack(stages), axis=0)
+    mb = (len(st) - 3) // 3
+    stage_ms = {"raygen": float(st[0]), "finalize+resolve": float(st[-2] + st[-1])}
+    for b in range(mb):
+        for k, name in enumerate(("trace", "shade", "shadow")):
+            stage_ms[f"{name}@{b}"] = float(st[1 + 3 * b + k])
     rec = {"ms_per_frame": float(np.mean(ms)), "ms_p50": float(np.median(ms)), "ms_max": float(np.max(ms)),
            "denoise_ms_per_frame": float(np.mean(dn)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
            "prepare_ms": prep_ms, "triangles": sc.view.triangle_count, "frames": frames,
-           "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None}
+           "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None,
+           "stage_ms": stage_ms}
     sc.close()
     return rec
 
@@ -561,11 +570,11 @@ def run_ours(args, rank, world, local_rank):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
     for _ in range(args.warmup):
         r.render_frame(rig, prof, CAMERAS)
-    # raygen, (trace, reset, shade, shadow) per bounce, the three ReSTIR passes,
-    # finalize, resolve; the denoiser: pack, 11 convolutions (pooling and
-    # upsampling fused into them at these even sizes), unpack per batch of
-    # equal-size cameras (one batch here)
-    launches_per_frame = 1 + 4 * prof.max_bounces + 3 + 2 + (13 if weights is not None else 0)
+    # raygen, (trace, reset, material bucketing x 3, shade, shadow) per bounce,
+    # the three ReSTIR passes, finalize, resolve; the denoiser: pack, 11
+    # convolutions (pooling and upsampling fused into them at these even
+    # sizes), unpack per batch of equal-size cameras (one batch here)
+    launches_per_frame = 1 + 7 * prof.max_bounces + 3 + 2 + (13 if weights is not None else 0)
 
     sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local_rank)).split(",")[0])
                            if os.environ.get("CUDA_VISIBLE_DEVICES", "").isdigit() else local_rank)

@@ -164,7 +164,7 @@ class RenderProfile(C.Structure):
 
 class CreateInfo(C.Structure):
     _fields_ = [("device", C.c_int32), ("use_cuda_graph", C.c_int32), ("debug_path_records", C.c_int32),
-                ("stage_timing", C.c_int32)]
+                ("stage_timing", C.c_int32), ("shade_order", C.c_int32)]
 
 
 class CameraFrameView(C.Structure):

@@ -548,8 +548,9 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
     const int out = in ^ 1;
     const int count = counters->active[in];
     const bool restir_bounce = fp.restir_enabled != 0 && bounce == 0;
+    const int* __restrict__ order = bounce >= fp.sort_from_bounce ? P.sorted : P.queue[in];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const int path = P.queue[in][i];
+        const int path = order[i];
         const float4 hr = P.hit[path];
         const int code = __float_as_int(hr.y);
         const int alight = __float_as_int(hr.z);

@@ -48,6 +48,10 @@ struct Paths {
     float* res_src_t;        // their bias-correction targets [path][9]
     int* res_meta;           // per path: source count, selected source + 1, canonical M
     int* vis_queue;          // (path << 4) | source of each bias-correction ray
+    int* sort_key;           // material bucket of each shade-queue slot (shade_sort.cu)
+    int* sorted;             // the shade queue in bucket order
+    int* sort_hist;          // [kSortBins] bucket sizes (zero between bounces)
+    int* sort_cursor;        // [kSortBins] bucket fill positions
 };
 
 struct Counters {
@@ -87,9 +91,12 @@ struct FrameParams {
     int restir_max_spatial;
     int restir_bias;
     int record_paths;
+    int sort_from_bounce;  // shade in material-bucket order from this bounce on (INT_MAX: never)
     FrameBufs cur;      // this frame's buffers
     FrameBufs hist;     // the previous frame's (ping-pong)
 };
+
+constexpr int kSortBins = 1024;  // material buckets of the shading order (one scan block)
 
 struct LaunchShape {
     int grid;
@@ -104,6 +111,10 @@ void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
     LaunchShape shape, cudaStream_t stream);
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream);
+// Buckets the bounce's shade queue by hit material into Paths::sorted (a no-op
+// below FrameParams::sort_from_bounce); shade_sort.cu.
+void launch_shade_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
+    cudaStream_t stream);
 void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream);
 // The three ReSTIR passes (RIS + merges, bias-correction rays, finalisation);

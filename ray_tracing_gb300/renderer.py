@@ -39,13 +39,13 @@ class CameraFrame:
 
 class Renderer:
     def __init__(self, device: int = 0, use_cuda_graph: bool = True, debug_path_records: bool = False,
-                 stage_timing: bool = False):
+                 stage_timing: bool = False, shade_order: int = 0):
         self.lib = abi.load()
         missing = getattr(self.lib, "rtgb_missing_symbols", [])
         if missing:
             raise RuntimeError(f"librtgb.so lacks {missing}: rebuild with __graft_entry__.build()")
         self.h = C.c_void_p()
-        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records), int(stage_timing))
+        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records), int(stage_timing), int(shade_order))
         st = self.lib.rtgb_create(C.byref(info), C.byref(self.h))
         if st != abi.OK:
             raise abi.RtgbError(st, "rtgb_create failed (no CUDA device?)")
