@@ -310,8 +310,10 @@ typedef struct rtgb_create_info {
     int32_t use_cuda_graph;    /* capture each frame's launch sequence as a CUDA graph */
     int32_t debug_path_records;/* record per-path hit codes and radiance (parity tests) */
     int32_t stage_timing;      /* record CUDA events between the frame's launches (rtgb_stage_times) */
-    int32_t shade_order;       /* shade each bounce's paths bucketed by hit material: 0 (default) and 2
-                                  from bounce 0, 1 from bounce 1, -1 never; results do not depend on it */
+    int32_t shade_order;       /* shade each bounce's paths bucketed by hit material: 0 automatic (from
+                                  bounce 0 when the scene has OpenPBR materials or more than 8
+                                  materials), 2 always from bounce 0, 1 from bounce 1, -1 never;
+                                  results do not depend on it */
 } rtgb_create_info;
 
 /* DeviceRadianceFrameView (src/realtime/gpu/device_radiance_frame_view.h) plus

@@ -1066,9 +1066,12 @@ struct rtgb_renderer {
         fp.restir_bias = profile.restir_bias_correction;
         fp.record_paths = record ? 1 : 0;
         // material-bucketed shading (shade_sort.cu) keeps a warp's paths on one
-        // material's branches; measured faster on every scene tried, most where
-        // OpenPBR parameters vary per material, so it is on by default
-        fp.sort_from_bounce = shade_order < 0 ? INT_MAX : (shade_order == 1 ? 1 : 0);
+        // material's branches. Automatic: on where there is divergence to remove
+        // (OpenPBR materials, or more than kBucketMaterials materials); a scene of
+        // a handful of materials (the Cornell box) only pays the three launches.
+        const bool bucket = shade_order > 0 ||
+            (shade_order == 0 && (scene.openpbr_count > 0 || scene.material_count > kBucketMaterials));
+        fp.sort_from_bounce = !bucket ? INT_MAX : (shade_order == 1 ? 1 : 0);
         fp.cur = frames[cur];
         fp.hist = frames[cur ^ 1];
         // Pageable source: the copy is staged before the call returns, so the

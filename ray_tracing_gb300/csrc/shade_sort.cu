@@ -58,10 +58,14 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_count(const FrameParams* 
     const int in = bounce & 1;
     int begin, end;
     chunk_of(counters->active[in], begin, end);
+    const int lane = static_cast<int>(threadIdx.x) & 31;
     for (int i = begin + static_cast<int>(threadIdx.x); i < end; i += blockDim.x) {
         const int key = shade_key(s, P.hit[P.queue[in][i]]);
         P.sort_key[i] = key;
-        atomicAdd(&bins[key], 1);
+        // one shared atomic per distinct key in the warp (few materials would
+        // otherwise serialise 32 lanes on one address)
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&bins[key], __popc(peers));
     }
     __syncthreads();
     for (int b = threadIdx.x; b < kSortBins; b += blockDim.x) {
@@ -107,7 +111,12 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_scatter(const FrameParams
     const int in = bounce & 1;
     int begin, end;
     chunk_of(counters->active[in], begin, end);
-    for (int i = begin + static_cast<int>(threadIdx.x); i < end; i += blockDim.x) atomicAdd(&bins[P.sort_key[i]], 1);
+    const int lane = static_cast<int>(threadIdx.x) & 31;
+    for (int i = begin + static_cast<int>(threadIdx.x); i < end; i += blockDim.x) {
+        const int key = P.sort_key[i];
+        const unsigned peers = __match_any_sync(__activemask(), key);
+        if (lane == __ffs(peers) - 1) atomicAdd(&bins[key], __popc(peers));
+    }
     __syncthreads();
     for (int b = threadIdx.x; b < kSortBins; b += blockDim.x) {
         base[b] = bins[b] != 0 ? atomicAdd(&P.sort_cursor[b], bins[b]) : 0;
@@ -116,7 +125,14 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_scatter(const FrameParams
     __syncthreads();
     for (int i = begin + static_cast<int>(threadIdx.x); i < end; i += blockDim.x) {
         const int key = P.sort_key[i];
-        P.sorted[base[key] + atomicAdd(&bins[key], 1)] = P.queue[in][i];
+        const unsigned act = __activemask();
+        const unsigned peers = __match_any_sync(act, key);
+        const int leader = __ffs(peers) - 1;
+        int start = 0;
+        if (lane == leader) start = atomicAdd(&bins[key], __popc(peers));
+        start = __shfl_sync(act, start, leader);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        P.sorted[base[key] + start + rank] = P.queue[in][i];
     }
 }
 

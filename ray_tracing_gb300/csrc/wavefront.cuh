@@ -97,6 +97,7 @@ struct FrameParams {
 };
 
 constexpr int kSortBins = 1024;  // material buckets of the shading order (one scan block)
+constexpr int kBucketMaterials = 8;  // automatic bucketing needs more materials than this (or OpenPBR)
 
 struct LaunchShape {
     int grid;
