@@ -4,7 +4,7 @@
 // (src/realtime/gpu/device_math.h:20-88), its RNG (src/realtime/gpu/programs.cu:104-137)
 // and the shared light / reservoir helpers (src/common/light_sampling.h:64-124,
 // src/common/restir_di.h:58-199). Only tests/, __graft_entry__.smoke() and
-// bench.py's cpu_baseline / reference legs use it, as the checker.
+// bench.py's cpu_baseline / reference legs use it, as the oracle.
 //
 // Build with -ffp-contract=off so every a*b+c rounds twice, as the CUDA
 // product does under --fmad=false.

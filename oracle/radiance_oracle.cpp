@@ -5,7 +5,7 @@
 // resolve_reprojection_kernel :1955-2067 and every helper they call), driven
 // the way src/realtime/gpu/optix_renderer.cpp:230-277 drives it (frame buffers
 // zeroed per launch, history captured and copied after the resolve pass).
-// It is the checker of the CUDA path: only tests/, __graft_entry__.smoke()
+// It is the oracle of the CUDA path: only tests/, __graft_entry__.smoke()
 // and bench.py's cpu_baseline / --impl reference legs load it.
 //
 // Intersection runs either brute force (programs.cu:1664-1710, the
