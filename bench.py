@@ -565,6 +565,9 @@ def run_ours(args, rank, world, local_rank):
     weights = _weights() if prof.enable_denoise else None
     if weights is not None:
         r.set_denoiser(weights)
+    # launch shapes picked by the library's autotuner for this scene and rig
+    # (tuning frames are discarded; results do not depend on the grids)
+    tuning = None if args.no_autotune else r.autotune_launches(rig, prof, CAMERAS, frames=4)
     r.reset_sequence(SEED)
     stream = torch.cuda.ExternalStream(r.stream_ptr())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
@@ -650,6 +653,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "gpu_launches": launches_per_frame * args.steps,
         "denoiser": denoiser_record(denoise_ms) if weights is not None else None,
+        "launch_tuning": tuning,
     }
     if world == 1 and not args.no_training:
         line["training"] = training_record()
@@ -672,7 +676,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
-    ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 workload records")
+    ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 / C5 workload records")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
     ap.add_argument("--workload", choices=["c1", "c3", "c5"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()

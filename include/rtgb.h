@@ -423,6 +423,27 @@ rtgb_status rtgb_frame_stats(rtgb_handle handle, rtgb_frame_views* out_views);
  * rtgb_create_info::stage_timing. */
 rtgb_status rtgb_stage_times(rtgb_handle handle, float* out_ms, int32_t capacity, int32_t* out_count);
 
+/* Launch-shape autotuner (no reference counterpart; the reference leaves
+ * launch shapes to OptiX). Renders `frames` (1..64) frames of this rig and
+ * profile with the wavefront grids at each of RTGB_TUNE_CANDIDATES scales of
+ * the persistent size (0.5, 1, 2, 4 x SMs x resident blocks), times every
+ * stage with events, and keeps per stage group (raygen, trace, shade with
+ * ReSTIR and material bucketing, shadow, finalize + resolve) the fastest
+ * scale for the handle's later frames. Results never depend on the grids
+ * (the kernels loop grid-stride over their queues). The tuning frames are
+ * discarded: accumulation and history restart. Call after prepare_scene. */
+#define RTGB_TUNE_CANDIDATES 4
+#define RTGB_TUNE_GROUPS 5
+typedef struct rtgb_launch_tuning {
+    float scales[RTGB_TUNE_CANDIDATES];                   /* grid scales tried */
+    float group_ms[RTGB_TUNE_CANDIDATES][RTGB_TUNE_GROUPS];/* per frame: raygen, trace, shade, shadow, finalize+resolve */
+    float frame_ms[RTGB_TUNE_CANDIDATES];                 /* whole frame at each scale */
+    int32_t chosen[RTGB_TUNE_GROUPS];                     /* index into scales, per group */
+    float tuned_frame_ms;                                 /* whole frame with the chosen shapes */
+} rtgb_launch_tuning;
+rtgb_status rtgb_autotune_launches(rtgb_handle handle, const rtgb_camera_rig* rig,
+    const rtgb_render_profile* profile, int32_t active_cameras, int32_t frames, rtgb_launch_tuning* out);
+
 /* Rays traced since the scene was prepared: primary, extension, shadow and
  * ReSTIR visibility (waits for the stream). */
 rtgb_status rtgb_ray_totals(rtgb_handle handle, uint64_t totals[4]);

@@ -184,6 +184,17 @@ class FrameViews(C.Structure):
                 ("shadow_per_bounce", C.c_uint64 * 64)]
 
 
+TUNE_CANDIDATES = 4
+TUNE_GROUPS = 5
+TUNE_GROUP_NAMES = ("raygen", "trace", "shade", "shadow", "finalize+resolve")
+
+
+class LaunchTuning(C.Structure):
+    _fields_ = [("scales", C.c_float * TUNE_CANDIDATES), ("group_ms", (C.c_float * TUNE_GROUPS) * TUNE_CANDIDATES),
+                ("frame_ms", C.c_float * TUNE_CANDIDATES), ("chosen", C.c_int32 * TUNE_GROUPS),
+                ("tuned_frame_ms", C.c_float)]
+
+
 class RestirDiagnostics(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("pixel_count", "active_reservoir_count", "temporal_reuse_count",
                                          "spatial_reuse_count", "bias_corrected_count", "max_candidate_count",
@@ -252,6 +263,8 @@ SIGNATURES = {
     "rtgb_host_scene_create": (C.c_int, [C.c_char_p, C.c_uint32, C.c_int64, P(C.c_void_p)]),
     "rtgb_host_scene_destroy": (None, [C.c_void_p]),
     "rtgb_host_scene_view": (C.c_int, [C.c_void_p, P(Scene)]),
+    "rtgb_autotune_launches": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32, C.c_int32,
+                                         P(LaunchTuning)]),
     "rtgb_host_scene_save": (C.c_int, [C.c_void_p, C.c_char_p]),
     "rtgb_host_scene_load": (C.c_int, [C.c_char_p, P(C.c_void_p)]),
     "rtgb_host_scene_from_view": (C.c_int, [P(Scene), P(C.c_void_p)]),

@@ -1336,6 +1336,90 @@ rtgb_status rtgb_stage_times(rtgb_handle h, float* out, int32_t capacity, int32_
     });
 }
 
+// Launch-shape autotuner: the wavefront kernels loop grid-stride over the
+// bounce's queue, so any grid size is correct; which one is fastest depends on
+// the scene and the rig (tail balance against per-block setup such as the BVH
+// node staging of k_trace / k_shadow). Each candidate scale of the persistent
+// grids (SMs x resident blocks) is rendered for `frames` frames with stage
+// events; per stage group the fastest scale wins. The frames rendered while
+// tuning are discarded: accumulation and history restart afterwards.
+rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, const rtgb_render_profile* profile,
+    int32_t active, int32_t frames, rtgb_launch_tuning* out) {
+    if (!h || !rig || !profile || !out || frames < 1 || frames > 64) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        constexpr int kCandidates = RTGB_TUNE_CANDIDATES;
+        constexpr float kScales[kCandidates] = {0.5f, 1.0f, 2.0f, 4.0f};
+        // shape slots of each stage group (rtgb_launch_tuning::group_ms order)
+        static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1}, {2, 6, 7, 8, 9, 10, 11, 12}, {3}, {4, 5}};
+        *out = rtgb_launch_tuning {};
+        LaunchShape base[kLaunchShapes];
+        query_launch_shapes(h->sm_count, base);
+        const bool had_timing = h->stage_timing;
+        h->stage_timing = true;
+        auto apply = [&](const float* scale_of_group) {
+            for (int g = 0; g < RTGB_TUNE_GROUPS; ++g) {
+                for (int slot : kGroups[g]) {
+                    h->shapes[slot] = base[slot];
+                    h->shapes[slot].grid = std::max(1, static_cast<int>(static_cast<float>(base[slot].grid) * scale_of_group[g]));
+                }
+            }
+            h->drop_graph();
+        };
+        rtgb_frame_views views {};
+        std::vector<float> st(256);
+        for (int c = 0; c < kCandidates; ++c) {
+            float scale[RTGB_TUNE_GROUPS];
+            for (float& x : scale) x = kScales[c];
+            apply(scale);
+            out->scales[c] = kScales[c];
+            if (const int st0 = h->render(*rig, *profile, active, true, &views); st0 != RTGB_OK) return static_cast<rtgb_status>(st0);  // warm
+            double frame = 0.0;
+            for (int f = 0; f < frames; ++f) {
+                if (const int st1 = h->render(*rig, *profile, active, true, &views); st1 != RTGB_OK) return static_cast<rtgb_status>(st1);
+                frame += views.frame_render_ms;
+                RTGB_CHECK(cudaStreamSynchronize(h->stream));
+                const int n = h->stage_count;
+                for (int i = 0; i < n && i < 256; ++i) {
+                    RTGB_CHECK(cudaEventElapsedTime(&st[static_cast<size_t>(i)], h->stage_events[static_cast<size_t>(i)],
+                        h->stage_events[static_cast<size_t>(i + 1)]));
+                }
+                // stage order: raygen, (trace, shade, shadow) per bounce, finalize, resolve
+                const int mb = (n - 3) / 3;
+                float* g = out->group_ms[c];
+                g[0] += st[0] / static_cast<float>(frames);
+                for (int b = 0; b < mb; ++b) {
+                    g[1] += st[static_cast<size_t>(1 + 3 * b)] / static_cast<float>(frames);
+                    g[2] += st[static_cast<size_t>(2 + 3 * b)] / static_cast<float>(frames);
+                    g[3] += st[static_cast<size_t>(3 + 3 * b)] / static_cast<float>(frames);
+                }
+                g[4] += (st[static_cast<size_t>(n - 2)] + st[static_cast<size_t>(n - 1)]) / static_cast<float>(frames);
+            }
+            out->frame_ms[c] = static_cast<float>(frame / frames);
+        }
+        float best[RTGB_TUNE_GROUPS];
+        for (int g = 0; g < RTGB_TUNE_GROUPS; ++g) {
+            int pick = 1;  // the persistent grid unless another is faster
+            for (int c = 0; c < kCandidates; ++c) {
+                if (out->group_ms[c][g] < out->group_ms[pick][g]) pick = c;
+            }
+            out->chosen[g] = pick;
+            best[g] = kScales[pick];
+        }
+        apply(best);
+        if (const int st2 = h->render(*rig, *profile, active, true, &views); st2 != RTGB_OK) return static_cast<rtgb_status>(st2);
+        double tuned = 0.0;
+        for (int f = 0; f < frames; ++f) {
+            if (const int st3 = h->render(*rig, *profile, active, true, &views); st3 != RTGB_OK) return static_cast<rtgb_status>(st3);
+            tuned += views.frame_render_ms;
+        }
+        out->tuned_frame_ms = static_cast<float>(tuned / frames);
+        h->stage_timing = had_timing;
+        h->drop_graph();
+        h->reset_accumulation();
+        return RTGB_OK;
+    });
+}
+
 rtgb_status rtgb_ray_totals(rtgb_handle h, uint64_t totals[4]) {
     if (!h || !totals) return RTGB_INVALID_ARGUMENT;
     return guarded(h, [&] {

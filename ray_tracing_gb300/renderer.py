@@ -105,6 +105,21 @@ class Renderer:
         self._check(self.lib.rtgb_stage_times(self.h, buf, 256, C.byref(n)), "stage_times")
         return np.array(buf[: n.value], dtype=np.float64)
 
+    def autotune_launches(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int,
+                          frames: int = 4) -> dict:
+        """rtgb_autotune_launches: picks the fastest grid scale per stage group
+        for this rig and profile; returns the measured table and the choice."""
+        t = abi.LaunchTuning()
+        self._check(self.lib.rtgb_autotune_launches(self.h, C.byref(rig), C.byref(profile), active, frames,
+                                                    C.byref(t)), "autotune_launches")
+        scales = list(t.scales)
+        return {"scales": scales,
+                "group_ms": {abi.TUNE_GROUP_NAMES[g]: [round(t.group_ms[c][g], 4) for c in range(abi.TUNE_CANDIDATES)]
+                             for g in range(abi.TUNE_GROUPS)},
+                "frame_ms": [round(x, 4) for x in t.frame_ms],
+                "chosen": {abi.TUNE_GROUP_NAMES[g]: scales[t.chosen[g]] for g in range(abi.TUNE_GROUPS)},
+                "tuned_frame_ms": round(t.tuned_frame_ms, 4)}
+
     def stream_ptr(self) -> int:
         return int(self.lib.rtgb_stream(self.h) or 0)
 
