@@ -731,22 +731,26 @@ void build_textured_room(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
     lamp.emission_color[2] = 0.8f;
     const int light = b.openpbr(lamp);
 
-    // a grid of cells x cells quads (two triangles each) spanning o + [0,1] u + [0,1] v
-    auto grid = [&](int m, const Vec3& o, const Vec3& u, const Vec3& v, int64_t tris, auto&& lift) {
-        const int cells = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(tris) / 2.0)));
+    // a grid of cu x cv quads (two triangles each) spanning o + [0,1] u + [0,1] v
+    auto grid_cells = [&](int m, const Vec3& o, const Vec3& u, const Vec3& v, int cu, int cv, auto&& lift) {
         auto P = [&](int i, int j) {
-            const double a = static_cast<double>(i) / cells, c = static_cast<double>(j) / cells;
+            const double a = static_cast<double>(i) / cu, c = static_cast<double>(j) / cv;
             Vec3 q {o[0] + a * u[0] + c * v[0], o[1] + a * u[1] + c * v[1], o[2] + a * u[2] + c * v[2]};
             q[1] += lift(q[0], q[2]);
             return q;
         };
-        for (int j = 0; j < cells; ++j) {
-            for (int i = 0; i < cells; ++i) {
+        for (int j = 0; j < cv; ++j) {
+            for (int i = 0; i < cu; ++i) {
                 const Vec3 p00 = P(i, j), p10 = P(i + 1, j), p01 = P(i, j + 1), p11 = P(i + 1, j + 1);
                 b.triangle(m, p00, p01, p10);
                 b.triangle(m, p10, p01, p11);
             }
         }
+    };
+    // a square grid of about `tris` triangles
+    auto grid = [&](int m, const Vec3& o, const Vec3& u, const Vec3& v, int64_t tris, auto&& lift) {
+        const int cells = std::max(1, static_cast<int>(std::sqrt(static_cast<double>(tris) / 2.0)));
+        grid_cells(m, o, u, v, cells, cells, lift);
     };
     const auto flat = [](double, double) { return 0.0; };
     const auto bumps = [](double x, double z) { return 0.03 * std::sin(1.7 * x) * std::cos(1.3 * z); };
@@ -763,7 +767,7 @@ void build_textured_room(rtgb_host_scene& s, uint32_t seed, int64_t detail) {
     // ceiling panels: 4 x 4 layout, each 8 x 16 quads just below the ceiling, facing down
     for (int k = 0; k < panels; ++k) {
         const double cx = -11.25 + 7.5 * (k % 4), cz = -11.25 + 7.5 * (k / 4);
-        grid(light, {cx - 1.5, top - 0.02, cz - 0.75}, {3.0, 0.0, 0.0}, {0.0, 0.0, 1.5}, 256, flat);
+        grid_cells(light, {cx - 1.5, top - 0.02, cz - 0.75}, {3.0, 0.0, 0.0}, {0.0, 0.0, 1.5}, 16, 8, flat);
     }
     // icosphere props (the 320-face sphere of the terrain scene)
     std::vector<Vec3> verts;
