@@ -10,7 +10,9 @@
 //
 // Extra flags: --width/--height (default 640 x 480, the reference's fixed
 // size), --denoiser-weights (default: the weights shipped beside the
-// library), --device, --write-exr.
+// library), --device, --write-exr, --scene-file (a scene file from
+// rtgb_host_scene_save, e.g. lowered from SceneIR v2; the rig then comes
+// from --scene when given, else four yawed pinholes at the origin).
 #include <sys/utsname.h>
 
 #include <chrono>
@@ -65,6 +67,8 @@ struct Args {
     unsigned long seed = 0;
     std::string output_dir = "build/realtime-smoke";
     std::string scene = "smoke";
+    bool scene_given = false;
+    std::string scene_file;  // a packed scene written by rtgb_host_scene_save (e.g. lowered from SceneIR v2)
     std::string profile;
     bool skip_image_write = false;
     bool write_exr = false;
@@ -79,7 +83,7 @@ void usage(FILE* out) {
         "usage: render_realtime [--camera-count N] [--frames N] [--warmup-frames N] [--seed S]\n"
         "                       [--output-dir DIR] [--scene NAME] [--profile quality|balanced|realtime]\n"
         "                       [--skip-image-write] [--width W] [--height H] [--device D]\n"
-        "                       [--denoiser-weights FILE] [--write-exr]");
+        "                       [--denoiser-weights FILE] [--write-exr] [--scene-file FILE]");
 }
 
 template <class T>
@@ -114,7 +118,7 @@ std::optional<Args> parse(int argc, char** argv) {
             std::exit(EXIT_SUCCESS);
         } else if (k != "--camera-count" && k != "--frames" && k != "--warmup-frames" && k != "--seed" &&
                    k != "--output-dir" && k != "--scene" && k != "--profile" && k != "--width" && k != "--height" &&
-                   k != "--device" && k != "--denoiser-weights") {
+                   k != "--device" && k != "--denoiser-weights" && k != "--scene-file") {
             println(stderr, "unknown argument: {}", k);
             return std::nullopt;
         } else if (!(v = value())) {
@@ -132,6 +136,9 @@ std::optional<Args> parse(int argc, char** argv) {
             a.output_dir = *v;
         } else if (k == "--scene") {
             a.scene = *v;
+            a.scene_given = true;
+        } else if (k == "--scene-file") {
+            a.scene_file = *v;
         } else if (k == "--profile") {
             a.profile = *v;
         } else if (k == "--width") {
@@ -212,13 +219,21 @@ int run(const Args& a) {
         return EXIT_FAILURE;
     }
     rtgb_host_scene* scene = nullptr;
-    if (rtgb_host_scene_create(a.scene.c_str(), 0, 0, &scene) != RTGB_OK) {
+    std::string rig_name = a.scene;
+    if (!a.scene_file.empty()) {
+        // the scene's content from the file; --scene (if given) still names the camera rig
+        if (rtgb_host_scene_load(a.scene_file.c_str(), &scene) != RTGB_OK) {
+            println(stderr, "--scene-file must name a readable scene file: {}", a.scene_file);
+            return EXIT_FAILURE;
+        }
+        if (!a.scene_given) rig_name = "scene_file";
+    } else if (rtgb_host_scene_create(a.scene.c_str(), 0, 0, &scene) != RTGB_OK) {
         println(stderr, "--scene must reference a registered realtime scene");
         return EXIT_FAILURE;
     }
     rtgb_camera_rig rig{};
-    if (rtgb_default_rig(a.scene.c_str(), a.camera_count, a.width, a.height, &rig) != RTGB_OK) {
-        println(stderr, "no camera rig for scene {}", a.scene);
+    if (rtgb_default_rig(rig_name.c_str(), a.camera_count, a.width, a.height, &rig) != RTGB_OK) {
+        println(stderr, "no camera rig for scene {}", rig_name);
         rtgb_host_scene_destroy(scene);
         return EXIT_FAILURE;
     }
@@ -267,7 +282,7 @@ int run(const Args& a) {
         check(rtgb_device_info_get(h, &dev), h, "rtgb_device_info_get");
         report.gpu_memory.prepared_used_bytes = dev.used_bytes;
         uint64_t peak = std::max(baseline_used, dev.used_bytes);
-        report.scene = a.scene;
+        report.scene = a.scene_file.empty() ? a.scene : std::filesystem::path(a.scene_file).stem().string();
         report.profile = profile_name;
         report.camera_count = a.camera_count;
         report.width = a.width;

@@ -59,6 +59,7 @@ def cli():
     (["--profile", "fast"], "--profile must be one of"),
     (["--scene", "no_such_scene"], "--scene must reference a registered realtime scene"),
     (["--bogus"], "unknown argument"),
+    (["--scene-file", "no_such_file.rtgbscene"], "--scene-file must name a readable scene file"),
 ])
 def test_argument_validation(cli, tmp_path, args, message):
     res = subprocess.run([str(cli), "--output-dir", str(tmp_path), *args], capture_output=True, text=True, timeout=60)

@@ -10,10 +10,12 @@ visibility and purpose, winding, normals, spheres, the scene file), then
 writes a parity scene lowered from SceneIR v2 to a scene file.
 GPU: that scene (meshes, n-gons, instances, subsets, checker / image /
 constant textures on OpenPBR inputs, all six analytic light types) renders
-through the wavefront path and matches the oracle along identical paths.
+through the wavefront path and matches the oracle along identical paths, and
+render_realtime renders it from the scene file into its usual artifacts.
 """
 from __future__ import annotations
 
+import json
 import subprocess
 from pathlib import Path
 
@@ -82,3 +84,19 @@ def test_scene_ir_v2_parity_scene_matches_oracle(parity_scene_file):
         assert diverged <= 2e-3, f"camera {cam}: {diverged:.2e} of paths diverged"
         assert bad == 0, f"camera {cam}: {bad} identical paths over 1e-4 relative (max {max_err:.2e})"
         assert float(np.mean(gr)) > 0.0
+
+
+@pytest.mark.gpu
+def test_render_realtime_renders_the_scene_file(parity_scene_file, tmp_path):
+    if not _build.CLI.exists():
+        _build.build_all()
+    res = subprocess.run([str(_build.CLI), "--scene-file", str(parity_scene_file), "--camera-count", "2", "--frames", "2",
+                          "--warmup-frames", "1", "--width", "96", "--height", "72", "--output-dir", str(tmp_path)],
+                         capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr
+    summary = json.loads((tmp_path / "benchmark_summary.json").read_text())
+    assert summary["metadata"]["camera_count"] == 2 and summary["extensions"]["rays_traced"] > 0
+    assert all(r["average_luminance"] > 0.0 for r in summary["per-camera"])
+    for f in range(2):
+        for c in range(2):
+            assert (tmp_path / f"frame_{f:04d}_cam_{c}.png").stat().st_size > 0
