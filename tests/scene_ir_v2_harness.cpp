@@ -649,8 +649,8 @@ static SceneIRv2 parity_scene(const std::string& image_path, unsigned lights = 0
     s.add_prim(prim("/World/Proto"));
     {
         SceneMeshGeometry f;
-        // 1 cm below y = 0: the checker is the sign of sin(x) sin(y) sin(z), so on
-        // the plane y = 0 a hit's cell would hang on the last bit of its position
+        // 1 cm below y = 0: the checker's cells are floor(p / scale) per axis, so
+        // on the plane y = 0 a hit's cell would hang on the last bit of its position
         f.points = {{-6.0, -0.01, -6.0}, {6.0, -0.01, -6.0}, {6.0, -0.01, 6.0}, {-6.0, -0.01, 6.0}};
         f.face_vertex_counts = {4};
         f.face_vertex_indices = {0, 3, 2, 1};  // facing +y
