@@ -5,6 +5,7 @@
 #pragma once
 
 #include <array>
+#include <string>
 #include <vector>
 
 #include "rtgb.h"
@@ -21,3 +22,9 @@ struct rtgb_host_scene {
     std::vector<rtgb_openpbr_material> openpbr;
     std::array<float, 3> background {0.0f, 0.0f, 0.0f};
 };
+
+namespace rtgb::scene::detail {
+// An 8-bit PNG's texels appended to `texels` as RGB floats scaled by 1/255
+// (scene_ir_adapter.cpp); false when no readable file is found.
+bool load_png_texels(const std::string& path, int& width, int& height, std::vector<float>& texels);
+}  // namespace rtgb::scene::detail

@@ -377,7 +377,7 @@ rtgb_openpbr_material compile_openpbr_core_material(const SceneOpenPbrSurface& m
     return out;
 }
 
-namespace {
+namespace detail {
 
 // Reads an 8-bit PNG as RGB floats v * float(1/255) (OpenCV's imread +
 // convertTo(CV_32FC3, 1/255) of the reference), trying the path and then
@@ -401,6 +401,10 @@ bool load_png_texels(const std::string& path, int& width, int& height, std::vect
     }
     return false;
 }
+
+}  // namespace detail
+
+namespace {
 
 rtgb_texture default_texture() {
     rtgb_texture t {};
@@ -448,7 +452,7 @@ rtgb_texture adapt_texture(const ScenePrim& prim, const std::unordered_map<std::
             p.image_offset = static_cast<int32_t>(out.texels.size() / 3);
             const std::string path = image_path(prim);
             int w = 0, h = 0;
-            if (opt.load_images && load_png_texels(path, w, h, out.texels)) {
+            if (opt.load_images && detail::load_png_texels(path, w, h, out.texels)) {
                 p.image_width = w;
                 p.image_height = h;
             }

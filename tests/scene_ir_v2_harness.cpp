@@ -1,4 +1,5 @@
-// Self-checking C++ cases of the SceneIR v2 layer (include/rtgb_scene_ir_v2.hpp),
+// Self-checking C++ cases of the SceneIR v2 layer (include/rtgb_scene_ir_v2.hpp)
+// and of the SceneIR v1 compatibility adapter (include/rtgb_scene_ir.hpp),
 // linked against librtgb.so; run by tests/test_scene_ir_v2.py.
 //
 // The reference's own expectations come first: tests/test_realtime_scene_adapter.cpp:43-131
@@ -24,6 +25,7 @@
 #include <vector>
 
 #include "cli/png_writer.h"
+#include "rtgb_scene_ir.hpp"
 #include "rtgb_scene_ir_v2.hpp"
 
 using namespace rtgb::scene;
@@ -800,6 +802,81 @@ static void file_case(const std::filesystem::path& dir) {
     }
 }
 
+// SceneIR v1: tests/test_realtime_scene_adapter.cpp:9-30 (one triangle), then
+// the Cornell box of shared_scene_builders.cpp:101-139 built through the IR,
+// which must pack to the builtin "cornell_box" scene's arrays byte for byte.
+static void scene_ir_v1_case() {
+    SceneIR tri;
+    const int white = tri.add_texture(ConstantColorTextureDesc {{1.0, 1.0, 1.0}});
+    const int matte = tri.add_material(DiffuseMaterial {white});
+    const int mesh = tri.add_shape(TriangleMeshShape {{{0.0, 0.0, 0.0}, {1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}}, {{0, 1, 2}}, {}, {}, {}, {}, {}, {}});
+    tri.add_instance(SurfaceInstance {mesh, matte, Transform::identity()});
+    CHECK(view_of(adapt_to_realtime(tri)).triangle_count == 1, "realtime adapter emits triangle primitive");
+
+    SceneIR c;
+    auto diffuse = [&](const Vec3& col) { return c.add_material(DiffuseMaterial {c.add_texture(ConstantColorTextureDesc {col})}); };
+    const int red = diffuse({0.65, 0.05, 0.05}), whitem = diffuse({0.73, 0.73, 0.73}), green = diffuse({0.12, 0.45, 0.15});
+    const int light = c.add_material(EmissiveMaterial {c.add_texture(ConstantColorTextureDesc {{15.0, 15.0, 15.0}})});
+    auto quad = [&](int m, const Vec3& o, const Vec3& u, const Vec3& v) {
+        c.add_instance(SurfaceInstance {c.add_shape(QuadShape {o, u, v}), m, Transform::identity()});
+    };
+    quad(green, {555, 0, 0}, {0, 555, 0}, {0, 0, 555});
+    quad(red, {0, 0, 0}, {0, 555, 0}, {0, 0, 555});
+    quad(light, {343, 554, 332}, {-130, 0, 0}, {0, 0, -105});
+    quad(whitem, {0, 0, 0}, {555, 0, 0}, {0, 0, 555});
+    quad(whitem, {555, 555, 555}, {-555, 0, 0}, {0, 0, -555});
+    quad(whitem, {0, 0, 555}, {555, 0, 0}, {0, 555, 0});
+    auto box = [&](const Vec3& mx, const Vec3& t, double deg) {
+        const double a = deg * std::numbers::pi / 180.0, co = std::cos(a), si = std::sin(a);
+        Transform xf;
+        xf.translation = t;
+        xf.rotation = {co, 0.0, si, 0.0, 1.0, 0.0, -si, 0.0, co};
+        c.add_instance(SurfaceInstance {c.add_shape(BoxShape {{0, 0, 0}, mx}), whitem, xf});
+    };
+    box({165, 330, 165}, {265, 0, 295}, 15.0);
+    box({165, 165, 165}, {130, 0, 65}, -18.0);
+    const HostScenePtr ir = adapt_to_realtime(c);
+    rtgb_host_scene* raw = nullptr;
+    CHECK(rtgb_host_scene_create("cornell_box", 0, 0, &raw) == RTGB_OK, "builtin cornell_box");
+    const HostScenePtr builtin(raw);
+    const rtgb_scene a = view_of(ir), b = view_of(builtin);
+    const auto same = [](const void* x, const void* y, size_t n) { return n == 0 || std::memcmp(x, y, n) == 0; };
+    CHECK(a.quad_count == 18 && a.quad_count == b.quad_count &&
+              same(a.quads, b.quads, sizeof(rtgb_quad) * static_cast<size_t>(a.quad_count)),
+        "Cornell quads through SceneIR v1 = the builtin scene's");
+    CHECK(a.material_count == b.material_count && same(a.materials, b.materials, sizeof(rtgb_material) * 4) &&
+              a.texture_count == b.texture_count && same(a.textures, b.textures, sizeof(rtgb_texture) * 4),
+        "Cornell materials and textures through SceneIR v1 = the builtin scene's");
+
+    // media: a box of fog with an isotropic material; rows are world -> local
+    SceneIR fog;
+    const int t0 = fog.add_texture(ConstantColorTextureDesc {{1.0, 1.0, 1.0}});
+    const int iso = fog.add_material(IsotropicVolumeMaterial {t0});
+    const int diff = fog.add_material(DiffuseMaterial {t0});
+    const int cube = fog.add_shape(BoxShape {{-1, -1, -1}, {1, 1, 1}});
+    fog.add_instance(SurfaceInstance {fog.add_shape(SphereShape {{0, 0, 0}, 0.5}), diff, Transform::identity()});
+    Transform spin;
+    spin.rotation = {0.0, -1.0, 0.0, 1.0, 0.0, 0.0, 0.0, 0.0, 1.0};  // +90 deg about z
+    spin.translation = {3.0, 0.0, 0.0};
+    fog.add_medium(MediumInstance {cube, iso, 0.25, spin});
+    const HostScenePtr f = adapt_to_realtime(fog);
+    const rtgb_scene fv = view_of(f);
+    CHECK(fv.medium_count == 1 && fv.media[0].boundary_type == 1 && fv.media[0].density == 0.25f &&
+              fv.media[0].rotation_row0[1] == 1.0f && fv.media[0].rotation_row1[0] == -1.0f && fv.media[0].translation[0] == 3.0f,
+        "medium: box boundary, density, world-to-local rows, translation");
+    fog.add_medium(MediumInstance {cube, diff, 0.25, spin});
+    expect_invalid([&] { (void)adapt_to_realtime(fog); }, "isotropic volume material", "medium with a surface material");
+    SceneIR bad;
+    bad.add_instance(SurfaceInstance {0, 0, Transform::identity()});
+    ++g_checks;
+    try {
+        (void)adapt_to_realtime(bad);
+        ++g_failures;
+        std::fprintf(stderr, "FAILED: a dangling shape index was accepted\n");
+    } catch (const std::out_of_range&) {
+    }
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
         std::fprintf(stderr, "usage: %s DIR [--write-scene FILE]\n", argv[0]);
@@ -819,6 +896,7 @@ int main(int argc, char** argv) {
     rtgb::png::write_rgb(dir / "grid.png", 8, 8, rgb.data());
     try {
         reference_adapter_case();
+        scene_ir_v1_case();
         reference_light_case();
         validator_case();
         transform_case();

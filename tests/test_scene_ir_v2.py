@@ -2,9 +2,11 @@
 realtime_scene_adapter.cpp, openpbr_core_adapter.cpp and
 analytic_light_compiler.cpp of the reference).
 
-CPU: tests/scene_ir_v2_harness.cpp, compiled against the header and linked
+CPU: tests/scene_ir_v2_harness.cpp, compiled against the headers and linked
 to librtgb.so, runs the reference's adapter and light-compiler expectations
-(tests/test_realtime_scene_adapter.cpp, tests/test_analytic_light_compiler.cpp)
+(tests/test_realtime_scene_adapter.cpp, tests/test_analytic_light_compiler.cpp;
+for SceneIR v1 also the Cornell box built through the IR, byte for byte equal
+to the builtin scene)
 and cases of its own (validator codes, time samples, reset transforms,
 visibility and purpose, winding, normals, spheres, the scene file), then
 writes a parity scene lowered from SceneIR v2 to a scene file.
