@@ -18,6 +18,7 @@
 #pragma once
 
 #include <array>
+#include <optional>
 #include <string>
 #include <variant>
 #include <vector>
@@ -155,5 +156,20 @@ void validate_scene_ir(const SceneIR& scene);
 // instance order (a box becomes six quads), then the media; the background is
 // black and there are no analytic lights (the compatibility IR has none).
 HostScenePtr adapt_to_realtime(const SceneIR& scene, const AdaptOptions& options = {});
+
+// openpbr_core_adapter.cpp:215-254: the OpenPBR block of every SceneIR v2
+// material prim that names a compatibility material (its
+// compatibility_source_index), indexed by that material; texture connections
+// bind the compatibility texture index of their texture prim. Prims with a
+// volume payload leave their entry empty. Every compatibility material must
+// be named exactly once.
+std::vector<std::optional<rtgb_openpbr_material>> compile_openpbr_core_material_table(const SceneIRv2& scene,
+    std::size_t compatibility_material_count, std::size_t compatibility_texture_count);
+
+// realtime_scene_adapter.cpp:488-500: the compatibility scene with each
+// surface material replaced by its OpenPBR block from `scene_v2` (a volume
+// material must stay a volume), then the analytic lights of `scene_v2`.
+HostScenePtr adapt_to_realtime_openpbr(const SceneIR& compatibility_scene, const SceneIRv2& scene_v2,
+    const AdaptOptions& options = {});
 
 }  // namespace rtgb::scene

@@ -28,3 +28,13 @@ namespace rtgb::scene::detail {
 // (scene_ir_adapter.cpp); false when no readable file is found.
 bool load_png_texels(const std::string& path, int& width, int& height, std::vector<float>& texels);
 }  // namespace rtgb::scene::detail
+
+namespace rtgb::scene {
+struct SceneMaterialConnection;
+struct SceneTexture;
+namespace detail {
+// One OpenPBR texture connection bound to realtime texture `index`
+// (scene_ir_adapter.cpp); throws for connections the core cannot read.
+void bind_connection(rtgb_openpbr_material& out, const SceneMaterialConnection& c, const SceneTexture& tex, int index);
+}  // namespace detail
+}  // namespace rtgb::scene

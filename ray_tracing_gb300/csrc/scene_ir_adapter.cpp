@@ -280,6 +280,10 @@ int32_t source_color_space(SceneColorSpace cs) {
     throw std::invalid_argument("OpenPBR production core does not yet support ACEScg source conversion");
 }
 
+}  // namespace
+
+namespace detail {
+
 // Binds one connection: RGB colour inputs (base, specular, transmission,
 // emission colour) and raw float scalar inputs (base_metalness,
 // specular_roughness) are what the core reads from textures.
@@ -307,7 +311,7 @@ void bind_connection(rtgb_openpbr_material& out, const SceneMaterialConnection& 
     }
 }
 
-}  // namespace
+}  // namespace detail
 
 rtgb_openpbr_material compile_openpbr_core_material(const SceneOpenPbrSurface& m) {
     require_core_support(m);
@@ -372,7 +376,7 @@ rtgb_openpbr_material compile_openpbr_core_material(const SceneOpenPbrSurface& m
         if (idx == texture_indices.end()) {
             throw std::invalid_argument("OpenPBR connected texture has no realtime texture index: " + c.texture_path);
         }
-        bind_connection(out, c, *tex->texture, idx->second);
+        detail::bind_connection(out, c, *tex->texture, idx->second);
     }
     return out;
 }

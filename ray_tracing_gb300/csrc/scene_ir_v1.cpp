@@ -187,12 +187,68 @@ void validate_scene_ir(const SceneIR& scene) {
     }
 }
 
-HostScenePtr adapt_to_realtime(const SceneIR& scene, const AdaptOptions& options) {
+std::vector<std::optional<rtgb_openpbr_material>> compile_openpbr_core_material_table(const SceneIRv2& scene,
+    std::size_t material_count, std::size_t texture_count) {
+    require_valid_scene_ir_v2(scene);
+    std::vector<std::optional<rtgb_openpbr_material>> table(material_count);
+    std::vector<bool> seen(material_count, false);
+    for (const ScenePrim& prim : scene.prims()) {
+        if (prim.kind != ScenePrimKind::material || !prim.compatibility_source_index) continue;
+        const std::size_t index = *prim.compatibility_source_index;
+        if (index >= material_count) throw std::invalid_argument("SceneIR v2 material compatibility index is out of range");
+        if (seen[index]) throw std::invalid_argument("SceneIR v2 material compatibility index is duplicated");
+        if (!prim.material) throw std::invalid_argument("SceneIR v2 material prim has no material payload");
+        seen[index] = true;
+        const auto* surface = std::get_if<SceneOpenPbrSurface>(&*prim.material);
+        if (!surface) continue;
+        SceneOpenPbrSurface constants = *surface;
+        constants.connections.clear();
+        rtgb_openpbr_material compiled = compile_openpbr_core_material(constants);
+        for (const SceneMaterialConnection& c : surface->connections) {
+            const ScenePrim* tex = scene.find_prim(c.texture_path);
+            if (!tex || !tex->texture) throw std::invalid_argument("OpenPBR connected input does not resolve to a SceneIR v2 texture");
+            if (!tex->compatibility_source_index) {
+                throw std::invalid_argument("OpenPBR connected texture requires a compatibility texture index");
+            }
+            if (*tex->compatibility_source_index >= texture_count) {
+                throw std::invalid_argument("OpenPBR connected texture compatibility index is out of range");
+            }
+            detail::bind_connection(compiled, c, *tex->texture, static_cast<int>(*tex->compatibility_source_index));
+        }
+        table[index] = compiled;
+    }
+    for (std::size_t i = 0; i < seen.size(); ++i) {
+        if (!seen[i]) throw std::invalid_argument("SceneIR v2 is missing a compatibility material for index " + std::to_string(i));
+    }
+    return table;
+}
+
+namespace {
+
+HostScenePtr adapt_impl(const SceneIR& scene, const std::vector<std::optional<rtgb_openpbr_material>>* openpbr,
+    const AdaptOptions& options) {
     validate_scene_ir(scene);
     HostScenePtr result(new rtgb_host_scene);
     rtgb_host_scene& out = *result;
     for (const TextureDesc& t : scene.textures()) out.textures.push_back(pack_texture(t, out, options));
-    for (const MaterialDesc& m : scene.materials()) out.materials.push_back(pack_material(m));
+    for (size_t i = 0; i < scene.materials().size(); ++i) {
+        const MaterialDesc& m = scene.materials()[i];
+        const bool volume = std::holds_alternative<IsotropicVolumeMaterial>(m);
+        if (openpbr && (*openpbr)[i]) {
+            if (volume) throw std::invalid_argument("SceneIR v2 surface material cannot replace a compatibility volume");
+            out.openpbr.push_back(*(*openpbr)[i]);
+            rtgb_material r {};
+            r.albedo_texture = -1;
+            r.emission_texture = -1;
+            r.ior = 1.0f;
+            r.type = RTGB_MATERIAL_OPENPBR;
+            r.openpbr_index = static_cast<int32_t>(out.openpbr.size()) - 1;
+            out.materials.push_back(r);
+            continue;
+        }
+        if (openpbr && !volume) throw std::invalid_argument("SceneIR v2 compatibility surface must compile to OpenPBR");
+        out.materials.push_back(pack_material(m));
+    }
     const auto& shapes = scene.shapes();
     for (const SurfaceInstance& inst : scene.surface_instances()) {
         const ShapeDesc& shape = shapes[static_cast<size_t>(inst.shape_index)];
@@ -246,6 +302,21 @@ HostScenePtr adapt_to_realtime(const SceneIR& scene, const AdaptOptions& options
         }
         out.media.push_back(p);
     }
+    return result;
+}
+
+}  // namespace
+
+HostScenePtr adapt_to_realtime(const SceneIR& scene, const AdaptOptions& options) {
+    return adapt_impl(scene, nullptr, options);
+}
+
+HostScenePtr adapt_to_realtime_openpbr(const SceneIR& compatibility_scene, const SceneIRv2& scene_v2,
+    const AdaptOptions& options) {
+    const auto table = compile_openpbr_core_material_table(scene_v2, compatibility_scene.materials().size(),
+        compatibility_scene.textures().size());
+    HostScenePtr result = adapt_impl(compatibility_scene, &table, options);
+    for (const AnalyticLightDesc& l : compile_analytic_lights(scene_v2)) result->analytic.push_back(pack_analytic_light(l));
     return result;
 }
 

@@ -877,6 +877,71 @@ static void scene_ir_v1_case() {
     }
 }
 
+// adapt_to_realtime_openpbr (realtime_scene_adapter.cpp:488-500): the
+// compatibility surface material becomes the OpenPBR block its SceneIR v2
+// material prim names, the volume stays a volume, the v2 lights come along.
+static void openpbr_compatibility_case() {
+    SceneIR compat;
+    const int tex = compat.add_texture(ConstantColorTextureDesc {{0.4, 0.5, 0.6}});
+    const int surf = compat.add_material(DiffuseMaterial {tex});
+    const int fogm = compat.add_material(IsotropicVolumeMaterial {tex});
+    compat.add_instance(SurfaceInstance {compat.add_shape(SphereShape {{0, 1, 0}, 1.0}), surf, Transform::identity()});
+    compat.add_medium(MediumInstance {compat.add_shape(SphereShape {{0, 0, 0}, 3.0}), fogm, 0.1, Transform::identity()});
+    SceneIRv2 v2;
+    v2.add_prim(prim("/World"));
+    ScenePrim t = prim("/World/Tex", ScenePrimKind::texture);
+    t.texture = SceneTexture {};
+    t.texture->value = {0.4, 0.5, 0.6};
+    t.compatibility_source_index = 0;
+    v2.add_prim(t);
+    SceneOpenPbrSurface pbr;
+    pbr.specular_roughness = 0.2;
+    pbr.connections.push_back({"base_color", SceneMaterialValueType::color3, "/World/Tex", SceneTextureChannel::rgb});
+    ScenePrim m0 = prim("/World/M0", ScenePrimKind::material);
+    m0.material = SceneMaterial {pbr};
+    m0.compatibility_source_index = 0;
+    v2.add_prim(m0);
+    ScenePrim m1 = prim("/World/M1", ScenePrimKind::material);
+    m1.material = SceneMaterial {SceneIsotropicVolumeMaterial {}};
+    m1.compatibility_source_index = 1;
+    v2.add_prim(m1);
+    v2.add_prim(light_prim("/World/Key", light_of(SceneLightType::sphere), translate(0.0, 4.0, 0.0)));
+    const HostScenePtr h = adapt_to_realtime_openpbr(compat, v2);
+    const rtgb_scene v = view_of(h);
+    CHECK(v.material_count == 2 && v.materials[0].type == RTGB_MATERIAL_OPENPBR && v.materials[1].type == RTGB_MATERIAL_ISOTROPIC,
+        "surface material replaced by OpenPBR, volume kept");
+    CHECK(v.openpbr_material_count == 1 && v.openpbr_materials[0].color_texture[0] == 0 &&
+              v.openpbr_materials[0].specular_roughness == 0.2f,
+        "compatibility texture index bound to base_color");
+    CHECK(v.analytic_light_count == 1 && v.sphere_count == 1 && v.medium_count == 1, "v2 lights, v1 geometry and media");
+    SceneIRv2 missing;
+    missing.add_prim(prim("/World"));
+    missing.add_prim(m0);
+    missing.add_prim(t);
+    expect_invalid([&] { (void)adapt_to_realtime_openpbr(compat, missing); }, "missing a compatibility material for index 1",
+        "every compatibility material must be named");
+    SceneIRv2 swap;
+    swap.add_prim(prim("/World"));
+    swap.add_prim(t);
+    ScenePrim s0 = m0, s1 = m1;
+    s0.compatibility_source_index = 1;
+    s1.compatibility_source_index = 0;
+    swap.add_prim(s0);
+    swap.add_prim(s1);
+    expect_invalid([&] { (void)adapt_to_realtime_openpbr(compat, swap); }, "compatibility surface must compile to OpenPBR",
+        "a surface material must get an OpenPBR block");
+    SceneIR only_fog;
+    const int ft = only_fog.add_texture(ConstantColorTextureDesc {{1.0, 1.0, 1.0}});
+    const int fm = only_fog.add_material(IsotropicVolumeMaterial {ft});
+    only_fog.add_instance(SurfaceInstance {only_fog.add_shape(SphereShape {{0, 0, 0}, 1.0}), fm, Transform::identity()});
+    SceneIRv2 pbr_for_fog;
+    pbr_for_fog.add_prim(prim("/World"));
+    pbr_for_fog.add_prim(t);
+    pbr_for_fog.add_prim(m0);
+    expect_invalid([&] { (void)adapt_to_realtime_openpbr(only_fog, pbr_for_fog); }, "cannot replace a compatibility volume",
+        "an OpenPBR surface cannot replace a volume");
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
         std::fprintf(stderr, "usage: %s DIR [--write-scene FILE]\n", argv[0]);
@@ -897,6 +962,7 @@ int main(int argc, char** argv) {
     try {
         reference_adapter_case();
         scene_ir_v1_case();
+        openpbr_compatibility_case();
         reference_light_case();
         validator_case();
         transform_case();
