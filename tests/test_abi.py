@@ -71,3 +71,29 @@ def test_null_arguments_are_invalid():
     assert lib.rtgb_render_frame(None, None, None, 1, None) == 1
     assert lib.rtgb_reset_sequence(None, 0) == 1
     assert lib.rtgb_download_frame(None, 0, None, None, None, None, None) == 1
+    assert lib.rtgb_autotune_launches(None, None, None, 1, 4, None) == 1
+    assert lib.rtgb_host_scene_save(None, b"x") == 1
+    assert lib.rtgb_host_scene_from_view(None, None) == 1
+
+
+def test_scene_files_refuse_bad_input(tmp_path):
+    lib = abi.load()
+    out = C.c_void_p()
+    assert lib.rtgb_host_scene_load(str(tmp_path / "missing.rtgbscene").encode(), C.byref(out)) == 1 and not out.value
+    (tmp_path / "wrong.rtgbscene").write_bytes(b"NOTASCENE" * 8)
+    assert lib.rtgb_host_scene_load(str(tmp_path / "wrong.rtgbscene").encode(), C.byref(out)) == 1 and not out.value
+    # a header whose record sizes disagree with this build's structs
+    import struct
+    bad = b"RTGBSCN1" + struct.pack("<I", 1) + struct.pack("<9I", *([7] * 9))
+    (tmp_path / "layout.rtgbscene").write_bytes(bad)
+    assert lib.rtgb_host_scene_load(str(tmp_path / "layout.rtgbscene").encode(), C.byref(out)) == 1 and not out.value
+    # a file claiming more records than it holds
+    from ray_tracing_gb300 import scenes
+    sc = scenes.HostScene("cornell_box")
+    sc.save(tmp_path / "ok.rtgbscene")
+    data = bytearray((tmp_path / "ok.rtgbscene").read_bytes())
+    data[8 + 4 + 36:8 + 4 + 36 + 8] = struct.pack("<Q", 1 << 40)  # texture count
+    (tmp_path / "huge.rtgbscene").write_bytes(bytes(data))
+    assert lib.rtgb_host_scene_load(str(tmp_path / "huge.rtgbscene").encode(), C.byref(out)) == 1 and not out.value
+    again = scenes.HostScene.load(tmp_path / "ok.rtgbscene")
+    assert again.counts() == sc.counts()
