@@ -129,6 +129,26 @@ def plain_render(r, rig, spp: int):
     return acc / spp, ms
 
 
+def mixed_rig_1080p(scene_name: str = "random_spheres"):
+    """The benchmark scene's four cameras at 1920x1080 with cameras 1 and 3 as
+    180-degree equi62_lut1d fisheyes (r = f theta, f = (w / 2) / (pi / 2), no
+    distortion) at the same poses: the mixed-model 1080p rig of the
+    equal-relMSE target."""
+    import ctypes as C
+    from ray_tracing_gb300 import abi, scenes
+    rig = scenes.default_rig(scene_name, CAMERAS, 1920, 1080)
+    lib = abi.load()
+    for i in (1, 3):
+        c = rig.cameras[i]
+        f = (c.width / 2.0) / (np.pi / 2.0)
+        radial = (C.c_double * 6)(*([0.0] * 6))
+        tangential = (C.c_double * 2)(0.0, 0.0)
+        abi.check(lib.rtgb_make_equi62_lut1d(c.width, c.height, f, f, c.width / 2.0, c.height / 2.0, radial, tangential,
+                                             C.byref(c.equi)), what="rtgb_make_equi62_lut1d")
+        c.model = 1
+    return rig
+
+
 def equal_relmse(sc, rig, prof, frames: int = 8):
     from ray_tracing_gb300.renderer import Renderer
     weights = _weights()
@@ -660,7 +680,7 @@ def run_ours(args, rank, world, local_rank):
     if world == 1 and not args.no_workloads:
         line["workloads"] = workload_records()
     if world == 1 and not args.no_relmse:
-        line["equal_relmse"] = equal_relmse(sc, rig, prof)
+        line["equal_relmse"] = equal_relmse(sc, mixed_rig_1080p() if args.relmse_rig == "mixed1080" else rig, prof)
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(sc, rig, prof)
     print(json.dumps(line), flush=True)
@@ -677,6 +697,9 @@ def main():
     ap.add_argument("--no-relmse", action="store_true", help="skip the equal-relMSE comparison")
     ap.add_argument("--no-training", action="store_true", help="skip the native denoiser-training measurement")
     ap.add_argument("--no-workloads", action="store_true", help="skip the C1 / C3 / C5 workload records")
+    ap.add_argument("--relmse-rig", choices=["bench", "mixed1080"], default="bench",
+                    help="rig of the equal-relMSE comparison: the bench's 4 x 640x480 pinholes, or 2 pinhole + 2 "
+                         "fisheye cameras at 1920x1080")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
     ap.add_argument("--workload", choices=["c1", "c3", "c5"], default=None,
