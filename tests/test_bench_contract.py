@@ -50,3 +50,15 @@ def test_training_flops_count_forward_and_both_gradients():
     fwd = bench.denoiser_flops(w, h, n)
     first = 2.0 * n * h * w * denoiser.LAYERS[0][0] * denoiser.LAYERS[0][1] * 9
     assert bench.training_flops(n, h, w) == pytest.approx(3 * fwd - first)
+
+
+def test_mixed_1080p_rig_for_the_relmse_target():
+    import math
+    rig = bench.mixed_rig_1080p()
+    assert rig.active_count == 4
+    assert [(c.width, c.height, c.model) for c in rig.cameras[:4]] == [(1920, 1080, 0), (1920, 1080, 1)] * 2
+    f = 960.0 / (math.pi / 2.0)
+    for i in (1, 3):
+        e = rig.cameras[i].equi
+        assert e.fx == pytest.approx(f) and e.cx == 960.0 and e.cy == 540.0
+        assert all(e.lut[k] <= e.lut[k + 1] for k in range(len(e.lut) - 1))   # monotone theta(r) table
