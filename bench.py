@@ -301,7 +301,7 @@ def gpu_frames(sc, rig, prof, cameras, warmup, frames):
     return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
 
 
-def workload_records(names=("c1", "c3", "c5"), c3_steps=10, c3_warmup=3):
+def workload_records(names=("c1", "c3", "c5", "smoke"), c3_steps=10, c3_warmup=3):
     """The other configurations of the reference protocol, measured beside the
     headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
     on all host threads renders the same full frame) and C3 (1 M triangles with
@@ -337,7 +337,43 @@ def workload_records(names=("c1", "c3", "c5"), c3_steps=10, c3_warmup=3):
         sc.close()
     if "c5" in names:
         out["C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6"] = c5_record()
+    if "smoke" in names:
+        out["published_protocol_smoke_realtime_4x640x480"] = smoke_record()
     return out
+
+
+def smoke_record(frames=30, warmup=5):
+    """The reference's published realtime protocol: the `smoke` scene (one
+    sphere, one emissive quad), realtime profile (1 spp, 2 bounces, denoised),
+    4 cameras at 640x480, timed per frame with CUDA events. Its published
+    numbers are RTX 3090 ones (frame 31.07 ms average including host work,
+    render critical path 1.54 ms, OptiX temporal denoise 7.29 ms); the render
+    and denoise times here are the comparable parts."""
+    from ray_tracing_gb300 import scenes
+    from ray_tracing_gb300.renderer import Renderer
+    sc = scenes.HostScene("smoke")
+    rig = scenes.default_rig("smoke", 4, 640, 480)
+    weights = _weights()
+    prof = scenes.profile("realtime", enable_denoise=1 if weights is not None else 0)
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    if weights is not None:
+        r.set_denoiser(weights)
+    r.reset_sequence(SEED)
+    for _ in range(warmup):
+        r.render_frame(rig, prof, 4)
+    ms, dn = [], []
+    for _ in range(frames):
+        v = r.render_frame(rig, prof, 4)
+        ms.append(v.frame_render_ms)
+        dn.append(v.cameras[0].denoise_ms)
+    r.close()
+    sc.close()
+    return {"ms_per_frame": float(np.mean(ms)), "ms_p99": float(np.percentile(ms, 99)),
+            "denoise_ms_per_frame": float(np.mean(dn)), "render_ms_per_frame": float(np.mean(ms) - np.mean(dn)),
+            "spp": prof.samples_per_pixel, "max_bounces": prof.max_bounces, "denoised": weights is not None,
+            "reference_rtx3090": {"frame_ms_avg": 31.0712, "render_critical_path_ms": 1.5418,
+                                  "denoise_critical_path_ms": 7.2927, "source": ".planning/v2.0-BASELINE.json:210-222"}}
 
 
 def c5_record(frames=60, warmup=3, degrees_per_frame=2.0):
@@ -702,7 +738,7 @@ def main():
                          "fisheye cameras at 1920x1080")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
-    ap.add_argument("--workload", choices=["c1", "c3", "c5"], default=None,
+    ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
