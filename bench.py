@@ -714,7 +714,10 @@ def run_ours(args, rank, world, local_rank):
     if world == 1 and not args.no_training:
         line["training"] = training_record()
     if world == 1 and not args.no_workloads:
-        line["workloads"] = workload_records()
+        try:
+            line["workloads"] = workload_records()
+        except Exception as e:  # an optional record must not cost the headline line
+            line["workloads"] = {"error": f"{type(e).__name__}: {e}"}
     if world == 1 and not args.no_relmse:
         line["equal_relmse"] = equal_relmse(sc, mixed_rig_1080p() if args.relmse_rig == "mixed1080" else rig, prof)
     if world == 1 and not args.no_cpu_baseline:
