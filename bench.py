@@ -623,7 +623,12 @@ def run_ours(args, rank, world, local_rank):
         r.set_denoiser(weights)
     # launch shapes picked by the library's autotuner for this scene and rig
     # (tuning frames are discarded; results do not depend on the grids)
-    tuning = None if args.no_autotune else r.autotune_launches(rig, prof, CAMERAS, frames=4)
+    tuning = None
+    if not args.no_autotune:
+        try:
+            tuning = r.autotune_launches(rig, prof, CAMERAS, frames=4)
+        except Exception as e:  # the persistent shapes stay in force
+            tuning = {"error": f"{type(e).__name__}: {e}"}
     r.reset_sequence(SEED)
     stream = torch.cuda.ExternalStream(r.stream_ptr())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local_rank}")
