@@ -73,7 +73,10 @@ BYTES_SHADOW = 32 + 4           # per shadow ray
 BYTES_RESOLVE = 68 + 36 + 68 + 12  # per pixel (accumulate + resolve)
 
 
-def workload_config(spatial=1):
+CPU_ROW_STRIDE = 4       # the CPU oracle renders every 4th row of each camera (both arms)
+
+
+def workload_config(spatial=1, world=1):
     return {
         "workload": "random_spheres_4x640x480_1spp_d4_restir32",
         "scene": f"ground + 22x22 spheres, {LIGHTS} analytic rect lights",
@@ -82,6 +85,7 @@ def workload_config(spatial=1):
         "denoise": "BF16 U-Net (tcgen05 implicit-GEMM 3x3 convolutions)" if _weights() is not None
                     else "off (trained weights absent)",
         "seed": SEED, "l2": f"{L2_FLUSH_BYTES >> 20} MiB buffer written between timed frames",
+        "parallelism": f"replicas{world}" if world > 1 else "single",
     }
 
 
@@ -112,21 +116,154 @@ def relmse(x: np.ndarray, ref: np.ndarray) -> float:
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + RELMSE_EPS)))
 
 
-def plain_render(r, rig, spp: int):
+def plain_render(r, rig, spp: int, cameras: int = CAMERAS, max_bounces: int = 4, per_frame: int = SPP_PER_FRAME,
+                 images: bool = True):
     """Averaged beauty of `spp` plain samples per pixel (no ReSTIR, no denoiser),
-    as frames of at most SPP_PER_FRAME spp with the accumulation reset each
-    frame; returns (per-camera images, device ms)."""
+    as frames of at most `per_frame` spp with the accumulation reset each
+    frame; returns (per-camera images or None, device ms)."""
     from ray_tracing_gb300 import scenes
-    chunks = [SPP_PER_FRAME] * (spp // SPP_PER_FRAME) + ([spp % SPP_PER_FRAME] if spp % SPP_PER_FRAME else [])
+    chunks = [per_frame] * (spp // per_frame) + ([spp % per_frame] if spp % per_frame else [])
     acc, ms = None, 0.0
     for per in chunks:
-        prof = scenes.profile("balanced", samples_per_pixel=per, max_bounces=4, enable_denoise=0, enable_restir_di=0)
+        prof = scenes.profile("balanced", samples_per_pixel=per, max_bounces=max_bounces, enable_denoise=0,
+                              enable_restir_di=0)
         r.reset_accumulation()
-        v = r.render_frame(rig, prof, CAMERAS)
+        v = r.render_frame(rig, prof, cameras)
         ms += v.frame_render_ms
-        cur = np.stack([r.buffer(c, "beauty")[..., :3].astype(np.float64) for c in range(CAMERAS)]) * per
-        acc = cur if acc is None else acc + cur
-    return acc / spp, ms
+        if images:
+            cur = np.stack([r.buffer(c, "beauty")[..., :3].astype(np.float64) for c in range(cameras)]) * per
+            acc = cur if acc is None else acc + cur
+    return (acc / spp if images else None), ms
+
+
+# ---- equal relMSE on row bands (1080p rigs) -------------------------------------------
+#
+# A 4096-spp reference of four 1920x1080 cameras costs minutes, so the large
+# rigs are judged on row bands: each camera's band rows are rendered as
+# cropped cameras (same pose and intrinsics, principal point shifted by the
+# band's first row, height = the band), which trace exactly the full camera's
+# rays for those rows. Per-pixel seeds differ from the full frame's, which
+# changes the noise realisation, not its distribution.
+
+BAND_COUNT = 8          # bands per camera, evenly spaced over the image
+BAND_ROWS = 8           # rows per band
+
+
+def band_starts(height: int, bands: int = BAND_COUNT, rows: int = BAND_ROWS) -> list[int]:
+    return [max(0, min(height - rows, int((k + 0.5) * height / bands) - rows // 2)) for k in range(bands)]
+
+
+def crop_camera(cam, y0: int, rows: int):
+    import ctypes as C
+    from ray_tracing_gb300 import abi
+    c = abi.Camera()
+    C.memmove(C.byref(c), C.byref(cam), C.sizeof(abi.Camera))
+    c.height = rows
+    if c.model == 0:
+        c.pinhole.cy = cam.pinhole.cy - y0
+    else:
+        c.equi.cy = cam.equi.cy - y0
+        c.equi.height = rows
+    return c
+
+
+def band_rigs(rig, cameras: int):
+    """Rigs of up to four cropped cameras covering every camera's bands, with
+    the (camera, first row) of each slot."""
+    from ray_tracing_gb300 import abi
+    crops = [(c, y0) for c in range(cameras) for y0 in band_starts(rig.cameras[c].height)]
+    out = []
+    for i in range(0, len(crops), 4):
+        part = crops[i:i + 4]
+        rr = abi.CameraRig()
+        rr.active_count = len(part)
+        for j, (c, y0) in enumerate(part):
+            rr.cameras[j] = crop_camera(rig.cameras[c], y0, BAND_ROWS)
+        out.append((rr, part))
+    return out
+
+
+def band_rows_of(full: np.ndarray, height: int) -> np.ndarray:
+    """The band rows of one full-frame camera image, in band order."""
+    return np.concatenate([full[y0:y0 + BAND_ROWS] for y0 in band_starts(height)], axis=0)
+
+
+def plain_bands(r, rig, cameras: int, spp: int, max_bounces: int, per_frame: int):
+    """Plain `spp`-sample render of every camera's bands; returns (per camera
+    band image (rows, width, 3), device ms)."""
+    parts, ms = {}, 0.0
+    for rr, part in band_rigs(rig, cameras):
+        img, t = plain_render(r, rr, spp, cameras=rr.active_count, max_bounces=max_bounces, per_frame=per_frame)
+        ms += t
+        for j, key in enumerate(part):
+            parts[key] = img[j]
+    bands = [np.concatenate([parts[(c, y0)] for y0 in band_starts(rig.cameras[c].height)], axis=0)
+             for c in range(cameras)]
+    return bands, ms
+
+
+def banded_equal_relmse(sc, frame_rigs: dict, denoised: dict, den_ms: float, max_bounces: int, cameras: int = 4,
+                        ref_spp: int = REFERENCE_SPP, max_spp: int = 1024, time_spp_cap: int = 128):
+    """Equal-relMSE comparison on row bands. `frame_rigs`: frame -> rig;
+    `denoised`: frame -> per-camera band rows of the denoised pipeline's output
+    at that frame; `den_ms`: the pipeline's device ms per frame. The plain path
+    (no ReSTIR, no denoiser) is searched by doubling then bisecting spp until the
+    mean relMSE over the frames is no larger than the denoised mean; its
+    ms/frame is the full rig's device time at that spp (measured up to
+    `time_spp_cap` spp, larger counts scaled linearly from there)."""
+    from ray_tracing_gb300.renderer import Renderer
+    t0 = time.perf_counter()
+    with Renderer() as r:
+        r.prepare_scene(sc.view)
+        r.reset_sequence(SEED + 1)
+        refs = {f: plain_bands(r, rig, cameras, ref_spp, max_bounces, per_frame=64)[0] for f, rig in frame_rigs.items()}
+        ref_secs = time.perf_counter() - t0
+
+        def err(imgs, f):
+            return float(np.mean([relmse(imgs[c], refs[f][c]) for c in range(cameras)]))
+
+        d_err = {f: err(denoised[f], f) for f in frame_rigs}
+        target = float(np.mean(list(d_err.values())))
+
+        def probe(spp):
+            per = {f: err(plain_bands(r, frame_rigs[f], cameras, spp, max_bounces, per_frame=16)[0], f)
+                   for f in frame_rigs}
+            return {"spp": spp, "relmse": float(np.mean(list(per.values()))),
+                    "per_frame": {str(f): v for f, v in per.items()}}
+
+        trail, found, spp = [], None, 1
+        while spp <= max_spp:
+            trail.append(probe(spp))
+            if trail[-1]["relmse"] <= target:
+                found = trail[-1]
+                break
+            spp *= 2
+        if found is not None and len(trail) >= 2:
+            lo, hi = trail[-2]["spp"], trail[-1]["spp"]
+            while hi - lo > max(1, lo // 8):
+                mid = (lo + hi) // 2
+                trail.append(probe(mid))
+                if trail[-1]["relmse"] <= target:
+                    hi, found = mid, trail[-1]
+                else:
+                    lo = mid
+        plain = None
+        if found is not None:
+            first = next(iter(frame_rigs))
+            timed = min(found["spp"], time_spp_cap)
+            _, ms = plain_render(r, frame_rigs[first], timed, cameras=cameras, max_bounces=max_bounces, per_frame=4,
+                                 images=False)
+            plain = dict(found, ms=ms * found["spp"] / timed, timed_spp=timed)
+    return {
+        "eps": RELMSE_EPS, "reference_spp": ref_spp, "frames": [int(f) for f in frame_rigs],
+        "sample": f"{BAND_COUNT} bands of {BAND_ROWS} rows per camera (evenly spaced), rendered as cropped cameras; "
+                  f"{BAND_COUNT * BAND_ROWS} of each camera's rows",
+        "reference_seconds": ref_secs,
+        "denoised": {"relmse": target, "per_frame": {str(f): v for f, v in d_err.items()}, "ms_per_frame": den_ms},
+        "plain": plain if plain is not None else {"spp": None, "note": f"not reached within {max_spp} spp"},
+        "plain_search": trail,
+        "speedup_at_equal_relmse": (plain["ms"] / den_ms) if plain is not None else None,
+    }
 
 
 def mixed_rig_1080p(scene_name: str = "random_spheres"):
@@ -301,45 +438,55 @@ def gpu_frames(sc, rig, prof, cameras, warmup, frames):
     return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
 
 
-def workload_records(names=("c1", "c3", "c5", "smoke"), c3_steps=10, c3_warmup=3):
+def workload_records(names=("c1", "c3", "c5", "smoke", "c4"), c3_steps=10, c3_warmup=3):
     """The other configurations of the reference protocol, measured beside the
     headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
-    on all host threads renders the same full frame) and C3 (1 M triangles with
+    on all host threads renders the same full frame), C3 (1 M triangles with
     200 icosphere instances, constant OpenPBR materials, 256 emissive
     triangles; 2 x pinhole32 640x480 + 2 x equi62_lut1d 1280x1024 fisheye in one
     launch; 1 spp, depth 4, ReSTIR DI on; no analytic lights, so emissive NEE
-    carries the direct light)."""
-    from ray_tracing_gb300 import scenes
+    carries the direct light), C5 (c5_record) with its equal-relMSE
+    comparison, the reference's published smoke protocol and the C4 denoiser
+    inference size. Each record is measured on its own: one that fails is
+    reported as {"error": ...} and the others stand."""
     out = {}
-    if "c1" not in names:
-        sc = None
-    else:
-        sc = scenes.HostScene("cornell_box")
-    if sc is not None:
+    jobs = {
+        "c1": ("C1_cornell_256x256_64spp_d8", c1_record),
+        "c3": ("C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280", lambda: c3_record(c3_steps, c3_warmup)),
+        "c5": ("C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6", c5_record),
+        "smoke": ("published_protocol_smoke_realtime_4x640x480", smoke_record),
+        "c4": ("C4_denoiser_inference_4x1280x720", c4_inference_record),
+    }
+    for key in names:
+        name, fn = jobs[key]
+        try:
+            out[name] = fn()
+        except Exception as e:  # one record's failure must not cost the others
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
+def c1_record():
+    from ray_tracing_gb300 import scenes
+    with scenes.HostScene("cornell_box") as sc:
         rig = scenes.default_rig("cornell_box", 1)
         prof = scenes.profile("quality", samples_per_pixel=64, max_bounces=8, enable_denoise=0, enable_restir_di=0)
         prep, ms, mrays = gpu_frames(sc, rig, prof, 1, 2, 5)
         cores = os.cpu_count() or 1
         rays, secs = oracle_frames(sc, rig, prof, 1, 1, threads=cores, cameras=1)
-        out["C1_cornell_256x256_64spp_d8"] = {
-            "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep,
+    return {"ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep,
             "cpu_oracle": {"ms_per_frame": 1000.0 * secs, "mrays_per_s": rays / secs / 1e6, "cores": cores,
                            "sample": "the full frame, reference BVH"},
             "gpu_over_cpu": (1000.0 * secs) / ms if ms > 0 else None}
-        sc.close()
-    if "c3" in names:
-        sc = scenes.HostScene("triangle_terrain_pbr", detail=1000000)
+
+
+def c3_record(steps=10, warmup=3):
+    from ray_tracing_gb300 import scenes
+    with scenes.HostScene("triangle_terrain_pbr", detail=1000000) as sc:
         rig = scenes.default_rig("triangle_terrain_pbr", 4)
         prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1)
-        prep, ms, mrays = gpu_frames(sc, rig, prof, 4, c3_warmup, c3_steps)
-        out["C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280"] = {
-            "ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
-        sc.close()
-    if "c5" in names:
-        out["C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6"] = c5_record()
-    if "smoke" in names:
-        out["published_protocol_smoke_realtime_4x640x480"] = smoke_record()
-    return out
+        prep, ms, mrays = gpu_frames(sc, rig, prof, 4, warmup, steps)
+        return {"ms_per_frame": ms, "mrays_per_s": mrays, "prepare_ms": prep, "triangles": sc.view.triangle_count}
 
 
 def smoke_record(frames=30, warmup=5):
@@ -351,24 +498,21 @@ def smoke_record(frames=30, warmup=5):
     and denoise times here are the comparable parts."""
     from ray_tracing_gb300 import scenes
     from ray_tracing_gb300.renderer import Renderer
-    sc = scenes.HostScene("smoke")
-    rig = scenes.default_rig("smoke", 4, 640, 480)
     weights = _weights()
     prof = scenes.profile("realtime", enable_denoise=1 if weights is not None else 0)
-    r = Renderer()
-    r.prepare_scene(sc.view)
-    if weights is not None:
-        r.set_denoiser(weights)
-    r.reset_sequence(SEED)
-    for _ in range(warmup):
-        r.render_frame(rig, prof, 4)
-    ms, dn = [], []
-    for _ in range(frames):
-        v = r.render_frame(rig, prof, 4)
-        ms.append(v.frame_render_ms)
-        dn.append(v.cameras[0].denoise_ms)
-    r.close()
-    sc.close()
+    with scenes.HostScene("smoke") as sc, Renderer() as r:
+        rig = scenes.default_rig("smoke", 4, 640, 480)
+        r.prepare_scene(sc.view)
+        if weights is not None:
+            r.set_denoiser(weights)
+        r.reset_sequence(SEED)
+        for _ in range(warmup):
+            r.render_frame(rig, prof, 4)
+        ms, dn = [], []
+        for _ in range(frames):
+            v = r.render_frame(rig, prof, 4)
+            ms.append(v.frame_render_ms)
+            dn.append(v.cameras[0].denoise_ms)
     return {"ms_per_frame": float(np.mean(ms)), "ms_p99": float(np.percentile(ms, 99)),
             "denoise_ms_per_frame": float(np.mean(dn)), "render_ms_per_frame": float(np.mean(ms) - np.mean(dn)),
             "spp": prof.samples_per_pixel, "max_bounces": prof.max_bounces, "denoised": weights is not None,
@@ -376,57 +520,98 @@ def smoke_record(frames=30, warmup=5):
                                   "denoise_critical_path_ms": 7.2927, "source": ".planning/v2.0-BASELINE.json:210-222"}}
 
 
-def c5_record(frames=60, warmup=3, degrees_per_frame=2.0):
+def c4_inference_record(frames=20, warmup=3):
+    """The U-Net at the C4 inference size, 4 x 1280x720 in one batch: the
+    denoiser stage's CUDA-event time inside frames of a cheap scene (one
+    bounce of the smoke scene; the denoiser's cost does not depend on the
+    content) and its algorithmic TFLOP/s against the measured dense BF16 rate."""
+    from ray_tracing_gb300 import scenes
+    from ray_tracing_gb300.renderer import Renderer
+    weights = _weights()
+    if weights is None:
+        return {"unavailable": "trained denoiser weights absent"}
+    prof = scenes.profile("realtime", max_bounces=1, enable_denoise=1)
+    with scenes.HostScene("smoke") as sc, Renderer() as r:
+        rig = scenes.default_rig("smoke", 4, 1280, 720)
+        r.prepare_scene(sc.view)
+        r.set_denoiser(weights)
+        for _ in range(warmup):
+            r.render_frame(rig, prof, 4)
+        dn = []
+        for _ in range(frames):
+            dn.append(r.render_frame(rig, prof, 4).cameras[0].denoise_ms)
+    rec = denoiser_record(dn, 1280, 720, 4)
+    rec["frames"] = frames
+    return rec
+
+
+C5_EVAL_FRAMES = (0, 30, 59)
+
+
+def c5_record(frames=60, warmup=3, degrees_per_frame=2.0, relmse_eval=True):
     """C5: the 4 M-triangle textured room (checker / 3D-noise OpenPBR, 600
     icosphere props, 4096 emissive triangles), 2 x pinhole32 + 2 x
     equi62_lut1d at 1920x1080 in one launch, the rig orbiting the room by
     `degrees_per_frame` each of `frames` frames; 1 spp, depth 6, ReSTIR DI
     (32 candidates, temporal + 1 spatial) and the U-Net denoiser when its
-    weights are present. Frame times are the frames' CUDA events."""
+    weights are present. Frame times are the frames' CUDA events. With the
+    weights, `equal_relmse` compares the denoised output of frames 0, 30 and
+    59 with 4096-spp plain renders of the same frames (row bands,
+    banded_equal_relmse)."""
     from ray_tracing_gb300 import scenes
     from ray_tracing_gb300.renderer import Renderer
-    sc = scenes.HostScene("textured_room")
-    rig = scenes.default_rig("textured_room", 4)
     weights = _weights()
     prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=1 if weights is not None else 0,
                           enable_restir_di=1, restir_initial_candidates=32, restir_temporal_reuse=1,
                           restir_spatial_neighbors=1)
-    r = Renderer(stage_timing=True)
-    t0 = time.perf_counter()
-    r.prepare_scene(sc.view)
-    prep_ms = 1000.0 * (time.perf_counter() - t0)
-    if weights is not None:
-        r.set_denoiser(weights)
-    r.reset_sequence(SEED)
-    for _ in range(warmup):
-        r.render_frame(rig, prof, 4)
-    ms, dn, stages, rays = [], [], [], 0
-    for f in range(frames):
-        v = r.render_frame(scenes.orbit_rig(rig, degrees_per_frame * f), prof, 4)
-        ms.append(v.frame_render_ms)
-        dn.append(v.cameras[0].denoise_ms)
-        stages.append(r.stage_times())
-        rays += v.rays_traced
-    r.close()
-    # per-stage mean ms: raygen, (trace, shade, shadow) per bounce, finalize + resolve
-    st = np.mean(np.stack(stages), axis=0)
-    mb = (len(st) - 3) // 3
-    stage_ms = {"raygen": float(st[0]), "finalize+resolve": float(st[-2] + st[-1])}
-    for b in range(mb):
-        for k, name in enumerate(("trace", "shade", "shadow")):
-            stage_ms[f"{name}@{b}"] = float(st[1 + 3 * b + k])
-    rec = {"ms_per_frame": float(np.mean(ms)), "ms_p50": float(np.median(ms)), "ms_max": float(np.max(ms)),
-           "denoise_ms_per_frame": float(np.mean(dn)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
-           "prepare_ms": prep_ms, "triangles": sc.view.triangle_count, "frames": frames,
-           "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None,
-           "stage_ms": stage_ms}
-    sc.close()
+    with scenes.HostScene("textured_room") as sc:
+        rig = scenes.default_rig("textured_room", 4)
+        with Renderer(stage_timing=True) as r:
+            t0 = time.perf_counter()
+            r.prepare_scene(sc.view)
+            prep_ms = 1000.0 * (time.perf_counter() - t0)
+            if weights is not None:
+                r.set_denoiser(weights)
+            r.reset_sequence(SEED)
+            for _ in range(warmup):
+                r.render_frame(rig, prof, 4)
+            r.reset_accumulation()
+            ms, dn, stages, rays = [], [], [], 0
+            bands, frame_rigs = {}, {}
+            for f in range(frames):
+                frig = scenes.orbit_rig(rig, degrees_per_frame * f)
+                v = r.render_frame(frig, prof, 4)
+                ms.append(v.frame_render_ms)
+                dn.append(v.cameras[0].denoise_ms)
+                stages.append(r.stage_times())
+                rays += v.rays_traced
+                if weights is not None and relmse_eval and f in C5_EVAL_FRAMES:
+                    frame_rigs[f] = frig
+                    bands[f] = [band_rows_of(r.buffer(c, "denoised")[..., :3], frig.cameras[c].height)
+                                for c in range(4)]
+        # per-stage mean ms: raygen, (trace, shade, shadow) per bounce, finalize + resolve
+        st = np.mean(np.stack(stages), axis=0)
+        mb = (len(st) - 3) // 3
+        stage_ms = {"raygen": float(st[0]), "finalize+resolve": float(st[-2] + st[-1])}
+        for b in range(mb):
+            for k, name in enumerate(("trace", "shade", "shadow")):
+                stage_ms[f"{name}@{b}"] = float(st[1 + 3 * b + k])
+        rec = {"ms_per_frame": float(np.mean(ms)), "ms_p50": float(np.median(ms)), "ms_max": float(np.max(ms)),
+               "denoise_ms_per_frame": float(np.mean(dn)), "mrays_per_s": rays / (sum(ms) * 1e-3) / 1e6,
+               "prepare_ms": prep_ms, "triangles": sc.view.triangle_count, "frames": frames,
+               "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None,
+               "stage_ms": stage_ms}
+        if bands:
+            try:
+                rec["equal_relmse"] = banded_equal_relmse(sc, frame_rigs, bands, float(np.mean(ms)), max_bounces=6)
+            except Exception as e:  # the frame timings above stand on their own
+                rec["equal_relmse"] = {"error": f"{type(e).__name__}: {e}"}
     return rec
 
 
 def cpu_baseline(sc, rig, prof):
     cores = os.cpu_count() or 1
-    stride = 2
+    stride = CPU_ROW_STRIDE
     rays, secs = oracle_frames(sc, rig, prof, stride, frames=2, threads=cores)
     return {"value": rays / secs / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"CPU oracle (reference BVH, {cores} threads): every {stride}th row of each of the "
@@ -438,7 +623,7 @@ def run_reference(args, rank, world):
         return 0
     sc, rig, prof = make_inputs()
     cores = os.cpu_count() or 1
-    stride = 20
+    stride = CPU_ROW_STRIDE
     from oracle.binding import OracleRenderer
     orc = OracleRenderer(sc.view, use_reference_bvh=True, threads=cores)
     orc.reset_sequence(SEED)
@@ -454,7 +639,8 @@ def run_reference(args, rank, world):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(world=world),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"every {stride}th row of each camera per step; the reference's renderer "
                                    "needs CUDA/OptiX/Eigen and does not build here, so its radiance kernel runs as "
@@ -477,18 +663,20 @@ def denoiser_flops(width: int, height: int, cameras: int) -> float:
     return sum(2.0 * px * ci * co * 9 for px, (ci, co) in zip(res, denoiser.LAYERS))
 
 
-def denoiser_record(denoise_ms):
-    """Tensor-core roofline of the denoiser stage (all its launches), against
-    the measured dense BF16 throughput."""
+def denoiser_record(denoise_ms, width=WIDTH, height=HEIGHT, cameras=CAMERAS):
+    """Tensor-core roofline of the denoiser stage (all its launches) on
+    `cameras` frames of width x height, against the measured dense BF16
+    throughput."""
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("bf16_tflops")
     note = "of measured (burst)" if peak else "of fallback"
     peak = peak or 1900.0
     ms = float(np.mean(denoise_ms)) if denoise_ms else 0.0
-    flops = denoiser_flops(WIDTH, HEIGHT, CAMERAS)
+    flops = denoiser_flops(width, height, cameras)
     achieved = flops / (ms * 1e-3) / 1e12 if ms > 0 else 0.0
     return {"ms_per_frame": ms, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "peak_source": note, "flops_per_frame": flops}
+            "frac": achieved / peak, "peak_source": note, "flops_per_frame": flops,
+            "frame": f"{cameras} x {width}x{height}"}
 
 
 TRAIN_BATCH, TRAIN_CROP = 16, 256     # the learned-denoiser training shape (16 crops of 256 x 256)
@@ -627,7 +815,7 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_autotune:
         try:
             tuning = r.autotune_launches(rig, prof, CAMERAS, frames=4)
-        except Exception as e:  # the persistent shapes stay in force
+        except Exception as e:  # a failed tuning leaves the handle's grids as they were
             tuning = {"error": f"{type(e).__name__}: {e}"}
     r.reset_sequence(SEED)
     stream = torch.cuda.ExternalStream(r.stream_ptr())
@@ -707,7 +895,7 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": dict(workload_config(), parallelism=f"replicas{world}" if world > 1 else "single"),
+        "config": workload_config(world=world),
         "rays_per_frame": rays / args.steps / world,
         "roofline": roof,
         "e2e": e2e,
@@ -719,10 +907,7 @@ def run_ours(args, rank, world, local_rank):
     if world == 1 and not args.no_training:
         line["training"] = training_record()
     if world == 1 and not args.no_workloads:
-        try:
-            line["workloads"] = workload_records()
-        except Exception as e:  # an optional record must not cost the headline line
-            line["workloads"] = {"error": f"{type(e).__name__}: {e}"}
+        line["workloads"] = workload_records()
     if world == 1 and not args.no_relmse:
         line["equal_relmse"] = equal_relmse(sc, mixed_rig_1080p() if args.relmse_rig == "mixed1080" else rig, prof)
     if world == 1 and not args.no_cpu_baseline:
@@ -746,7 +931,7 @@ def main():
                          "fisheye cameras at 1920x1080")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
-    ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke"], default=None,
+    ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke", "c4"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -314,6 +314,12 @@ typedef struct rtgb_create_info {
                                   bounce 0 when the scene has OpenPBR materials or more than 8
                                   materials), 2 always from bounce 0, 1 from bounce 1, -1 never;
                                   results do not depend on it */
+    int32_t debug_traversal_limit; /* node visits per BVH traversal before the loop gives up; 0 = 2^24.
+                                      No reference counterpart: the reference's traversal loop is unbounded
+                                      (programs.cu:1632-1650). A loop that gives up makes the frame return
+                                      RTGB_DEVICE_FAULT_FLAG; small values exist to test that path. */
+    int32_t debug_rejection_limit; /* draws of the rejection sampler (random_in_unit_sphere,
+                                      programs.cu:125-133, unbounded there) before it gives up; 0 = 10^6 */
 } rtgb_create_info;
 
 /* DeviceRadianceFrameView (src/realtime/gpu/device_radiance_frame_view.h) plus
@@ -422,6 +428,19 @@ rtgb_status rtgb_frame_stats(rtgb_handle handle, rtgb_frame_views* out_views);
  * then finalize and resolve (3 * max_bounces + 3 entries). Needs
  * rtgb_create_info::stage_timing. */
 rtgb_status rtgb_stage_times(rtgb_handle handle, float* out_ms, int32_t capacity, int32_t* out_count);
+
+/* Changes the debug loop bounds of rtgb_create_info on a live handle (0 keeps
+ * the default). No reference counterpart. Frames after the call use the new
+ * bounds; a frame in which a bounded loop gave up returns
+ * RTGB_DEVICE_FAULT_FLAG with the count in rtgb_last_error, and the handle
+ * stays usable. */
+rtgb_status rtgb_set_debug_limits(rtgb_handle handle, int32_t traversal_limit, int32_t rejection_limit);
+
+/* Grid size (blocks) of each wavefront launch slot the handle uses now
+ * (persistent sizes, or the autotuner's choice). No reference counterpart
+ * (OptiX picks its own launch shapes). Fills min(capacity, count) entries;
+ * *count = number of slots. */
+rtgb_status rtgb_launch_grids(rtgb_handle handle, int32_t* grids, int32_t capacity, int32_t* count);
 
 /* Launch-shape autotuner (no reference counterpart; the reference leaves
  * launch shapes to OptiX). Renders `frames` (1..64) frames of this rig and
@@ -687,8 +706,10 @@ const char* rtgb_trainer_last_error(rtgb_trainer trainer);
  *   message           optional caller buffer for the error text
  * 2 <= primitive_count <= RTGB_STATIC_LBVH_MAX_PRIMITIVES, else RTGB_INVALID_ARGUMENT.
  * The first call on a device looks up the array's address there; make it
- * before any stream capture. Calls overlapping in time share the one array
- * and race: serialise them. Asynchronous on `stream`. */
+ * before any stream capture. The address is cached for the life of the
+ * process: after cudaDeviceReset of that device the entry point must not be
+ * called for it again. Calls overlapping in time share the one array and
+ * race: serialise them. Asynchronous on `stream`. */
 rtgb_status rtgb_build_lbvh_static(int32_t device, const float* aabb_lo, const float* aabb_hi,
     int32_t primitive_count, uint32_t* sorted_morton, int32_t* sorted_primitive, int32_t* node_children,
     float* nodes, void* stream, char* message, size_t message_size);

@@ -3,9 +3,13 @@
 // RendererPool (src/realtime/gpu/renderer_pool.h:30-53) with their frame
 // types (frame_types.h:9-22), so C++ callers of the reference switch by
 // changing the namespace and the scene type. Failures throw what the
-// reference throws: std::invalid_argument for a rejected request (status
-// RTGB_INVALID_ARGUMENT), std::runtime_error for everything else; the
-// message is the handle's rtgb_last_error.
+// reference throws, with the handle's rtgb_last_error as the message:
+// std::runtime_error for a rejected render request (active camera count, rig
+// slots, camera index: validate_render_pool_request and
+// validate_render_camera_request, src/realtime/gpu/render_request_validation.cpp:15-62)
+// and for CUDA failures; std::invalid_argument where the reference uses it,
+// for a scene without surfaces (gpu_scene_acceleration.cpp:335) and a bad
+// denoiser input.
 //
 // One handle renders all cameras of a frame in one launch sequence, so the
 // pool's N renderers are one handle here; RendererPool(n) only bounds the
@@ -70,15 +74,25 @@ struct CameraDeviceRenderResult {
 
 namespace detail {
 
-inline void check(rtgb_status st, rtgb_handle h, const char* what) {
-    if (st == RTGB_OK) return;
+inline std::string message(rtgb_handle h, const char* what) {
     std::string msg = what;
     if (h) {
         const char* e = rtgb_last_error(h);
         if (e && *e) msg += std::string(": ") + e;
     }
-    if (st == RTGB_INVALID_ARGUMENT) throw std::invalid_argument(msg);
-    throw std::runtime_error(msg);
+    return msg;
+}
+
+// Scene and set-up calls: a rejected argument is std::invalid_argument.
+inline void check(rtgb_status st, rtgb_handle h, const char* what) {
+    if (st == RTGB_OK) return;
+    if (st == RTGB_INVALID_ARGUMENT) throw std::invalid_argument(message(h, what));
+    throw std::runtime_error(message(h, what));
+}
+
+// Render requests: the reference's request validation throws std::runtime_error.
+inline void check_request(rtgb_status st, rtgb_handle h, const char* what) {
+    if (st != RTGB_OK) throw std::runtime_error(message(h, what));
 }
 
 inline double luminance(const std::vector<float>& rgba) {
@@ -114,7 +128,7 @@ public:
 
     rtgb_restir_stats restir_diagnostics(int camera_index = 0) const {
         rtgb_restir_stats s {};
-        detail::check(rtgb_restir_diagnostics(h_, camera_index, &s), h_, "restir_diagnostics");
+        detail::check_request(rtgb_restir_diagnostics(h_, camera_index, &s), h_, "restir_diagnostics");
         return s;
     }
     rtgb_acceleration_info acceleration_diagnostics() const {
@@ -124,12 +138,15 @@ public:
     }
 
     DirectionDebugFrame render_direction_debug(const rtgb_camera_rig& rig, int camera_index = 0) {
-        if (camera_index < 0 || camera_index >= RTGB_MAX_CAMERAS) throw std::invalid_argument("camera_index out of range");
+        if (camera_index < 0 || camera_index >= RTGB_MAX_CAMERAS) {
+            throw std::runtime_error("render_direction_debug camera_index out of range");
+        }
         DirectionDebugFrame f;
         f.width = rig.cameras[camera_index].width;
         f.height = rig.cameras[camera_index].height;
         f.rgba.resize(static_cast<size_t>(f.width) * static_cast<size_t>(f.height) * 4);
-        detail::check(rtgb_render_direction_debug(h_, &rig, camera_index, f.rgba.data()), h_, "render_direction_debug");
+        detail::check_request(rtgb_render_direction_debug(h_, &rig, camera_index, f.rgba.data()), h_,
+            "render_direction_debug");
         return f;
     }
 
@@ -159,11 +176,11 @@ public:
     // every active camera of one frame (RendererPool::render_frame's work)
     rtgb_frame_views render(const rtgb_camera_rig& rig, const rtgb_render_profile& profile, int active) {
         rtgb_frame_views v {};
-        detail::check(rtgb_render_frame(h_, &rig, &profile, active, &v), h_, "render_frame");
+        detail::check_request(rtgb_render_frame(h_, &rig, &profile, active, &v), h_, "render_frame");
         return v;
     }
     ProfiledRadianceFrame download(const rtgb_frame_views& v, int camera_index) {
-        if (camera_index < 0 || camera_index >= v.camera_count) throw std::invalid_argument("camera_index out of range");
+        if (camera_index < 0 || camera_index >= v.camera_count) throw std::runtime_error("camera_index out of range");
         const rtgb_camera_frame_view& c = v.cameras[camera_index];
         ProfiledRadianceFrame out;
         RadianceFrame& f = out.frame;
@@ -175,15 +192,15 @@ public:
         f.albedo_rgba.resize(px * 4);
         f.depth.resize(px);
         float dl = 0.0f;
-        detail::check(rtgb_download_frame(h_, camera_index, f.beauty_rgba.data(), f.normal_rgba.data(), f.albedo_rgba.data(),
-                          f.depth.data(), &dl),
+        detail::check_request(rtgb_download_frame(h_, camera_index, f.beauty_rgba.data(), f.normal_rgba.data(),
+                                  f.albedo_rgba.data(), f.depth.data(), &dl),
             h_, "download_frame");
         f.average_luminance = detail::luminance(f.beauty_rgba);
         out.timing = {c.render_ms, c.denoise_ms, dl};
         return out;
     }
     ProfiledDeviceRadianceFrame device_view(const rtgb_frame_views& v, int camera_index) const {
-        if (camera_index < 0 || camera_index >= v.camera_count) throw std::invalid_argument("camera_index out of range");
+        if (camera_index < 0 || camera_index >= v.camera_count) throw std::runtime_error("camera_index out of range");
         const rtgb_camera_frame_view& c = v.cameras[camera_index];
         return {c.beauty, c.width, c.height, {c.render_ms, c.denoise_ms, 0.0}};
     }
@@ -230,7 +247,8 @@ private:
         return device;
     }
     void require_active(int active) const {
-        if (active < 1 || active > count_) throw std::invalid_argument("active camera count exceeds the renderer pool");
+        // validate_render_pool_request (render_request_validation.cpp:43-46)
+        if (active < 1 || active > count_) throw std::runtime_error("RendererPool::render_frame active_cameras out of range");
     }
     int count_;
     OptixRenderer renderer_;

@@ -164,7 +164,8 @@ class RenderProfile(C.Structure):
 
 class CreateInfo(C.Structure):
     _fields_ = [("device", C.c_int32), ("use_cuda_graph", C.c_int32), ("debug_path_records", C.c_int32),
-                ("stage_timing", C.c_int32), ("shade_order", C.c_int32)]
+                ("stage_timing", C.c_int32), ("shade_order", C.c_int32), ("debug_traversal_limit", C.c_int32),
+                ("debug_rejection_limit", C.c_int32)]
 
 
 class CameraFrameView(C.Structure):
@@ -237,6 +238,8 @@ SIGNATURES = {
     "rtgb_frame_stats": (C.c_int, [Handle, P(FrameViews)]),
     "rtgb_ray_totals": (C.c_int, [Handle, P(C.c_uint64)]),
     "rtgb_stage_times": (C.c_int, [Handle, P(C.c_float), C.c_int32, P(C.c_int32)]),
+    "rtgb_set_debug_limits": (C.c_int, [Handle, C.c_int32, C.c_int32]),
+    "rtgb_launch_grids": (C.c_int, [Handle, P(C.c_int32), C.c_int32, P(C.c_int32)]),
     "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       P(C.c_float)]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),

@@ -81,20 +81,36 @@ RTGB_HD float rnd(uint32_t& s) {
     s = s * 1664525u + 1013904223u;
     return static_cast<float>(s & 0x00ffffffu) * (1.0f / 16777216.0f);
 }
+// Bounds of the device loops that have no fixed trip count. The defaults never
+// bind on real inputs; a smaller limit (rtgb_create_info's debug fields) makes
+// a loop give up early so the error path can be exercised. A loop that reaches
+// its bound counts itself in *gave_up and returns a defined value.
+constexpr int kDefaultTraversalLimit = 1 << 24;
+constexpr int kDefaultRejectionLimit = 1000000;
+
+struct LoopBounds {
+    int traversal;   // wide-BVH node visits per ray
+    int rejection;   // draws of random_in_unit_sphere
+    int* gave_up;    // per-frame count of loops that reached their bound (device word)
+};
+
 // Draws are consumed left to right (x, y, z).
-RTGB_D float3 random_in_unit_sphere(uint32_t& rng) {
+RTGB_D float3 random_in_unit_sphere(uint32_t& rng, const LoopBounds& lb) {
     // The reference loops until acceptance; 1e6 rejections have probability
-    // (1 - pi/6)^1e6, so the bound never binds but keeps the loop finite.
-    for (int guard = 0; guard < 1000000; ++guard) {
+    // (1 - pi/6)^1e6, so the default bound never binds but keeps the loop finite.
+    for (int guard = 0; guard < lb.rejection; ++guard) {
         const float a = rnd(rng) * 2.0f - 1.0f;
         const float b = rnd(rng) * 2.0f - 1.0f;
         const float c = rnd(rng) * 2.0f - 1.0f;
         const float3 p = f3(a, b, c);
         if (len_sq(p) < 1.0f) return p;
     }
+    if (lb.gave_up) atomicAdd(lb.gave_up, 1);
     return f3(0.0f, 0.0f, 0.0f);
 }
-RTGB_D float3 random_unit_vector(uint32_t& rng) { return normalize(random_in_unit_sphere(rng)); }
+RTGB_D float3 random_unit_vector(uint32_t& rng, const LoopBounds& lb) {
+    return normalize(random_in_unit_sphere(rng, lb));
+}
 
 // ---- light pdfs (light_sampling.h:64-124) --------------------------------------
 RTGB_HD float uniform_sphere_pdf() { return 0.07957747154594767f; }
@@ -362,6 +378,7 @@ struct DeviceScene {
     const rtgb_openpbr_material* openpbr;  // compiled OpenPBR materials (rtgb_material::openpbr_index)
     int openpbr_count;
     float background[3];
+    LoopBounds bounds;              // traversal / rejection bounds and the gave-up word
 };
 
 // ---- cameras: programs.cu:304-537 ------------------------------------------------
@@ -690,7 +707,8 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
     int sp = 0;
     int node = 0;
     const float kInf = __int_as_float(0x7f800000);
-    for (int guard = 0; guard < (1 << 24); ++guard) {
+    int guard = 0;
+    for (; guard < s.bounds.traversal; ++guard) {
         float4 q[kNode4];
         load_node4(s, staged, staged_count, node, q);
         float t0 = kInf, t1 = kInf, t2 = kInf, t3 = kInf;
@@ -735,6 +753,7 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
         if (sp == 0) break;
         node = stack[--sp];
     }
+    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     return best;
 }
 
@@ -752,7 +771,8 @@ RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d,
     int stack[kTraversalStack];
     int sp = 0;
     int node = 0;
-    for (int guard = 0; guard < (1 << 24); ++guard) {
+    int guard = 0;
+    for (; guard < s.bounds.traversal; ++guard) {
         float4 q[kNode4];
         load_node4(s, staged, staged_count, node, q);
         int next = -1;
@@ -783,6 +803,7 @@ RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d,
         if (sp == 0) break;
         node = stack[--sp];
     }
+    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     return false;
 }
 

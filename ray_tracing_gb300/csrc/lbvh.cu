@@ -6,7 +6,7 @@
 // Ties between equal Morton codes break by primitive index (the sort is
 // stable over index-ordered input, and the Karras prefix length falls back to
 // the index when keys are equal), so the leaf order is a pure function of the
-// input and oracle/lbvh_oracle.cpp reproduces it bit for bit.
+// input and oracle/lbvh.py reproduces it bit for bit.
 #include "lbvh.cuh"
 
 #include <algorithm>
@@ -287,6 +287,10 @@ LbvhScratch lbvh_carve(void* base, int n) {
 cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals, uint32_t** sorted_keys,
     cudaStream_t stream) {
     if (n < 2) return cudaErrorInvalidValue;
+    // An error left on this thread by earlier work is returned unchanged (and
+    // not cleared) before anything is launched, so the launch check at the end
+    // sees this build's launches only.
+    if (const cudaError_t pending = cudaPeekAtLastError(); pending != cudaSuccess) return pending;
     const int threads = 256;
     const int grid = std::min((n + threads - 1) / threads, 4096);
     k_init_bounds<<<1, 32, 0, stream>>>(s.bounds_bits);
@@ -302,7 +306,9 @@ cudaError_t lbvh_build(LbvhScratch& s, int n, BvhNode* nodes, int** sorted_vals,
         cur ^= 1;
     }
     k_karras<<<(n - 1 + threads - 1) / threads, threads, 0, stream>>>(s.keys[cur], n, s.children, s.parent);
-    cudaMemsetAsync(s.flags, 0, static_cast<size_t>(n) * sizeof(int), stream);
+    if (const cudaError_t e = cudaMemsetAsync(s.flags, 0, static_cast<size_t>(n) * sizeof(int), stream); e != cudaSuccess) {
+        return e;
+    }
     k_bounds<<<(n + threads - 1) / threads, threads, 0, stream>>>(s.aabb_lo, s.aabb_hi, s.vals[cur], n, s.children,
         s.parent, s.flags, s.node_lo, s.node_hi, nodes);
     *sorted_vals = s.vals[cur];
@@ -389,7 +395,9 @@ cudaError_t lbvh_refit(LbvhScratch& s, int n, const int* sorted_vals, const int*
     BvhNode* nodes, cudaStream_t stream) {
     if (n < 2) return cudaErrorInvalidValue;
     const int threads = 256;
-    cudaMemsetAsync(s.flags, 0, static_cast<size_t>(n) * sizeof(int), stream);
+    if (const cudaError_t e = cudaMemsetAsync(s.flags, 0, static_cast<size_t>(n) * sizeof(int), stream); e != cudaSuccess) {
+        return e;
+    }
     k_bounds<<<(n + threads - 1) / threads, threads, 0, stream>>>(s.aabb_lo, s.aabb_hi, sorted_vals, n, children,
         parent, s.flags, s.node_lo, s.node_hi, nodes);
     return cudaGetLastError();

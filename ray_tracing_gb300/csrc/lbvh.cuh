@@ -56,7 +56,7 @@ cudaError_t fill_bvh4(const BvhNode* nodes2, const int* child4, const int* ref4,
     cudaStream_t stream);
 
 // Morton code of a centroid inside the centroid bounds, 10 bits per axis.
-// The CPU restatement in oracle/lbvh_oracle.cpp follows it operation for operation.
+// The CPU restatement in oracle/lbvh.py (numpy) follows it operation for operation.
 RTGB_HD uint32_t expand_bits10(uint32_t v) {
     v = (v * 0x00010001u) & 0xFF0000FFu;
     v = (v * 0x00000101u) & 0x0F00F00Fu;

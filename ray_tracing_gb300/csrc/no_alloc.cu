@@ -14,6 +14,9 @@
 // device (cudaGetSymbolAddress, with that device current) and caches it; later
 // calls only launch. That first call may load the module and create the primary
 // context, so make it once before any stream capture or latency-critical loop.
+// The cached address belongs to the device's primary context: after
+// cudaDeviceReset on that device it is stale, so a process that resets a
+// device must not call this entry point for that device again.
 // The one array is shared by every call on a device: calls that overlap in time
 // (two host threads, or two streams without an ordering between them) race on
 // it and must be serialised by the caller.
@@ -103,6 +106,10 @@ extern "C" rtgb_status rtgb_build_lbvh_static(int32_t device, const float* aabb_
     DeviceGuard guard;
     cudaError_t e = guard.enter(device);
     if (e != cudaSuccess) return fail(message, message_size, RTGB_RUNTIME_ERROR, "cudaSetDevice", e);
+    // an error from earlier work on this thread is reported as such and left
+    // in place for its owner
+    if ((e = cudaPeekAtLastError()) != cudaSuccess)
+        return fail(message, message_size, RTGB_RUNTIME_ERROR, "a CUDA error was pending before the call", e);
     if (g_scratch_address[device] == nullptr) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_lbvh_scratch);

@@ -268,6 +268,9 @@ struct rtgb_renderer {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     bool stage_timing = false;
     int shade_order = 0;  // rtgb_create_info::shade_order
+    // device loop bounds (rtgb_create_info debug fields, rtgb_set_debug_limits)
+    int traversal_limit = kDefaultTraversalLimit;
+    int rejection_limit = kDefaultRejectionLimit;
     std::vector<cudaEvent_t> stage_events;
     int stage_count = 0;
     uint64_t frame_h2d = 0;
@@ -285,6 +288,17 @@ struct rtgb_renderer {
         graph_exec = nullptr;
         graph_key[0] = -1;
     }
+
+    // Loop bounds of the device code: 0 (or less) keeps the default. The scene
+    // struct is baked into captured graphs, so the graph is dropped.
+    void set_limits(int traversal, int rejection) {
+        traversal_limit = traversal > 0 ? traversal : kDefaultTraversalLimit;
+        rejection_limit = rejection > 0 ? rejection : kDefaultRejectionLimit;
+        scene.bounds = loop_bounds();
+        drop_graph();
+    }
+
+    LoopBounds loop_bounds() const { return LoopBounds{traversal_limit, rejection_limit, &d_counters->gave_up}; }
 
     void set_denoiser(const float* params, long long count) {
         RTGB_CHECK(cudaSetDevice(device));
@@ -334,6 +348,7 @@ struct rtgb_renderer {
         d_counters = static_cast<Counters*>(counters_mem.ensure(sizeof(Counters)));
         RTGB_CHECK(cudaMemsetAsync(d_counters, 0, sizeof(Counters), stream));
         d_fp = static_cast<FrameParams*>(fp_mem.ensure(sizeof(FrameParams)));
+        set_limits(info.debug_traversal_limit, info.debug_rejection_limit);
         RTGB_CHECK(cudaMallocHost(reinterpret_cast<void**>(&h_counters), sizeof(Counters)));
         std::memset(h_counters, 0, sizeof(Counters));
         RTGB_CHECK(cudaEventCreate(&ev_start));
@@ -601,6 +616,7 @@ struct rtgb_renderer {
         RTGB_CHECK(cudaStreamSynchronize(stream));
         RTGB_CHECK(cudaGetLastError());
         RTGB_CHECK(cudaEventElapsedTime(&build_ms, ev.a, ev.b));
+        d.bounds = loop_bounds();
         scene = d;
     }
 
@@ -1137,8 +1153,18 @@ struct rtgb_renderer {
                 error = "a denoiser kernel gave up waiting (code " + std::to_string(h_counters->denoise_error) + ")";
                 return RTGB_DEVICE_FAULT_FLAG;
             }
+            if (h_counters->gave_up != 0) {
+                error = gave_up_message();
+                return RTGB_DEVICE_FAULT_FLAG;
+            }
         }
         return RTGB_OK;
+    }
+
+    std::string gave_up_message() const {
+        return std::to_string(h_counters->gave_up) + " device loops reached their bound this frame (traversal " +
+               std::to_string(traversal_limit) + " node visits, rejection sampling " + std::to_string(rejection_limit) +
+               " draws); the frame's results are incomplete";
     }
 
     void fill_view(int c, rtgb_camera_frame_view& v) const {
@@ -1316,7 +1342,10 @@ rtgb_status rtgb_frame_stats(rtgb_handle h, rtgb_frame_views* out) {
         out->sample_stream = h->sample_stream - 1;
         for (int c = 0; c < h->last_count; ++c) h->fill_view(c, out->cameras[c]);
         h->fill_stats(out);
-        return h->h_counters->error != 0 || h->h_counters->denoise_error != 0 ? RTGB_DEVICE_FAULT_FLAG : RTGB_OK;
+        if (h->h_counters->gave_up != 0) h->error = h->gave_up_message();
+        return h->h_counters->error != 0 || h->h_counters->denoise_error != 0 || h->h_counters->gave_up != 0
+                   ? RTGB_DEVICE_FAULT_FLAG
+                   : RTGB_OK;
     });
 }
 
@@ -1334,6 +1363,23 @@ rtgb_status rtgb_stage_times(rtgb_handle h, float* out, int32_t capacity, int32_
         *count = h->stage_count;
         return RTGB_OK;
     });
+}
+
+rtgb_status rtgb_set_debug_limits(rtgb_handle h, int32_t traversal_limit, int32_t rejection_limit) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        RTGB_CHECK(cudaSetDevice(h->device));
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        h->set_limits(traversal_limit, rejection_limit);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_launch_grids(rtgb_handle h, int32_t* grids, int32_t capacity, int32_t* count) {
+    if (!h || !count || capacity < 0 || (capacity > 0 && !grids)) return RTGB_INVALID_ARGUMENT;
+    for (int i = 0; i < capacity && i < kLaunchShapes; ++i) grids[i] = h->shapes[i].grid;
+    *count = kLaunchShapes;
+    return RTGB_OK;
 }
 
 // Launch-shape autotuner: the wavefront kernels loop grid-stride over the
@@ -1354,6 +1400,24 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         *out = rtgb_launch_tuning {};
         LaunchShape base[kLaunchShapes];
         query_launch_shapes(h->sm_count, base);
+        // Every exit that does not reach the end (a failed render, a CUDA
+        // error thrown out of here) puts back the shapes and the stage-timing
+        // switch the handle had before, drops the graph captured with a
+        // candidate's grids and restarts accumulation.
+        struct Restore {
+            rtgb_renderer* h;
+            LaunchShape shapes[kLaunchShapes];
+            bool had_timing;
+            bool done = false;
+            ~Restore() {
+                if (done) return;
+                std::memcpy(h->shapes, shapes, sizeof shapes);
+                h->stage_timing = had_timing;
+                h->drop_graph();
+                h->reset_accumulation();
+            }
+        } restore{h, {}, h->stage_timing};
+        std::memcpy(restore.shapes, h->shapes, sizeof restore.shapes);
         const bool had_timing = h->stage_timing;
         h->stage_timing = true;
         auto apply = [&](const float* scale_of_group) {
@@ -1416,6 +1480,7 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         h->stage_timing = had_timing;
         h->drop_graph();
         h->reset_accumulation();
+        restore.done = true;
         return RTGB_OK;
     });
 }

@@ -389,15 +389,15 @@ RTGB_D void load_path(const Paths& P, int path, PathRegs& st) {
 // parameters when h.mtype == 5; `sss_event` reports an OpenPBR subsurface
 // entry (1) or exit (2).
 template <bool kPbr>
-RTGB_D bool scatter(const FrameParams& fp, const Hit& h, const pbr::Mat* pm, int bounce, uint32_t& rng, PathRegs& st,
-    int& sss_event, int& event) {
+RTGB_D bool scatter(const FrameParams& fp, const LoopBounds& lb, const Hit& h, const pbr::Mat* pm, int bounce,
+    uint32_t& rng, PathRegs& st, int& sss_event, int& event) {
     sss_event = 0;
     event = 0;
     bool scattered = false;
     float pdf = 0.0f;
     bool delta = true;
     if (h.mtype == 0) {
-        float3 dir = add(h.sn, random_unit_vector(rng));
+        float3 dir = add(h.sn, random_unit_vector(rng, lb));
         if (near_zero(dir)) dir = h.sn;
         st.o = add(h.pos, mul(h.sn, kRayEpsilon));
         st.d = normalize(dir);
@@ -407,7 +407,7 @@ RTGB_D bool scatter(const FrameParams& fp, const Hit& h, const pbr::Mat* pm, int
         scattered = true;
     } else if (h.mtype == 1) {
         const float3 refl = reflect(normalize(st.d), h.sn);
-        const float3 fz = mul(random_in_unit_sphere(rng), fminf(fmaxf(h.fuzz, 0.0f), 1.0f));
+        const float3 fz = mul(random_in_unit_sphere(rng, lb), fminf(fmaxf(h.fuzz, 0.0f), 1.0f));
         const float3 sc = normalize(add(refl, fz));
         if (dot(sc, h.sn) > 0.0f) {
             st.o = add(h.pos, mul(h.sn, kRayEpsilon));
@@ -450,7 +450,7 @@ RTGB_D bool scatter(const FrameParams& fp, const Hit& h, const pbr::Mat* pm, int
             event = smp.event;
         }
     } else if (h.mtype == 4) {
-        const float3 dir = random_unit_vector(rng);
+        const float3 dir = random_unit_vector(rng, lb);
         st.o = add(h.pos, mul(dir, kRayEpsilon));
         st.d = dir;
         st.thr = mul(st.thr, h.base);
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
                     }
                     if (!deferred && bsdf_avail) {
                         int sss_event = 0, event = 0;
-                        keep = scatter<kPbr>(fp, h, &pm, bounce, rng, st, sss_event, event);
+                        keep = scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
                         if constexpr (kPbr) {
                             if (keep && sss_event != 0) update_subsurface(P, path, h, pm, sss_event);
                             if (fp.record_paths && event != 0) record_decision(P, fp, path, bounce, event << 2);
@@ -801,7 +801,7 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         restir_finish<kPbr>(ctx, P, cur, c, pixel % cam.width, pixel / cam.width, path, h, &pm, st.d, bsdf_avail,
             st.thr, r, P.res_meta[path], sh_o1, sh_d1, sh_c1);
         int sss_event = 0, event = 0;
-        const bool keep = bsdf_avail && scatter<kPbr>(fp, h, &pm, bounce, rng, st, sss_event, event);
+        const bool keep = bsdf_avail && scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
         if constexpr (kPbr) {
             if (keep && sss_event != 0) update_subsurface(P, path, h, pm, sss_event);
             if (fp.record_paths && event != 0) record_decision(P, fp, path, bounce, event << 2);

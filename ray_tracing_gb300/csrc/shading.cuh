@@ -533,7 +533,8 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
     int stack[kTraversalStack];
     int sp = 0;
     int node = 0;
-    for (int guard = 0; guard < (1 << 22); ++guard) {
+    int guard = 0;
+    for (; guard < s.bounds.traversal; ++guard) {
         const float4* np = reinterpret_cast<const float4*>(s.analytic_nodes + node);
         const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
         const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
@@ -551,6 +552,7 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
         if (h0 && h1) {
             const bool first0 = t0 <= t1;
             if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
+            else if (s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);  // a dropped subtree is reported
             node = first0 ? c0 : c1;
             continue;
         }
@@ -565,6 +567,7 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
         if (sp == 0) break;
         node = stack[--sp];
     }
+    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     t_hit = closest;
     return best;
 }
@@ -743,10 +746,10 @@ RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t&
     if (sel <= 0.0f) return smp;
     if (light.type == 3) {
         if (rcv.mtype == 4) {
-            smp.direction = random_unit_vector(rng);
+            smp.direction = random_unit_vector(rng, s.bounds);
             smp.pdf = sel * uniform_sphere_pdf();
         } else {
-            smp.direction = add(rcv.sn, random_unit_vector(rng));
+            smp.direction = add(rcv.sn, random_unit_vector(rng, s.bounds));
             if (near_zero(smp.direction)) smp.direction = rcv.sn;
             smp.direction = normalize(smp.direction);
             const float c = fmaxf(dot(rcv.sn, smp.direction), 0.0f);

@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(256) k_raygen(const FrameParams* __restrict__ 
         counters->rays[2] = 0;
         counters->rays[3] = 0;
         counters->restir_pixels = 0;
+        counters->gave_up = 0;
     }
 }
 

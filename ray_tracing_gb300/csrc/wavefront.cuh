@@ -61,7 +61,8 @@ struct Counters {
     unsigned long long rays[4];  // primary, extension, shadow, restir visibility
     int overflow;
     int denoise_error;                // a denoiser kernel's bounded wait ran out
-    int pad[2];
+    int gave_up;                      // this frame's loops that reached their bound (LoopBounds)
+    int pad;
     unsigned long long cum_rays[4];  // running totals since the counters were last cleared
     int bounce_active[64];           // paths entering each bounce of the last frame
     unsigned long long restir_pixels; // paths that ran ReSTIR DI in the last frame

@@ -39,13 +39,15 @@ class CameraFrame:
 
 class Renderer:
     def __init__(self, device: int = 0, use_cuda_graph: bool = True, debug_path_records: bool = False,
-                 stage_timing: bool = False, shade_order: int = 0):
+                 stage_timing: bool = False, shade_order: int = 0, debug_traversal_limit: int = 0,
+                 debug_rejection_limit: int = 0):
         self.lib = abi.load()
         missing = getattr(self.lib, "rtgb_missing_symbols", [])
         if missing:
             raise RuntimeError(f"librtgb.so lacks {missing}: rebuild with __graft_entry__.build()")
         self.h = C.c_void_p()
-        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records), int(stage_timing), int(shade_order))
+        info = abi.CreateInfo(device, int(use_cuda_graph), int(debug_path_records), int(stage_timing), int(shade_order),
+                              int(debug_traversal_limit), int(debug_rejection_limit))
         st = self.lib.rtgb_create(C.byref(info), C.byref(self.h))
         if st != abi.OK:
             raise abi.RtgbError(st, "rtgb_create failed (no CUDA device?)")
@@ -62,6 +64,12 @@ class Renderer:
             self.close()
         except Exception:
             pass
+
+    def __enter__(self) -> "Renderer":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
 
     def _check(self, st, what):
         abi.check(st, self.h, what)
@@ -104,6 +112,17 @@ class Renderer:
         n = C.c_int32()
         self._check(self.lib.rtgb_stage_times(self.h, buf, 256, C.byref(n)), "stage_times")
         return np.array(buf[: n.value], dtype=np.float64)
+
+    def set_debug_limits(self, traversal_limit: int = 0, rejection_limit: int = 0) -> None:
+        """rtgb_set_debug_limits: loop bounds of later frames (0 = default)."""
+        self._check(self.lib.rtgb_set_debug_limits(self.h, traversal_limit, rejection_limit), "set_debug_limits")
+
+    def launch_grids(self) -> list[int]:
+        """rtgb_launch_grids: the grid size of every wavefront launch slot in use."""
+        buf = (C.c_int32 * 64)()
+        n = C.c_int32()
+        self._check(self.lib.rtgb_launch_grids(self.h, buf, 64, C.byref(n)), "launch_grids")
+        return list(buf)[: n.value]
 
     def autotune_launches(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int,
                           frames: int = 4) -> dict:

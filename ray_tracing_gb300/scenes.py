@@ -44,6 +44,12 @@ class HostScene:
             self.lib.rtgb_host_scene_destroy(self.ptr)
             self.ptr = C.c_void_p()
 
+    def __enter__(self) -> "HostScene":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
     def __del__(self):
         try:
             self.close()

@@ -18,6 +18,7 @@ from __future__ import annotations
 
 import ctypes as C
 import hashlib
+import os
 import sys
 from pathlib import Path
 
@@ -175,7 +176,9 @@ def run(lib_path: Path, symbol: str, inputs: np.ndarray) -> np.ndarray:
 
 def main() -> None:
     ref_lib = ROOT / "oracle" / "_ref" / "libopenpbr_ref.so"
-    header = Path("/root/reference/src/common/openpbr_core.h")
+    # the reference checkout: first argument, else RTGB_REFERENCE_ROOT (as oracle/build_ref.py)
+    root = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ["RTGB_REFERENCE_ROOT"])
+    header = root / "src" / "common" / "openpbr_core.h"
     inputs = make_inputs()
     outputs = run(ref_lib, "ref_openpbr_kat", inputs)
     OUT.mkdir(exist_ok=True)

@@ -7,11 +7,13 @@ recorded in the reference's manifest before it is copied.
 """
 import hashlib
 import json
+import os
 import shutil
 import sys
 from pathlib import Path
 
-SRC = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference") / "tests/references/restir_di"
+# the reference checkout: first argument, else RTGB_REFERENCE_ROOT (as oracle/build_ref.py)
+SRC = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ["RTGB_REFERENCE_ROOT"]) / "tests/references/restir_di"
 DST = Path(__file__).resolve().parent / "restir_di"
 
 manifest = json.loads((SRC / "manifest.json").read_text())

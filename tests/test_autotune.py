@@ -44,3 +44,28 @@ def test_tuned_grids_trace_the_same_paths():
         assert np.array_equal(pr, tr)
     plain.close()
     tuned.close()
+
+
+def test_a_failed_tuning_leaves_the_handle_as_it_was():
+    """A render that fails inside the tuner (here a profile the request
+    validation refuses) must not leave a candidate's grids or the tuner's
+    stage events in force: the handle keeps the grids it had, stage timing is
+    off again, and the next frame renders."""
+    from ray_tracing_gb300.renderer import Renderer
+    sc = scenes.HostScene("random_spheres", detail=64)
+    rig = scaled_rig(scenes.default_rig("random_spheres", 2), 0.2)
+    good = scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0)
+    bad = scenes.profile("balanced", samples_per_pixel=5000, max_bounces=4, enable_denoise=0)
+    r = Renderer()
+    r.prepare_scene(sc.view)
+    before = r.launch_grids()
+    assert len(before) == 13 and min(before) > 0
+    with pytest.raises(abi.RtgbError):
+        r.autotune_launches(rig, bad, 2, frames=1)
+    assert r.launch_grids() == before
+    r.render_frame(rig, good, 2)
+    with pytest.raises(abi.RtgbError):
+        r.stage_times()
+    tuned = r.autotune_launches(rig, good, 2, frames=1)
+    assert r.launch_grids() != before or all(v == 1.0 for v in tuned["chosen"].values())
+    r.close()

@@ -34,6 +34,11 @@ int main(int argc, char** argv) {
     }
     EXPECT(threw, "other statuses map to std::runtime_error");
     threw = false;
+    try { rtgb::detail::check_request(RTGB_INVALID_ARGUMENT, nullptr, "r"); } catch (const std::runtime_error& e) {
+        threw = std::string(e.what()) == "r";
+    }
+    EXPECT(threw, "a rejected render request is std::runtime_error, as validate_render_pool_request throws");
+    threw = false;
     try { rtgb::RendererPool pool(5); } catch (const std::runtime_error& e) {
         threw = std::string(e.what()) == "RendererPool requires renderer_count in [1, 4]";
     }
@@ -61,7 +66,7 @@ int main(int argc, char** argv) {
         EXPECT(frames[0].frame.width == 64 && frames[0].frame.beauty_rgba.size() == 64 * 64 * 4, "frame shape");
         EXPECT(frames[0].frame.average_luminance > 0.0 && frames[0].timing.render_ms > 0.0, "luminance and timing");
         threw = false;
-        try { (void)pool.render_frame(rig, prof, 3); } catch (const std::invalid_argument&) { threw = true; }
+        try { (void)pool.render_frame(rig, prof, 3); } catch (const std::runtime_error&) { threw = true; }
         EXPECT(threw, "more active cameras than the pool holds");
         rtgb_host_scene_destroy(hs);
     }
