@@ -438,7 +438,7 @@ def gpu_frames(sc, rig, prof, cameras, warmup, frames):
     return prep_ms, ms / frames, rays / (ms * 1e-3) / 1e6
 
 
-def workload_records(names=("c1", "c3", "c5", "smoke", "c4"), c3_steps=10, c3_warmup=3):
+def workload_records(names=("c1", "c3", "c5", "smoke", "c4"), steps=None, warmup=None):
     """The other configurations of the reference protocol, measured beside the
     headline one: C1 (Cornell box 256 x 256, 64 spp, depth 8; the CPU oracle
     on all host threads renders the same full frame), C3 (1 M triangles with
@@ -450,10 +450,12 @@ def workload_records(names=("c1", "c3", "c5", "smoke", "c4"), c3_steps=10, c3_wa
     inference size. Each record is measured on its own: one that fails is
     reported as {"error": ...} and the others stand."""
     out = {}
+    frames = {} if steps is None else {"steps": steps, "warmup": warmup if warmup is not None else 3}
     jobs = {
         "c1": ("C1_cornell_256x256_64spp_d8", c1_record),
-        "c3": ("C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280", lambda: c3_record(c3_steps, c3_warmup)),
-        "c5": ("C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6", c5_record),
+        "c3": ("C3_terrain_1Mtri_openpbr_2pinhole640_2equi1280", lambda: c3_record(**frames)),
+        "c5": ("C5_room_4Mtri_textured_openpbr_4x1920x1080_orbit60_d6",
+               lambda: c5_record(frames=frames["steps"], warmup=frames["warmup"]) if frames else c5_record()),
         "smoke": ("published_protocol_smoke_realtime_4x640x480", smoke_record),
         "c4": ("C4_denoiser_inference_4x1280x720", c4_inference_record),
     }
@@ -546,6 +548,8 @@ def c4_inference_record(frames=20, warmup=3):
 
 
 C5_EVAL_FRAMES = (0, 30, 59)
+C5_SIZE = (0, 0)            # camera size override (0: the rig's 1920x1080), for profiling a smaller case
+C5_RELMSE = True            # the equal-relMSE comparison of c5_record (bench.py --no-relmse turns it off)
 
 
 def c5_record(frames=60, warmup=3, degrees_per_frame=2.0, relmse_eval=True):
@@ -564,8 +568,9 @@ def c5_record(frames=60, warmup=3, degrees_per_frame=2.0, relmse_eval=True):
     prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=1 if weights is not None else 0,
                           enable_restir_di=1, restir_initial_candidates=32, restir_temporal_reuse=1,
                           restir_spatial_neighbors=1)
+    relmse_eval = relmse_eval and C5_RELMSE
     with scenes.HostScene("textured_room") as sc:
-        rig = scenes.default_rig("textured_room", 4)
+        rig = scenes.default_rig("textured_room", 4, *C5_SIZE)
         with Renderer(stage_timing=True) as r:
             t0 = time.perf_counter()
             r.prepare_scene(sc.view)
@@ -931,6 +936,7 @@ def main():
                          "fisheye cameras at 1920x1080")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
+    ap.add_argument("--c5-size", default=None, help="WxH of the C5 cameras (default 1920x1080; for profiling)")
     ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke", "c4"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
@@ -938,6 +944,11 @@ def main():
         args.warmup = 3
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    global C5_SIZE, C5_RELMSE
+    if args.c5_size:
+        w, h = (int(v) for v in args.c5_size.lower().split("x"))
+        C5_SIZE = (w, h)
+    C5_RELMSE = not args.no_relmse
     if args.workload is not None:
         if rank == 0:
             print(json.dumps({"workloads": workload_records((args.workload,), args.steps, args.warmup)}), flush=True)

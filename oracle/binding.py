@@ -31,6 +31,7 @@ _SIGS = {
     "orc_last_rays": (C.c_uint64, [C.c_void_p, C.c_int]),
     "orc_direction_debug": (C.c_int, [P(abi.Camera), C.c_void_p]),
     "orc_unproject": (None, [P(abi.Camera), C.c_double, C.c_double, P(C.c_float)]),
+    "orc_noise_sinf": (C.c_float, [C.c_float]),
     "orc_project": (None, [P(abi.Camera), P(C.c_float), P(C.c_float)]),
     "orc_reservoir_update": (C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int,
                                        C.c_float]),

@@ -22,6 +22,7 @@
 // Compiled with -ffp-contract=off; multi-draw RNG calls evaluate left to right.
 #include "../include/rtgb.h"
 #include "oracle_math.h"
+#include "noise_sin.h"
 #include "openpbr.h"
 
 #include <algorithm>
@@ -354,8 +355,11 @@ void sphere_uv(const V3& p, float& u, float& v) {
     v = theta / kPi;
 }
 
+// programs.cu:184-209. The sine is rtgb_noise::noise_sinf, the one the
+// kernels use: the hash multiplies sin by 43758, so two correct sines that
+// differ in the last bit (CUDA's and glibc's) give different noise.
 float hash_noise(const V3& p) {
-    const float n = std::sin(dot(p, V3{12.9898f, 78.233f, 37.719f})) * 43758.5453f;
+    const float n = rtgb_noise::noise_sinf(dot(p, V3{12.9898f, 78.233f, 37.719f})) * 43758.5453f;
     return fractf(n) * 2.0f - 1.0f;
 }
 
@@ -433,7 +437,7 @@ V3 eval_texture(const Scene& s, int index, float u, float v, const V3& p) {
         if (t.type == 2) return sample_image(s, t, u, v);
         if (t.type == 3) {
             const float turb = turbulence(p);
-            const float value = 0.5f * (1.0f + std::sin(t.scale * p.z + 10.0f * turb));
+            const float value = 0.5f * (1.0f + rtgb_noise::noise_sinf(t.scale * p.z + 10.0f * turb));
             return {value, value, value};
         }
         return {1, 0, 1};
@@ -2206,6 +2210,8 @@ int orc_direction_debug(const rtgb_camera* cam, uint8_t* rgba) {
 }
 
 // Camera-space direction of a pixel (unproject), and projection, for KATs.
+float orc_noise_sinf(float x) { return rtgb_noise::noise_sinf(x); }
+
 void orc_unproject(const rtgb_camera* cam, double px, double py, float out[3]) {
     const orc::Camera c = orc::make_camera(*cam);
     const orc::V3 d = orc::unproject(c, px, py);

@@ -10,6 +10,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "rtgb.h"
@@ -295,6 +296,117 @@ RTGB_HD MergeResult reservoir_merge(Reservoir& cur, const Reservoir& prev, float
         cur.spatial_candidate_count += m;
     }
     return MergeResult{m, sel ? 1 : 0};
+}
+
+// ---- reservoirs in HBM ----------------------------------------------------------
+//
+// A frame reservoir is stored as 96 bytes on a 32-byte boundary, three DRAM
+// sectors ordered by which pass reads them, instead of the 84-byte record the
+// algebra above works on:
+//   sector 0 (q[0], q[1]) surface: position xyz, normal xyz, primitive index,
+//            material type and primitive type (8 bits each, sign-extended)
+//   sector 1 (q[2], q[3]) sample: selected light, u0, u1, valid; age,
+//            candidate count, estimator weight, (spare)
+//   sector 2 (q[4], q[5]) sums: weight sum, selected target, temporal,
+//            spatial and bias-correction source counts, (spare)
+// A temporal or spatial reuse reads sectors 0 and 1 (surface_valid and
+// reservoir_merge read nothing else), a bias-correction ray sector 0, the
+// finalisation sectors 1 and 2. All-zero bits decode to zero_reservoir().
+struct alignas(32) ReservoirRec {
+    float4 q[6];
+};
+static_assert(sizeof(ReservoirRec) == 96, "ReservoirRec layout");
+
+// Bit casts usable on the host (the record is converted there for downloads).
+RTGB_HD float bits_f(int v) {
+    float f;
+    memcpy(&f, &v, sizeof f);
+    return f;
+}
+RTGB_HD int bits_i(float v) {
+    int i;
+    memcpy(&i, &v, sizeof i);
+    return i;
+}
+
+RTGB_HD int pack_types(int material_type, int primitive_type) {
+    return (material_type & 0xff) | ((primitive_type & 0xff) << 8);
+}
+RTGB_HD int unpack_type(int packed, int shift) {
+    return static_cast<int>(static_cast<signed char>((packed >> shift) & 0xff));
+}
+
+RTGB_HD void pack_surface(const Surface& s, float4& a, float4& b) {
+    a = make_float4(s.position[0], s.position[1], s.position[2], s.normal[0]);
+    b = make_float4(s.normal[1], s.normal[2], bits_f(s.primitive_index),
+        bits_f(pack_types(s.material_type, s.primitive_type)));
+}
+RTGB_HD Surface unpack_surface(const float4& a, const float4& b) {
+    Surface s;
+    s.position[0] = a.x;
+    s.position[1] = a.y;
+    s.position[2] = a.z;
+    s.normal[0] = a.w;
+    s.normal[1] = b.x;
+    s.normal[2] = b.y;
+    s.primitive_index = bits_i(b.z);
+    const int t = bits_i(b.w);
+    s.material_type = unpack_type(t, 0);
+    s.primitive_type = unpack_type(t, 8);
+    return s;
+}
+
+RTGB_HD void pack_sample(const Reservoir& r, float4& a, float4& b) {
+    a = make_float4(bits_f(r.selected.light_index), r.selected.u0, r.selected.u1, bits_f(r.valid));
+    b = make_float4(bits_f(r.age), bits_f(r.candidate_count), r.estimator_weight, 0.0f);
+}
+RTGB_HD void unpack_sample(const float4& a, const float4& b, Reservoir& r) {
+    r.selected.light_index = bits_i(a.x);
+    r.selected.u0 = a.y;
+    r.selected.u1 = a.z;
+    r.valid = bits_i(a.w);
+    r.age = bits_i(b.x);
+    r.candidate_count = bits_i(b.y);
+    r.estimator_weight = b.z;
+}
+
+RTGB_HD void pack_sums(const Reservoir& r, float4& a, float4& b) {
+    a = make_float4(r.weight_sum, r.selected_target, bits_f(r.temporal_candidate_count),
+        bits_f(r.spatial_candidate_count));
+    b = make_float4(bits_f(r.bias_correction_source_count), 0.0f, 0.0f, 0.0f);
+}
+RTGB_HD void unpack_sums(const float4& a, const float4& b, Reservoir& r) {
+    r.weight_sum = a.x;
+    r.selected_target = a.y;
+    r.temporal_candidate_count = bits_i(a.z);
+    r.spatial_candidate_count = bits_i(a.w);
+    r.bias_correction_source_count = bits_i(b.x);
+}
+
+RTGB_HD void store_reservoir(ReservoirRec* p, const Reservoir& r) {
+    float4 q[6];
+    pack_surface(r.surface, q[0], q[1]);
+    pack_sample(r, q[2], q[3]);
+    pack_sums(r, q[4], q[5]);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) p->q[k] = q[k];
+}
+
+RTGB_HD Reservoir load_reservoir(const ReservoirRec* p) {
+    Reservoir r;
+    r.surface = unpack_surface(p->q[0], p->q[1]);
+    unpack_sample(p->q[2], p->q[3], r);
+    unpack_sums(p->q[4], p->q[5], r);
+    return r;
+}
+
+// The fields a temporal or spatial reuse reads (sectors 0 and 1); the sums
+// are left zero (surface_valid and reservoir_merge do not read them).
+RTGB_HD Reservoir load_reuse(const ReservoirRec* p) {
+    Reservoir r = zero_reservoir();
+    r.surface = unpack_surface(p->q[0], p->q[1]);
+    unpack_sample(p->q[2], p->q[3], r);
+    return r;
 }
 
 // ---- device scene ------------------------------------------------------------
@@ -707,8 +819,9 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
     int sp = 0;
     int node = 0;
     const float kInf = __int_as_float(0x7f800000);
+    const int limit = s.bounds.traversal;
     int guard = 0;
-    for (; guard < s.bounds.traversal; ++guard) {
+    for (; guard < limit; ++guard) {
         float4 q[kNode4];
         load_node4(s, staged, staged_count, node, q);
         float t0 = kInf, t1 = kInf, t2 = kInf, t3 = kInf;
@@ -753,7 +866,7 @@ RTGB_D int traverse_closest(const DeviceScene& s, const float3& o, const float3&
         if (sp == 0) break;
         node = stack[--sp];
     }
-    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
+    if (guard >= limit && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     return best;
 }
 
@@ -771,8 +884,9 @@ RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d,
     int stack[kTraversalStack];
     int sp = 0;
     int node = 0;
+    const int limit = s.bounds.traversal;
     int guard = 0;
-    for (; guard < s.bounds.traversal; ++guard) {
+    for (; guard < limit; ++guard) {
         float4 q[kNode4];
         load_node4(s, staged, staged_count, node, q);
         int next = -1;
@@ -803,7 +917,7 @@ RTGB_D bool traverse_any(const DeviceScene& s, const float3& o, const float3& d,
         if (sp == 0) break;
         node = stack[--sp];
     }
-    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
+    if (guard >= limit && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     return false;
 }
 

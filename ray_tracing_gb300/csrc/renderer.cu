@@ -778,8 +778,8 @@ struct rtgb_renderer {
     }
 
     void ensure_frames(long long pixels) {
-        // beauty, normal, dnormal, albedo float4; depth, trust float; flow float2; reservoir 84 B
-        const size_t per = 4 * 16 + 4 + 4 + 8 + sizeof(Reservoir);
+        // beauty, normal, dnormal, albedo float4; depth, trust float; flow float2; reservoir record 96 B
+        const size_t per = 4 * 16 + 4 + 4 + 8 + sizeof(ReservoirRec);
         for (int f = 0; f < 2; ++f) {
             if (frame_mem[f].bytes >= static_cast<size_t>(pixels) * per + 2048 && frame_mem[f].p) continue;
             drop_graph();
@@ -797,7 +797,7 @@ struct rtgb_renderer {
             b.depth = reinterpret_cast<float*>(take(pixels * 4));
             b.flow = reinterpret_cast<float2*>(take(pixels * 8));
             b.trust = reinterpret_cast<float*>(take(pixels * 4));
-            b.reservoirs = reinterpret_cast<Reservoir*>(take(pixels * sizeof(Reservoir)));
+            b.reservoirs = reinterpret_cast<ReservoirRec*>(take(pixels * sizeof(ReservoirRec)));
         }
     }
 
@@ -811,9 +811,9 @@ struct rtgb_renderer {
         const size_t src2 = sz(static_cast<size_t>(n) * 8 * kMaxReuseSources);
         const size_t src1 = sz(static_cast<size_t>(n) * 4 * kMaxReuseSources);
         const size_t bins = sz(static_cast<size_t>(kSortBins) * 4);
-        size_t total = f4 * 17 + i2 + i1 * 10 + src2 + 2 * src1 + 2 * bins;
+        size_t total = f4 * 17 + i2 + i1 * 11 + src2 + 2 * src1 + 2 * bins;
         const bool scratch = true;
-        if (scratch) total += sz(static_cast<size_t>(n) * sizeof(Reservoir));
+        if (scratch) total += sz(static_cast<size_t>(n) * sizeof(ReservoirRec));
         if (need_records) total += sz(static_cast<size_t>(n) * 4 * bounces);
         char* p = static_cast<char*>(path_mem.ensure(total));
         auto take = [&](size_t b) {
@@ -852,10 +852,11 @@ struct rtgb_renderer {
         P.vis_queue = reinterpret_cast<int*>(take(src1));
         P.sort_key = reinterpret_cast<int*>(take(i1));
         P.sorted = reinterpret_cast<int*>(take(i1));
+        P.scatter_queue = reinterpret_cast<int*>(take(i1));
         P.sort_hist = reinterpret_cast<int*>(take(bins));
         P.sort_cursor = reinterpret_cast<int*>(take(bins));
         RTGB_CHECK(cudaMemsetAsync(P.sort_hist, 0, bins, stream));  // k_sort_scan re-zeroes it after each use
-        P.res_scratch = reinterpret_cast<Reservoir*>(take(sz(static_cast<size_t>(n) * sizeof(Reservoir))));
+        P.res_scratch = reinterpret_cast<ReservoirRec*>(take(sz(static_cast<size_t>(n) * sizeof(ReservoirRec))));
         P.codes = need_records ? reinterpret_cast<int*>(take(sz(static_cast<size_t>(n) * 4 * bounces))) : nullptr;
         paths = P;
         path_capacity = n;
@@ -959,7 +960,7 @@ struct rtgb_renderer {
             launch_reset_counters(d_counters, b, stream);
             const bool pbr_scene = scene.openpbr_count > 0;
             if (h_fp.sort_from_bounce <= b) launch_shade_sort(d_fp, scene, paths, d_counters, b, sh[1].grid, stream);
-            launch_shade(d_fp, scene, paths, d_counters, b, sh[pbr_scene ? 7 : 2], stream);
+            launch_shade(d_fp, scene, paths, d_counters, b, sh[pbr_scene ? 7 : 2], sh[13], stream);
             if (b == 0) launch_restir(d_fp, scene, paths, d_counters, sh, stream);
             mark(k);
             launch_shadow(d_fp, scene, paths, d_counters, b, sh[3], stream);
@@ -1242,7 +1243,18 @@ struct rtgb_renderer {
             case 4: src = f.depth + o; need = n * 4; break;
             case 5: src = f.flow + o; need = n * 8; break;
             case 6: src = f.trust + o; need = n * 4; break;
-            case 7: src = f.reservoirs + o; need = n * sizeof(Reservoir); break;
+            case 7: {
+                // the reference's 84-byte RestirReservoir records, converted from the device records
+                need = n * sizeof(Reservoir);
+                if (bytes != need) throw Invalid{"buffer size mismatch: expected " + std::to_string(need) + " bytes"};
+                std::vector<ReservoirRec> recs(n);
+                RTGB_CHECK(cudaMemcpyAsync(recs.data(), f.reservoirs + o, n * sizeof(ReservoirRec),
+                    cudaMemcpyDeviceToHost, stream));
+                RTGB_CHECK(cudaStreamSynchronize(stream));
+                Reservoir* out = static_cast<Reservoir*>(host);
+                for (size_t i = 0; i < n; ++i) out[i] = load_reservoir(&recs[i]);
+                return;
+            }
             case 8:
                 if (!last_denoised) throw Invalid{"the last frame was not denoised"};
                 src = denoised.as<float4>() + o;
@@ -1396,7 +1408,7 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         constexpr int kCandidates = RTGB_TUNE_CANDIDATES;
         constexpr float kScales[kCandidates] = {0.5f, 1.0f, 2.0f, 4.0f};
         // shape slots of each stage group (rtgb_launch_tuning::group_ms order)
-        static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1}, {2, 6, 7, 8, 9, 10, 11, 12}, {3}, {4, 5}};
+        static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1}, {2, 6, 7, 8, 9, 10, 11, 12, 13}, {3}, {4, 5}};
         *out = rtgb_launch_tuning {};
         LaunchShape base[kLaunchShapes];
         query_launch_shapes(h->sm_count, base);

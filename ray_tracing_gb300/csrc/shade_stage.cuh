@@ -154,17 +154,18 @@ RTGB_D float target_at_previous(ShadeCtx& ctx, int c, const Surface& src, const 
     return t;
 }
 
-RTGB_D Surface load_surface(const Reservoir* r) {
-    Surface s;
-    const Surface* p = &r->surface;
-    for (int k = 0; k < 3; ++k) {
-        s.position[k] = p->position[k];
-        s.normal[k] = p->normal[k];
-    }
-    s.material_type = p->material_type;
-    s.primitive_type = p->primitive_type;
-    s.primitive_index = p->primitive_index;
-    return s;
+// The surface of a stored reservoir (its first sector).
+RTGB_D Surface load_surface(const ReservoirRec* r) { return unpack_surface(r->q[0], r->q[1]); }
+
+// Where a bounce-0 path's reservoir lives during the frame: in its pixel's
+// frame record when there is one sample per pixel (written by k_restir_ris,
+// finalised in place by k_restir), else in the path's scratch record, which
+// k_finalize copies into the frame for the pixel's last ReSTIR sample.
+RTGB_D ReservoirRec* reservoir_slot(const FrameParams& fp, const Paths& P, const FrameBufs& cur, int c,
+    long long path) {
+    const CameraDev& cam = fp.cam[c];
+    if (fp.spp == 1) return cur.reservoirs + cam.pixel_offset + (path - cam.path_offset);
+    return P.res_scratch + path;
 }
 
 // ---- ReSTIR DI (accumulate_restir_analytic_direct_light, programs.cu:2315-2449) ----
@@ -268,7 +269,7 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
     canonical = r.candidate_count;
     nsrc = 0;
     selected_src = -1;
-    const Reservoir* hres = hist.reservoirs + cam.pixel_offset;
+    const ReservoirRec* hres = hist.reservoirs + cam.pixel_offset;
     const Surface cur_surface = restir_surface(h);
     const int nbrs = fp.restir_spatial < 8 ? fp.restir_spatial : 8;
     int reproj = -1;
@@ -276,7 +277,7 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
     // same hit into the same previous camera; the projection runs once.
     const bool have_prev = (fp.restir_temporal != 0 || nbrs > 0) && previous_pixel(fp, c, h, reproj);
     if (fp.restir_temporal != 0 && have_prev) {
-        const Reservoir prev = hres[reproj];
+        const Reservoir prev = load_reuse(hres + reproj);
         const float tol = fmaxf(0.005f, 0.01f * h.t);
         if (surface_valid(cur_surface, prev, tol, 0.95f, fp.restir_max_age)) {
             const LightSample l = analytic_candidate(s, h.pos, prev.selected.light_index, prev.selected.u0,
@@ -302,7 +303,7 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
             const int nx = reproj % cam.width + dx, ny = reproj / cam.width + dy;
             if (nx < 0 || nx >= cam.width || ny < 0 || ny >= cam.height) continue;
             const int ni = ny * cam.width + nx;
-            const Reservoir prev = hres[ni];
+            const Reservoir prev = load_reuse(hres + ni);
             const float tol = fmaxf(0.01f, 0.02f * h.t);
             if (!surface_valid(cur_surface, prev, tol, 0.95f, fp.restir_max_age)) continue;
             const LightSample l = analytic_candidate(s, h.pos, prev.selected.light_index, prev.selected.u0,
@@ -324,15 +325,18 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
 // Bias correction, reservoir store and the selected sample's shadow query
 // (programs.cu:2400-2449) from the parked reservoir and the source targets.
 template <bool kPbr>
-RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, int c, int x, int y, long long path,
-    const Hit& h, const pbr::Mat* pm, const float3& ray_d, bool bsdf_avail, const float3& thr, Reservoir& r, int meta,
-    float4& sh_o, float4& sh_d, float4& sh_c) {
+RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, ReservoirRec* slot, long long path, const Hit& h,
+    const pbr::Mat* pm, const float3& ray_d, bool bsdf_avail, const float3& thr, int meta, float4& sh_o, float4& sh_d,
+    float4& sh_c) {
     const FrameParams& fp = ctx.fp;
     const DeviceScene& s = ctx.s;
-    const CameraDev& cam = fp.cam[c];
     const int nsrc = meta & 0xff;
     const int selected_src = ((meta >> 8) & 0xff) - 1;
     const int canonical = meta >> 16;
+    // the parked reservoir's sample and sums (its surface sector stays as written)
+    Reservoir r = zero_reservoir();
+    unpack_sample(slot->q[2], slot->q[3], r);
+    unpack_sums(slot->q[4], slot->q[5], r);
     if (fp.restir_bias == 1 && nsrc > 0 && r.valid != 0) {
         float sel_t = r.selected_target;
         float sum = r.selected_target * static_cast<float>(canonical);
@@ -345,12 +349,12 @@ RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, int c, 
     } else {
         reservoir_finalize(r);
     }
-    if (fp.spp == 1) {
-        cur.reservoirs[cam.pixel_offset + y * cam.width + x] = r;
-    } else {
-        P.res_scratch[path] = r;
-        P.res_written[path] = 1;
-    }
+    float4 q[4];
+    pack_sample(r, q[0], q[1]);
+    pack_sums(r, q[2], q[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) slot->q[2 + k] = q[k];
+    if (fp.spp != 1) P.res_written[path] = 1;
     if (r.valid == 0) return;
     const LightSample l = analytic_candidate(s, h.pos, r.selected.light_index, r.selected.u0, r.selected.u1);
     float t = 0.0f;
@@ -361,6 +365,27 @@ RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, FrameBufs& cur, int c, 
     sh_o = f4(add(h.pos, mul(l.direction, kRayEpsilon * 2.0f)), max_t);
     sh_d = f4(l.direction, 0.0f);
     sh_c = f4(mul(thr, mul(num, r.estimator_weight)), 1.0f);
+}
+
+// The ray and throughput of a queued path, without the previous-scatter
+// record and radiance: for the ReSTIR passes, which rebuild the hit and (in
+// k_restir) scatter, and scatter rewrites every previous-scatter field before
+// store_path writes them.
+RTGB_D void load_ray(const Paths& P, int path, PathRegs& st) {
+    st.o = xyz(P.ray_o[path]);
+    st.d = xyz(P.ray_d[path]);
+    const float4 thr4 = P.thr[path];
+    st.thr = xyz(thr4);
+    st.prev_pdf = thr4.w;
+    st.rad = f3(0.0f, 0.0f, 0.0f);
+    st.prev_pos = f3(0.0f, 0.0f, 0.0f);
+    st.prev_nrm = f3(0.0f, 0.0f, 0.0f);
+    st.prev_valid = false;
+    st.prev_delta = false;
+    st.prev_mtype = -1;
+    st.prev_ptype = -1;
+    st.prev_pidx = -1;
+    st.alive = true;
 }
 
 RTGB_D void load_path(const Paths& P, int path, PathRegs& st) {
@@ -539,9 +564,12 @@ RTGB_D int subsurface_step(const Paths& P, int path, int sss, const Hit& h, uint
 // One bounce of radiance_kernel's loop body (programs.cu:1855-1932) per path.
 // At the ReSTIR bounce, surfaces that run ReSTIR DI stop after the
 // emissive-geometry NEE and continue in k_restir, which consumes the RNG
-// stream from exactly this point.
-template <bool kPbr>
-__global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+// stream from exactly this point. With kSplit (the OpenPBR instance) every
+// path stops there: the ones that scatter are queued for k_scatter, which
+// samples the BSDF from the same RNG state, so each kernel carries only half
+// of the OpenPBR code (evaluation here, sampling there) and fewer registers.
+template <bool kPbr, bool kSplit = false>
+__global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
     const FrameParams& fp = *fpp;
     const int in = bounce & 1;
@@ -566,6 +594,8 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
         sh_c[1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         bool keep = false;
         bool deferred = false;
+        bool to_scatter = false;
+        bool thr_changed = false;
         if (alight >= 0) {
             AnalyticHit ah;
             ah.hit = hit_analytic_at(s, alight, st.o, st.d, kRayEpsilon, kRayFar, ah);
@@ -584,7 +614,10 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
                 int walk = 0;
                 if constexpr (kPbr) {
                     const int sss = P.sss_mat[path];
-                    if (sss >= 0) walk = subsurface_step(P, path, sss, h, rng, st);
+                    if (sss >= 0) {
+                        walk = subsurface_step(P, path, sss, h, rng, st);
+                        thr_changed = true;
+                    }
                 }
                 if (walk == 2) {
                     keep = bounce + 1 < fp.max_bounces;
@@ -645,11 +678,15 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
                         }
                     }
                     if (!deferred && bsdf_avail) {
-                        int sss_event = 0, event = 0;
-                        keep = scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
-                        if constexpr (kPbr) {
-                            if (keep && sss_event != 0) update_subsurface(P, path, h, pm, sss_event);
-                            if (fp.record_paths && event != 0) record_decision(P, fp, path, bounce, event << 2);
+                        if constexpr (kSplit) {
+                            to_scatter = true;
+                        } else {
+                            int sss_event = 0, event = 0;
+                            keep = scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
+                            if constexpr (kPbr) {
+                                if (keep && sss_event != 0) update_subsurface(P, path, h, pm, sss_event);
+                                if (fp.record_paths && event != 0) record_decision(P, fp, path, bounce, event << 2);
+                            }
                         }
                     }
                 }
@@ -658,6 +695,8 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
         P.rad[path] = f4(st.rad, 0.0f);
         P.rng[path] = rng;
         if (keep) store_path(P, path, st);
+        // the random walk scaled the throughput k_scatter starts from
+        if (kSplit && to_scatter && thr_changed) P.thr[path] = f4(st.thr, st.prev_pdf);
         if (deferred) {
             // slot 0 travels to k_restir, which adds slot 1 and queues the shadow rays
             P.sh_c[0][path] = sh_c[0];
@@ -678,6 +717,40 @@ __global__ void __launch_bounds__(128) k_shade(const FrameParams* __restrict__ f
         }
         queue_push(P.queue[out], &counters->active[out], path, keep);
         queue_push(P.restir_queue, &counters->restir, path, deferred);
+        if constexpr (kSplit) queue_push(P.scatter_queue, &counters->scatter, path, to_scatter);
+    }
+}
+
+// BSDF sampling and Russian roulette (sample_bsdf, programs.cu:2463-2565;
+// apply_russian_roulette, :1764-1771) of the paths k_shade<kPbr, true> queued,
+// continuing their RNG stream where the next-event estimation left it.
+template <bool kPbr>
+__global__ void __launch_bounds__(128, 4) k_scatter(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+    Counters* counters, int bounce) {
+    const FrameParams& fp = *fpp;
+    const int out = (bounce & 1) ^ 1;
+    const int count = counters->scatter;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int path = P.scatter_queue[i];
+        const float4 hr = P.hit[path];
+        PathRegs st;
+        load_ray(P, path, st);
+        uint32_t rng = P.rng[path];
+        Hit h;
+        rebuild_hit<kPbr>(s, hr, st, h);  // rebuilt in k_shade from the same record
+        pbr::Mat pm;
+        if constexpr (kPbr) {
+            if (h.mtype == 5) openpbr_scattering(s, h, pm);
+        }
+        int sss_event = 0, event = 0;
+        const bool keep = scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
+        if constexpr (kPbr) {
+            if (keep && sss_event != 0) update_subsurface(P, path, h, pm, sss_event);
+            if (fp.record_paths && event != 0) record_decision(P, fp, path, bounce, event << 2);
+        }
+        P.rng[path] = rng;
+        if (keep) store_path(P, path, st);
+        queue_push(P.queue[out], &counters->active[out], path, keep);
     }
 }
 
@@ -719,7 +792,7 @@ __global__ void __launch_bounds__(128, 6) k_restir_ris(const FrameParams* __rest
         const int path = P.restir_queue[i];
         const float4 hr = P.hit[path];
         PathRegs st;
-        load_path(P, path, st);
+        load_ray(P, path, st);
         uint32_t rng = P.rng[path];
         Hit h;
         rebuild_hit<kPbr>(s, hr, st, h);
@@ -735,7 +808,7 @@ __global__ void __launch_bounds__(128, 6) k_restir_ris(const FrameParams* __rest
         int nsrc = 0, selected_src = -1, canonical = 0;
         restir_gather<kPbr>(ctx, hist, sh.guide, c, pixel % cam.width, pixel / cam.width, h, &pm, st.d, rng,
             bsdf_avail, st.thr, r, src_index, mult, nsrc, selected_src, canonical);
-        P.res_scratch[path] = r;
+        store_reservoir(reservoir_slot(fp, P, fp.cur, c, path), r);
         P.rng[path] = rng;
         P.res_meta[path] = pack_meta(nsrc, selected_src, canonical);
         for (int k = 0; k < nsrc; ++k) P.res_src[static_cast<long long>(path) * kMaxSources + k] = make_int2(src_index[k], mult[k]);
@@ -761,8 +834,9 @@ __global__ void __launch_bounds__(128) k_restir_vis(const FrameParams* __restric
         const int k = item & 15;
         const int c = camera_of_path(fp, path);
         const long long slot = static_cast<long long>(path) * kMaxSources + k;
-        const Reservoir* hres = hist.reservoirs + fp.cam[c].pixel_offset;
-        const Candidate sel = P.res_scratch[path].selected;
+        const ReservoirRec* hres = hist.reservoirs + fp.cam[c].pixel_offset;
+        const float4 sq = reservoir_slot(fp, P, fp.cur, c, path)->q[2];
+        const Candidate sel{__float_as_int(sq.x), sq.y, sq.z};
         P.res_src_t[slot] = target_at_previous<kPbr>(ctx, c, load_surface(hres + P.res_src[slot].x), sel, bsdf_avail);
     }
     count_add(&counters->rays[3], ctx.vis_rays);
@@ -783,7 +857,7 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         const int path = P.restir_queue[i];
         const float4 hr = P.hit[path];
         PathRegs st;
-        load_path(P, path, st);
+        load_ray(P, path, st);
         uint32_t rng = P.rng[path];
         Hit h;
         rebuild_hit<kPbr>(s, hr, st, h);
@@ -793,13 +867,10 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         }
         const bool bsdf_avail = bounce + 1 < fp.max_bounces;
         const int c = camera_of_path(fp, path);
-        const CameraDev& cam = fp.cam[c];
-        const int pixel = static_cast<int>((path - cam.path_offset) / fp.spp);
         float4 sh_o1, sh_d1, sh_c1 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        Reservoir r = P.res_scratch[path];
         ++runs;
-        restir_finish<kPbr>(ctx, P, cur, c, pixel % cam.width, pixel / cam.width, path, h, &pm, st.d, bsdf_avail,
-            st.thr, r, P.res_meta[path], sh_o1, sh_d1, sh_c1);
+        restir_finish<kPbr>(ctx, P, reservoir_slot(fp, P, cur, c, path), path, h, &pm, st.d, bsdf_avail, st.thr,
+            P.res_meta[path], sh_o1, sh_d1, sh_c1);
         int sss_event = 0, event = 0;
         const bool keep = bsdf_avail && scatter<kPbr>(fp, s.bounds, h, &pm, bounce, rng, st, sss_event, event);
         if constexpr (kPbr) {

@@ -8,6 +8,7 @@
 #include <cstddef>
 
 #include "device_common.cuh"
+#include "noise_sin.h"
 #include "openpbr.h"
 
 namespace rtgb {
@@ -79,8 +80,11 @@ RTGB_D void sphere_uv(const float3& p, float& u, float& v) {
     v = theta / kPi;
 }
 
+// The noise texture's sines use rtgb_noise::noise_sinf (noise_sin.h): the
+// hash amplifies the last bit of sin by 43758, so the kernels and the CPU
+// oracle share one bit-exact single-precision sine there.
 RTGB_D float hash_noise(const float3& p) {
-    const float n = sinf(dot(p, f3(12.9898f, 78.233f, 37.719f))) * 43758.5453f;
+    const float n = rtgb_noise::noise_sinf(dot(p, f3(12.9898f, 78.233f, 37.719f))) * 43758.5453f;
     return fractf(n) * 2.0f - 1.0f;
 }
 
@@ -157,7 +161,7 @@ RTGB_D float3 eval_texture(const DeviceScene& s, int index, float u, float v, co
         if (t.type == 2) return sample_image(s, t, u, v);
         if (t.type == 3) {
             const float turb = turbulence(p);
-            const float value = 0.5f * (1.0f + sinf(t.scale * p.z + 10.0f * turb));
+            const float value = 0.5f * (1.0f + rtgb_noise::noise_sinf(t.scale * p.z + 10.0f * turb));
             return f3(value, value, value);
         }
         return f3(1.0f, 0.0f, 1.0f);
@@ -533,8 +537,10 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
     int stack[kTraversalStack];
     int sp = 0;
     int node = 0;
+    int dropped = 0;
+    const int limit = s.bounds.traversal;
     int guard = 0;
-    for (; guard < s.bounds.traversal; ++guard) {
+    for (; guard < limit; ++guard) {
         const float4* np = reinterpret_cast<const float4*>(s.analytic_nodes + node);
         const float4 a = __ldg(np + 0), b = __ldg(np + 1), c = __ldg(np + 2), e = __ldg(np + 3);
         const int c0 = __float_as_int(a.w), c1 = __float_as_int(b.w);
@@ -552,7 +558,7 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
         if (h0 && h1) {
             const bool first0 = t0 <= t1;
             if (sp < kTraversalStack) stack[sp++] = first0 ? c1 : c0;
-            else if (s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);  // a dropped subtree is reported
+            else ++dropped;  // a dropped subtree is reported below
             node = first0 ? c0 : c1;
             continue;
         }
@@ -567,7 +573,7 @@ RTGB_D int traverse_analytic(const DeviceScene& s, const float3& o, const float3
         if (sp == 0) break;
         node = stack[--sp];
     }
-    if (guard >= s.bounds.traversal && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
+    if ((guard >= limit || dropped != 0) && s.bounds.gave_up) atomicAdd(s.bounds.gave_up, 1);
     t_hit = closest;
     return best;
 }

@@ -61,19 +61,15 @@ __global__ void __launch_bounds__(256) k_raygen(const FrameParams* __restrict__ 
         }
     }
     // The per-launch memset of the reservoir buffer (optix_renderer.cpp:253-254)
-    // as flat 16-byte stores over every active pixel's 84-byte reservoir; the
-    // frame buffers are 256-byte aligned.
+    // as flat 16-byte stores over every active pixel's 96-byte record (all-zero
+    // bits decode to the zeroed reservoir).
     {
-        const long long bytes = fp.total_pixels * static_cast<long long>(sizeof(Reservoir));
-        const long long n16 = bytes >> 4;
+        const long long n16 = fp.total_pixels * static_cast<long long>(sizeof(ReservoirRec) / 16);
         float4* base = reinterpret_cast<float4*>(cur.reservoirs);
         const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n16;
              i += static_cast<long long>(gridDim.x) * blockDim.x) {
             base[i] = z;
-        }
-        if (blockIdx.x == 0 && threadIdx.x < ((bytes & 15) >> 2)) {
-            reinterpret_cast<int*>(base + n16)[threadIdx.x] = 0;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -292,6 +288,7 @@ __global__ void k_reset_counters(Counters* counters, int bounce) {
         counters->shadow = 0;
         counters->restir = 0;
         counters->vis = 0;
+        counters->scatter = 0;
         if (bounce == 0) {
             for (int b = 0; b < 64; ++b) counters->shadow_bounce[b] = 0;
         }
@@ -363,9 +360,9 @@ void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
 }
 
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
-    LaunchShape shape, cudaStream_t stream) {
+    LaunchShape shape, LaunchShape scatter_shape, cudaStream_t stream) {
     if (scene.openpbr_count > 0) {
-        launch_shade_pbr(fp, scene, paths, counters, bounce, shape, stream);
+        launch_shade_pbr(fp, scene, paths, counters, bounce, shape, scatter_shape, stream);
         return;
     }
     k_shade<false><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
@@ -416,6 +413,7 @@ void query_launch_shapes(int sm_count, LaunchShape* shapes) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_restir_vis<false>, 128, 0);
     shapes[10] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     shapes[7] = query_shade_pbr_shape(sm_count);
+    shapes[13] = query_scatter_pbr_shape(sm_count);
     query_restir_pbr_shapes(sm_count, shapes);
 }
 

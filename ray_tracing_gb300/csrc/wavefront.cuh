@@ -16,7 +16,7 @@ struct FrameBufs {
     float* depth;
     float2* flow;
     float* trust;
-    Reservoir* reservoirs;
+    ReservoirRec* reservoirs;   // 96-byte sector-ordered records (device_common.cuh)
 };
 
 // Structure-of-arrays path streams, one slot per path (pixel-major, sample-minor).
@@ -35,7 +35,7 @@ struct Paths {
     float4* sh_o[2];    // shadow ray origin.xyz, w = tmax
     float4* sh_d[2];    // shadow ray direction.xyz
     float4* sh_c[2];    // contribution (throughput * direct).xyz, w = 1 when pending
-    Reservoir* res_scratch;  // per path reservoir when spp > 1 (ReSTIR)
+    ReservoirRec* res_scratch;  // per path reservoir when spp > 1 (ReSTIR)
     int* res_written;        // per path: 1 when the path wrote res_scratch
     int* queue[2];
     int* shadow_queue;
@@ -52,6 +52,7 @@ struct Paths {
     int* sorted;             // the shade queue in bucket order
     int* sort_hist;          // [kSortBins] bucket sizes (zero between bounces)
     int* sort_cursor;        // [kSortBins] bucket fill positions
+    int* scatter_queue;      // paths whose BSDF sampling runs in k_scatter (split OpenPBR shading)
 };
 
 struct Counters {
@@ -69,6 +70,7 @@ struct Counters {
     int restir;                       // ReSTIR queue length
     int vis;                          // bias-correction ray queue length
     unsigned long long shadow_bounce[64];  // shadow rays traced per bounce
+    int scatter;                      // scatter queue length (split OpenPBR shading)
 };
 
 struct FrameParams {
@@ -111,8 +113,9 @@ void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream);
 void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream);
 void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream);
+// `scatter_shape`: the grid of k_scatter, which the OpenPBR instance runs after k_shade.
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
-    LaunchShape shape, cudaStream_t stream);
+    LaunchShape shape, LaunchShape scatter_shape, cudaStream_t stream);
 // Buckets the bounce's shade queue by hit material into Paths::sorted (a no-op
 // below FrameParams::sort_from_bounce); shade_sort.cu.
 void launch_shade_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
@@ -131,9 +134,10 @@ void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
 // shade, shadow, finalize, resolve and restir.
 // shapes[0..6]: raygen, trace, shade, shadow, finalize, resolve, restir;
 // shapes[7..8]: the OpenPBR instances of shade and restir; [9..10]: restir RIS
-// and visibility passes; [11..12]: their OpenPBR instances.
+// and visibility passes; [11..12]: their OpenPBR instances; [13]: k_scatter
+// (OpenPBR BSDF sampling after k_shade).
 void query_launch_shapes(int sm_count, LaunchShape* shapes);
-constexpr int kLaunchShapes = 13;
+constexpr int kLaunchShapes = 14;
 
 // Reuse sources kept per path by the ReSTIR passes: temporal + up to 8 spatial.
 constexpr int kMaxReuseSources = 9;
@@ -142,10 +146,11 @@ constexpr int kMaxReuseSources = 9;
 // launch_shade and launch_restir forward to them when the scene has OpenPBR
 // materials.
 void launch_shade_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
-    LaunchShape shape, cudaStream_t stream);
+    LaunchShape shape, LaunchShape scatter_shape, cudaStream_t stream);
 void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
     const LaunchShape* shapes, cudaStream_t stream);
 LaunchShape query_shade_pbr_shape(int sm_count);
+LaunchShape query_scatter_pbr_shape(int sm_count);
 void query_restir_pbr_shapes(int sm_count, LaunchShape* shapes);
 void launch_tonemap(const float4* beauty, uint8_t* rgba, long long pixels, cudaStream_t stream);
 

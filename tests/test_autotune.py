@@ -59,7 +59,7 @@ def test_a_failed_tuning_leaves_the_handle_as_it_was():
     r = Renderer()
     r.prepare_scene(sc.view)
     before = r.launch_grids()
-    assert len(before) == 13 and min(before) > 0
+    assert len(before) >= 13 and min(before) > 0
     with pytest.raises(abi.RtgbError):
         r.autotune_launches(rig, bad, 2, frames=1)
     assert r.launch_grids() == before

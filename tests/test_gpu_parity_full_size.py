@@ -146,14 +146,37 @@ def test_c3_terrain_1m_triangles_mixed_rig():
     sc.close()
 
 
-def test_c5_textured_room_4m_triangles_1080p():
-    """C5: 3,996,544 triangles, checker and 3D-noise textured OpenPBR,
-    4096 emissive OpenPBR triangles; 2 x pinhole32 + 2 x equi62_lut1d at
-    1920x1080; 1 spp, depth 6."""
+def _c5(constant_walls: bool):
     sc = scenes.HostScene("textured_room")
+    if constant_walls:
+        v = sc.view
+        for i in range(v.texture_count):
+            if v.textures[i].type == 3:   # the walls' 3D noise -> a constant grey
+                v.textures[i].type = 0
+                v.textures[i].color[0] = v.textures[i].color[1] = v.textures[i].color[2] = 0.55
     rig = scenes.default_rig("textured_room", 4)
     prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=0, enable_restir_di=1,
                           restir_initial_candidates=32, restir_temporal_reuse=1, restir_spatial_neighbors=1)
+    return sc, rig, prof
+
+
+def test_c5_textured_room_4m_triangles_1080p():
+    """C5 as measured: 3,996,544 triangles, checker-textured floor, 3D-noise
+    walls, 4096 emissive OpenPBR triangles; 2 x pinhole32 + 2 x equi62_lut1d at
+    1920x1080; 1 spp, depth 6.
+
+    The walls' hash noise (fract(sin(dot(p, k)) * 43758.5453), programs.cu:184-209)
+    is chaotic in the position: its slope is about 3.5e6 per unit length, so
+    hit points that differ in the last bit, as the points after a BSDF sample
+    do (the sampled direction goes through CUDA's and the host's sinf/cosf/powf,
+    which differ in the last bit now and then), see unrelated colours from
+    there on. Paths therefore stay identical only up to the first scatter off a
+    wall (measured: 0.02 % of paths differ at depth 2, 4.2 % at depth 6, and
+    with the noise replaced by a constant 0.07 % at depth 6, the next test).
+    What is checked here: the divergence bound, the bounce-0 AOVs (the noise
+    itself at identical points, through the shared single-precision sine)
+    pixel for pixel, and the image means."""
+    sc, rig, prof = _c5(constant_walls=False)
     stride = 32
     gpu, orc = _render(sc, rig, prof, frames=1, stride=stride)
     assert gpu.acceleration_info().traversal_stack_overflows == 0
@@ -161,9 +184,51 @@ def test_c5_textured_room_4m_triangles_1080p():
     for cam in range(4):
         w, h = rig.cameras[cam].width, rig.cameras[cam].height
         assert (w, h) == (1920, 1080)
-        d, e = _gate_openpbr(*_paths(gpu, orc, cam, w, h, 1, 6, stride), max_diverged=2e-2)
-        out[f"camera{cam}"] = {"model": int(rig.cameras[cam].model), "diverged": d, "max_rel_err_identical": e}
+        gc, gr, oc, orad = _paths(gpu, orc, cam, w, h, 1, 6, stride)
+        diverged, _, _ = compare_paths(gc, gr, oc, orad, rel=REL)
+        assert diverged <= 0.06, f"{diverged:.2e} of paths diverged"
+        rows = np.arange(h) % stride == 0
+        for buf in ("albedo", "normal", "depth"):
+            g = gpu.buffer(cam, buf)[rows]
+            o = orc.buffer(cam, buf)[rows]
+            close = np.isclose(g, o, rtol=1e-5, atol=1e-6)
+            assert close.mean() > 0.999, f"cam {cam} {buf}: {1 - close.mean():.2e} mismatched"
+        gm, om = float(gr.mean()), float(orad.mean())
+        assert abs(gm - om) <= 0.03 * om, (gm, om)
+        out[f"camera{cam}"] = {"model": int(rig.cameras[cam].model), "diverged": diverged, "mean_gpu": gm,
+                               "mean_oracle": om}
     _report("C5_textured_room_4Mtri_4x1920x1080_d6", triangles=sc.view.triangle_count, row_stride=stride, **out)
+    gpu.close()
+    orc.close()
+    sc.close()
+
+
+def test_c5_room_with_constant_walls_paths_match():
+    """The C5 configuration with the walls' noise replaced by a constant grey:
+    path-by-path gates. Six bounces of OpenPBR in a closed room condition the
+    radiance a little worse than the gallery scene's (the GGX term amplifies
+    last-bit direction changes after each glossy bounce), so the bounds are the
+    measured ones with margin: 0.07 % of paths diverged, 99.9th percentile of
+    identical-path error 1.3e-4, 0.13 % of identical paths over 1e-4, worst
+    1.3e-2."""
+    sc, rig, prof = _c5(constant_walls=True)
+    stride = 32
+    gpu, orc = _render(sc, rig, prof, frames=1, stride=stride)
+    out = {}
+    for cam in range(4):
+        w, h = rig.cameras[cam].width, rig.cameras[cam].height
+        gc, gr, oc, orad = _paths(gpu, orc, cam, w, h, 1, 6, stride)
+        diverged, max_err, bad = compare_paths(gc, gr, oc, orad, rel=REL)
+        assert diverged <= 2e-3, f"{diverged:.2e} of paths diverged"
+        same = np.all(gc == oc, axis=1)
+        err = (np.abs(gr - orad) / np.maximum(np.abs(orad), 1e-6))[same].max(axis=1)
+        q = float(np.quantile(err, 0.999))
+        assert q <= 3e-4, f"99.9th percentile {q:.2e}"
+        assert max_err <= 5e-2, f"max relative error {max_err:.2e} on identical paths"
+        assert bad <= 3e-3 * same.sum(), f"{bad} identical paths over {REL} relative"
+        out[f"camera{cam}"] = {"diverged": diverged, "q999": q, "max_rel_err_identical": max_err,
+                               "over_1e-4": bad / max(int(same.sum()), 1)}
+    _report("C5_room_constant_walls_4x1920x1080_d6", row_stride=stride, **out)
     gpu.close()
     orc.close()
     sc.close()
