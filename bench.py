@@ -202,17 +202,20 @@ def plain_bands(r, rig, cameras: int, spp: int, max_bounces: int, per_frame: int
     return bands, ms
 
 
-def banded_equal_relmse(sc, frame_rigs: dict, denoised: dict, den_ms: float, max_bounces: int, cameras: int = 4,
+def banded_equal_relmse(sc, frame_rigs: dict, variants: dict, max_bounces: int, cameras: int = 4,
                         ref_spp: int = REFERENCE_SPP, max_spp: int = 1024, time_spp_cap: int = 128):
     """Equal-relMSE comparison on row bands. `frame_rigs`: frame -> rig;
-    `denoised`: frame -> per-camera band rows of the denoised pipeline's output
-    at that frame; `den_ms`: the pipeline's device ms per frame. The plain path
-    (no ReSTIR, no denoiser) is searched by doubling then bisecting spp until the
-    mean relMSE over the frames is no larger than the denoised mean; its
-    ms/frame is the full rig's device time at that spp (measured up to
-    `time_spp_cap` spp, larger counts scaled linearly from there)."""
+    `variants`: name -> (frame -> per-camera band rows of a denoised pipeline's
+    output at that frame, that pipeline's device ms per frame). Per variant the
+    plain path (no ReSTIR, no denoiser) is searched by doubling then bisecting
+    spp until the mean relMSE over the frames is no larger than the variant's
+    mean; its ms/frame is the full rig's device time at that spp (measured up
+    to `time_spp_cap` spp, larger counts scaled linearly from there). The
+    first variant's result is the record's top level; the others sit under
+    their names."""
     from ray_tracing_gb300.renderer import Renderer
     t0 = time.perf_counter()
+    results = {}
     with Renderer() as r:
         r.prepare_scene(sc.view)
         r.reset_sequence(SEED + 1)
@@ -222,48 +225,60 @@ def banded_equal_relmse(sc, frame_rigs: dict, denoised: dict, den_ms: float, max
         def err(imgs, f):
             return float(np.mean([relmse(imgs[c], refs[f][c]) for c in range(cameras)]))
 
-        d_err = {f: err(denoised[f], f) for f in frame_rigs}
-        target = float(np.mean(list(d_err.values())))
+        probes = {}
 
         def probe(spp):
-            per = {f: err(plain_bands(r, frame_rigs[f], cameras, spp, max_bounces, per_frame=16)[0], f)
-                   for f in frame_rigs}
-            return {"spp": spp, "relmse": float(np.mean(list(per.values()))),
-                    "per_frame": {str(f): v for f, v in per.items()}}
+            if spp not in probes:
+                per = {f: err(plain_bands(r, frame_rigs[f], cameras, spp, max_bounces, per_frame=16)[0], f)
+                       for f in frame_rigs}
+                probes[spp] = {"spp": spp, "relmse": float(np.mean(list(per.values()))),
+                               "per_frame": {str(f): v for f, v in per.items()}}
+            return probes[spp]
 
-        trail, found, spp = [], None, 1
-        while spp <= max_spp:
-            trail.append(probe(spp))
-            if trail[-1]["relmse"] <= target:
-                found = trail[-1]
-                break
-            spp *= 2
-        if found is not None and len(trail) >= 2:
-            lo, hi = trail[-2]["spp"], trail[-1]["spp"]
-            while hi - lo > max(1, lo // 8):
-                mid = (lo + hi) // 2
-                trail.append(probe(mid))
+        timed_ms = {}
+        for name, (denoised, den_ms) in variants.items():
+            d_err = {f: err(denoised[f], f) for f in frame_rigs}
+            target = float(np.mean(list(d_err.values())))
+            trail, found, spp = [], None, 1
+            while spp <= max_spp:
+                trail.append(probe(spp))
                 if trail[-1]["relmse"] <= target:
-                    hi, found = mid, trail[-1]
-                else:
-                    lo = mid
-        plain = None
-        if found is not None:
-            first = next(iter(frame_rigs))
-            timed = min(found["spp"], time_spp_cap)
-            _, ms = plain_render(r, frame_rigs[first], timed, cameras=cameras, max_bounces=max_bounces, per_frame=4,
-                                 images=False)
-            plain = dict(found, ms=ms * found["spp"] / timed, timed_spp=timed)
-    return {
-        "eps": RELMSE_EPS, "reference_spp": ref_spp, "frames": [int(f) for f in frame_rigs],
-        "sample": f"{BAND_COUNT} bands of {BAND_ROWS} rows per camera (evenly spaced), rendered as cropped cameras; "
-                  f"{BAND_COUNT * BAND_ROWS} of each camera's rows",
-        "reference_seconds": ref_secs,
-        "denoised": {"relmse": target, "per_frame": {str(f): v for f, v in d_err.items()}, "ms_per_frame": den_ms},
-        "plain": plain if plain is not None else {"spp": None, "note": f"not reached within {max_spp} spp"},
-        "plain_search": trail,
-        "speedup_at_equal_relmse": (plain["ms"] / den_ms) if plain is not None else None,
-    }
+                    found = trail[-1]
+                    break
+                spp *= 2
+            if found is not None and len(trail) >= 2:
+                lo, hi = trail[-2]["spp"], trail[-1]["spp"]
+                while hi - lo > max(1, lo // 8):
+                    mid = (lo + hi) // 2
+                    trail.append(probe(mid))
+                    if trail[-1]["relmse"] <= target:
+                        hi, found = mid, trail[-1]
+                    else:
+                        lo = mid
+            plain = None
+            if found is not None:
+                first = next(iter(frame_rigs))
+                timed = min(found["spp"], time_spp_cap)
+                if timed not in timed_ms:
+                    timed_ms[timed] = plain_render(r, frame_rigs[first], timed, cameras=cameras,
+                                                   max_bounces=max_bounces, per_frame=4, images=False)[1]
+                plain = dict(found, ms=timed_ms[timed] * found["spp"] / timed, timed_spp=timed)
+            results[name] = {
+                "denoised": {"relmse": target, "per_frame": {str(f): v for f, v in d_err.items()},
+                             "ms_per_frame": den_ms},
+                "plain": plain if plain is not None else {"spp": None, "note": f"not reached within {max_spp} spp"},
+                "plain_search": trail,
+                "speedup_at_equal_relmse": (plain["ms"] / den_ms) if plain is not None else None,
+            }
+    names = list(results)
+    out = {"eps": RELMSE_EPS, "reference_spp": ref_spp, "frames": [int(f) for f in frame_rigs],
+           "sample": f"{BAND_COUNT} bands of {BAND_ROWS} rows per camera (evenly spaced), rendered as cropped "
+                     f"cameras; {BAND_COUNT * BAND_ROWS} of each camera's rows",
+           "reference_seconds": ref_secs}
+    out.update(results[names[0]])
+    for name in names[1:]:
+        out[name] = results[name]
+    return out
 
 
 def mixed_rig_1080p(scene_name: str = "random_spheres"):
@@ -552,48 +567,61 @@ C5_SIZE = (0, 0)            # camera size override (0: the rig's 1920x1080), for
 C5_RELMSE = True            # the equal-relMSE comparison of c5_record (bench.py --no-relmse turns it off)
 
 
+def c5_orbit(sc, rig, prof, weights, frames, warmup, degrees_per_frame, eval_frames):
+    """Renders the C5 orbit; returns per-frame ms, denoise ms, stage times, rays,
+    the prepare time and, at `eval_frames`, the denoised output's band rows."""
+    from ray_tracing_gb300 import scenes
+    from ray_tracing_gb300.renderer import Renderer
+    with Renderer(stage_timing=True) as r:
+        t0 = time.perf_counter()
+        r.prepare_scene(sc.view)
+        prep_ms = 1000.0 * (time.perf_counter() - t0)
+        if weights is not None:
+            r.set_denoiser(weights)
+        r.reset_sequence(SEED)
+        for _ in range(warmup):
+            r.render_frame(rig, prof, 4)
+        r.reset_accumulation()
+        ms, dn, stages, rays = [], [], [], 0
+        bands, frame_rigs = {}, {}
+        for f in range(frames):
+            frig = scenes.orbit_rig(rig, degrees_per_frame * f)
+            v = r.render_frame(frig, prof, 4)
+            ms.append(v.frame_render_ms)
+            dn.append(v.cameras[0].denoise_ms)
+            stages.append(r.stage_times())
+            rays += v.rays_traced
+            if f in eval_frames:
+                frame_rigs[f] = frig
+                bands[f] = [band_rows_of(r.buffer(c, "denoised")[..., :3], frig.cameras[c].height)
+                            for c in range(4)]
+    return ms, dn, stages, rays, prep_ms, bands, frame_rigs
+
+
 def c5_record(frames=60, warmup=3, degrees_per_frame=2.0, relmse_eval=True):
     """C5: the 4 M-triangle textured room (checker / 3D-noise OpenPBR, 600
     icosphere props, 4096 emissive triangles), 2 x pinhole32 + 2 x
     equi62_lut1d at 1920x1080 in one launch, the rig orbiting the room by
     `degrees_per_frame` each of `frames` frames; 1 spp, depth 6, ReSTIR DI
     (32 candidates, temporal + 1 spatial) and the U-Net denoiser when its
-    weights are present. Frame times are the frames' CUDA events. With the
-    weights, `equal_relmse` compares the denoised output of frames 0, 30 and
-    59 with 4096-spp plain renders of the same frames (row bands,
-    banded_equal_relmse)."""
+    weights are present. Frame times are the frames' CUDA events. The room has
+    no analytic lights, so the reference's ReSTIR (analytic lights only) does
+    nothing and the emissive NEE carries the direct light; `restir_emissive`
+    is the same orbit with ReSTIR resampling the 4096 emissive triangles
+    (rtgb_render_profile::restir_emissive). With the weights, `equal_relmse`
+    compares the denoised output of frames 0, 30 and 59 of both orbits with
+    4096-spp plain renders of the same frames (row bands, banded_equal_relmse)."""
     from ray_tracing_gb300 import scenes
-    from ray_tracing_gb300.renderer import Renderer
     weights = _weights()
     prof = scenes.profile("balanced", samples_per_pixel=1, max_bounces=6, enable_denoise=1 if weights is not None else 0,
                           enable_restir_di=1, restir_initial_candidates=32, restir_temporal_reuse=1,
                           restir_spatial_neighbors=1)
-    relmse_eval = relmse_eval and C5_RELMSE
+    relmse_eval = relmse_eval and C5_RELMSE and weights is not None
+    eval_frames = C5_EVAL_FRAMES if relmse_eval else ()
     with scenes.HostScene("textured_room") as sc:
         rig = scenes.default_rig("textured_room", 4, *C5_SIZE)
-        with Renderer(stage_timing=True) as r:
-            t0 = time.perf_counter()
-            r.prepare_scene(sc.view)
-            prep_ms = 1000.0 * (time.perf_counter() - t0)
-            if weights is not None:
-                r.set_denoiser(weights)
-            r.reset_sequence(SEED)
-            for _ in range(warmup):
-                r.render_frame(rig, prof, 4)
-            r.reset_accumulation()
-            ms, dn, stages, rays = [], [], [], 0
-            bands, frame_rigs = {}, {}
-            for f in range(frames):
-                frig = scenes.orbit_rig(rig, degrees_per_frame * f)
-                v = r.render_frame(frig, prof, 4)
-                ms.append(v.frame_render_ms)
-                dn.append(v.cameras[0].denoise_ms)
-                stages.append(r.stage_times())
-                rays += v.rays_traced
-                if weights is not None and relmse_eval and f in C5_EVAL_FRAMES:
-                    frame_rigs[f] = frig
-                    bands[f] = [band_rows_of(r.buffer(c, "denoised")[..., :3], frig.cameras[c].height)
-                                for c in range(4)]
+        ms, dn, stages, rays, prep_ms, bands, frame_rigs = c5_orbit(sc, rig, prof, weights, frames, warmup,
+                                                                   degrees_per_frame, eval_frames)
         # per-stage mean ms: raygen, (trace, shade, shadow) per bounce, finalize + resolve
         st = np.mean(np.stack(stages), axis=0)
         mb = (len(st) - 3) // 3
@@ -606,9 +634,23 @@ def c5_record(frames=60, warmup=3, degrees_per_frame=2.0, relmse_eval=True):
                "prepare_ms": prep_ms, "triangles": sc.view.triangle_count, "frames": frames,
                "orbit_degrees_per_frame": degrees_per_frame, "denoised": weights is not None,
                "stage_ms": stage_ms}
+        variants = {"nee": (bands, float(np.mean(ms)))}
+        try:
+            prof.restir_emissive = 1
+            ems, edn, est, erays, _, ebands, _ = c5_orbit(sc, rig, prof, weights, frames, warmup, degrees_per_frame,
+                                                          eval_frames)
+            sh0 = float(np.mean(np.stack(est), axis=0)[2])
+            rec["restir_emissive"] = {"ms_per_frame": float(np.mean(ems)), "ms_p50": float(np.median(ems)),
+                                      "denoise_ms_per_frame": float(np.mean(edn)),
+                                      "mrays_per_s": erays / (sum(ems) * 1e-3) / 1e6,
+                                      "shade@0_ms (with the ReSTIR passes)": sh0}
+            if ebands:
+                variants["restir_emissive"] = (ebands, float(np.mean(ems)))
+        except Exception as e:  # the reference-rule orbit above stands on its own
+            rec["restir_emissive"] = {"error": f"{type(e).__name__}: {e}"}
         if bands:
             try:
-                rec["equal_relmse"] = banded_equal_relmse(sc, frame_rigs, bands, float(np.mean(ms)), max_bounces=6)
+                rec["equal_relmse"] = banded_equal_relmse(sc, frame_rigs, variants, max_bounces=6)
             except Exception as e:  # the frame timings above stand on their own
                 rec["equal_relmse"] = {"error": f"{type(e).__name__}: {e}"}
     return rec

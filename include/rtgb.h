@@ -297,6 +297,15 @@ typedef struct rtgb_render_profile {
     int32_t restir_max_spatial_candidates;
     int32_t restir_bias_correction;   /* 0 off, 1 basic (src/common/restir_di.h:16-19) */
     int32_t restir_min_analytic_lights;
+    /* No reference counterpart (0 keeps the reference's behaviour). 1: ReSTIR DI
+     * resamples the emissive-geometry lights (the light list NEE samples,
+     * packed_scene_preparation.cpp:265-302) instead of the analytic lights:
+     * bounce-0 receivers that are not emitters take their emissive direct
+     * light from the reservoir (candidates, temporal and spatial reuse, BASIC
+     * bias correction as for analytic lights) in place of the one-sample
+     * emissive NEE, and analytic lights, if any, get the plain analytic NEE.
+     * The reference's ReSTIR covers analytic lights only (programs.cu:1915-1924). */
+    int32_t restir_emissive;
 } rtgb_render_profile;
 
 /* ------------------------------------------------------------------------ */

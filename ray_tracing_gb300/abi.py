@@ -159,7 +159,8 @@ class RenderProfile(C.Structure):
                 ("restir_initial_candidates", C.c_int32), ("restir_temporal_reuse", C.c_int32),
                 ("restir_max_history_age", C.c_int32), ("restir_max_temporal_candidates", C.c_int32),
                 ("restir_spatial_neighbors", C.c_int32), ("restir_max_spatial_candidates", C.c_int32),
-                ("restir_bias_correction", C.c_int32), ("restir_min_analytic_lights", C.c_int32)]
+                ("restir_bias_correction", C.c_int32), ("restir_min_analytic_lights", C.c_int32),
+                ("restir_emissive", C.c_int32)]
 
 
 class CreateInfo(C.Structure):

@@ -849,6 +849,7 @@ struct rtgb_renderer {
         P.res_meta = reinterpret_cast<int*>(take(i1));
         P.res_src = reinterpret_cast<int2*>(take(src2));
         P.res_src_t = reinterpret_cast<float*>(take(src1));
+        P.src_stride = n;  // source-major: one source of consecutive paths is contiguous
         P.vis_queue = reinterpret_cast<int*>(take(src1));
         P.sort_key = reinterpret_cast<int*>(take(i1));
         P.sorted = reinterpret_cast<int*>(take(i1));
@@ -1073,7 +1074,11 @@ struct rtgb_renderer {
         fp.total_paths = total_paths;
         fp.stream = sample_stream;
         const int min_lights = profile.restir_min_analytic_lights > 0 ? profile.restir_min_analytic_lights : 1;
-        fp.restir_enabled = profile.enable_restir_di != 0 && scene.analytic_count >= min_lights ? 1 : 0;
+        // ReSTIR over emissive geometry (opt-in) needs an emissive light list; the
+        // reference's ReSTIR needs restir_min_analytic_lights analytic lights
+        fp.restir_emissive = profile.enable_restir_di != 0 && profile.restir_emissive != 0 && scene.light_count > 0 ? 1 : 0;
+        fp.restir_enabled = fp.restir_emissive != 0 ||
+                            (profile.enable_restir_di != 0 && scene.analytic_count >= min_lights) ? 1 : 0;
         fp.restir_candidates = profile.restir_initial_candidates;
         fp.restir_temporal = profile.restir_temporal_reuse;
         fp.restir_max_age = profile.restir_max_history_age;

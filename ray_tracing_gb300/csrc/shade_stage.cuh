@@ -69,8 +69,19 @@ struct ShadeCtx {
     int overflow;
     unsigned long long vis_rays;
     unsigned long long restir_runs;
-    const float* analytic_cdf;  // shared-memory copy when it fits, else global
+    const float* cdf;    // the ReSTIR candidates' light CDF: shared-memory copy when it fits, else global
+    int cdf_count;       // its length: analytic lights, or the emissive list (FrameParams::restir_emissive)
 };
+
+// The ReSTIR candidate of light `li` with (u0, u1) at a surface: an analytic
+// light (the reference's ReSTIR DI), or with FrameParams::restir_emissive a
+// light of the emissive-geometry list (emissive_candidate).
+template <bool kPbr>
+RTGB_D LightSample restir_candidate(const ShadeCtx& ctx, const float3& pos, const float3& sn, int mtype, int li,
+    float u0, float u1) {
+    if (ctx.fp.restir_emissive != 0) return emissive_candidate<kPbr>(ctx.s, pos, sn, mtype, li, u0, u1);
+    return analytic_candidate(ctx.s, pos, li, u0, u1);
+}
 
 RTGB_D float restir_lum(const float3& v) { return fmaxf(0.0f, 0.2126f * v.x + 0.7152f * v.y + 0.0722f * v.z); }
 
@@ -143,7 +154,7 @@ RTGB_D float target_at_previous(ShadeCtx& ctx, int c, const Surface& src, const 
     }
     const float tol = fmaxf(0.01f, 0.02f * dist);
     if (len_sq(sub(sh.pos, spos)) > tol * tol || dot(sh.sn, ld3(src.normal)) < 0.95f) return 0.0f;
-    const LightSample l = analytic_candidate(ctx.s, sh.pos, sel.light_index, sel.u0, sel.u1);
+    const LightSample l = restir_candidate<kPbr>(ctx, sh.pos, sh.sn, sh.mtype, sel.light_index, sel.u0, sel.u1);
     // the source path state is fresh: unit throughput, ray from the previous camera
     pbr::Mat spm;
     if constexpr (kPbr) {
@@ -239,16 +250,16 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
     int k = 0;
     for (; k + 1 < count; k += 2) {
         Candidate ca, cb;
-        ca.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
+        ca.light_index = sample_cdf_guided(ctx.cdf, guide, ctx.cdf_count, rnd(rng));
         ca.u0 = rnd(rng);
         ca.u1 = rnd(rng);
         const float ua = rnd(rng);
-        cb.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
+        cb.light_index = sample_cdf_guided(ctx.cdf, guide, ctx.cdf_count, rnd(rng));
         cb.u0 = rnd(rng);
         cb.u1 = rnd(rng);
         const float ub = rnd(rng);
-        const LightSample la = analytic_candidate(s, h.pos, ca.light_index, ca.u0, ca.u1);
-        const LightSample lb = analytic_candidate(s, h.pos, cb.light_index, cb.u0, cb.u1);
+        const LightSample la = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, ca.light_index, ca.u0, ca.u1);
+        const LightSample lb = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, cb.light_index, cb.u0, cb.u1);
         float ta = 0.0f, tb = 0.0f;
         unshadowed<kPbr>(h, pm, ray_d, thr, la, bsdf_avail, ta);
         unshadowed<kPbr>(h, pm, ray_d, thr, lb, bsdf_avail, tb);
@@ -257,10 +268,10 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
     }
     if (k < count) {
         Candidate cand;
-        cand.light_index = sample_cdf_guided(ctx.analytic_cdf, guide, s.analytic_count, rnd(rng));
+        cand.light_index = sample_cdf_guided(ctx.cdf, guide, ctx.cdf_count, rnd(rng));
         cand.u0 = rnd(rng);
         cand.u1 = rnd(rng);
-        const LightSample l = analytic_candidate(s, h.pos, cand.light_index, cand.u0, cand.u1);
+        const LightSample l = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, cand.light_index, cand.u0, cand.u1);
         float t = 0.0f;
         unshadowed<kPbr>(h, pm, ray_d, thr, l, bsdf_avail, t);
         const float w = l.pdf > 0.0f ? t / l.pdf : 0.0f;
@@ -280,7 +291,7 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
         const Reservoir prev = load_reuse(hres + reproj);
         const float tol = fmaxf(0.005f, 0.01f * h.t);
         if (surface_valid(cur_surface, prev, tol, 0.95f, fp.restir_max_age)) {
-            const LightSample l = analytic_candidate(s, h.pos, prev.selected.light_index, prev.selected.u0,
+            const LightSample l = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, prev.selected.light_index, prev.selected.u0,
                 prev.selected.u1);
             float t = 0.0f;
             unshadowed<kPbr>(h, pm, ray_d, thr, l, bsdf_avail, t);
@@ -306,7 +317,7 @@ RTGB_D void restir_gather(ShadeCtx& ctx, const FrameBufs& hist, const int* guide
             const Reservoir prev = load_reuse(hres + ni);
             const float tol = fmaxf(0.01f, 0.02f * h.t);
             if (!surface_valid(cur_surface, prev, tol, 0.95f, fp.restir_max_age)) continue;
-            const LightSample l = analytic_candidate(s, h.pos, prev.selected.light_index, prev.selected.u0,
+            const LightSample l = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, prev.selected.light_index, prev.selected.u0,
                 prev.selected.u1);
             float t = 0.0f;
             unshadowed<kPbr>(h, pm, ray_d, thr, l, bsdf_avail, t);
@@ -341,8 +352,8 @@ RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, ReservoirRec* slot, lon
         float sel_t = r.selected_target;
         float sum = r.selected_target * static_cast<float>(canonical);
         for (int k = 0; k < nsrc; ++k) {
-            const float t = P.res_src_t[path * kMaxSources + k];
-            sum += t * static_cast<float>(P.res_src[path * kMaxSources + k].y);
+            const float t = P.res_src_t[k * P.src_stride + path];
+            sum += t * static_cast<float>(P.res_src[k * P.src_stride + path].y);
             if (selected_src == k) sel_t = t;
         }
         reservoir_finalize_basic(r, sel_t, sum, nsrc);
@@ -356,7 +367,8 @@ RTGB_D void restir_finish(ShadeCtx& ctx, const Paths& P, ReservoirRec* slot, lon
     for (int k = 0; k < 4; ++k) slot->q[2 + k] = q[k];
     if (fp.spp != 1) P.res_written[path] = 1;
     if (r.valid == 0) return;
-    const LightSample l = analytic_candidate(s, h.pos, r.selected.light_index, r.selected.u0, r.selected.u1);
+    const LightSample l = restir_candidate<kPbr>(ctx, h.pos, h.sn, h.mtype, r.selected.light_index, r.selected.u0,
+        r.selected.u1);
     float t = 0.0f;
     const float3 num = unshadowed<kPbr>(h, pm, ray_d, thr, l, bsdf_avail, t);
     if (!l.valid || t <= 0.0f) return;
@@ -634,8 +646,13 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
                     const float ew = emission_mis_weight(s, st, &h, false);
                     st.rad = add(st.rad, mul(st.thr, mul(h.emis, ew)));
                     const bool bsdf_avail = bounce + 1 < fp.max_bounces;
+                    // ReSTIR over emissive geometry (opt-in, FrameParams::restir_emissive)
+                    // takes the place of the emissive NEE for receivers that are not
+                    // emitters themselves; its sample fills shadow slot 0 in k_restir
+                    const bool emissive_restir = restir_bounce && fp.restir_emissive != 0 && h.mtype != 3
+                                                 && s.light_count > 0 && find_light(s, h.ptype, h.pidx) < 0;
                     // accumulate_direct_light (programs.cu:2249-2280) -> shadow slot 0
-                    if (h.mtype != 3 && s.light_count > 0) {
+                    if (h.mtype != 3 && s.light_count > 0 && !emissive_restir) {
                         const LightSample l = sample_direct<kPbr>(s, h, rng);
                         if (l.valid) {
                             float bp = 0.0f;
@@ -652,7 +669,7 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
                             }
                         }
                     }
-                    if (restir_bounce) {
+                    if (restir_bounce && fp.restir_emissive == 0) {
                         // accumulate_restir_analytic_direct_light returns before any
                         // draw for emitters and light-less scenes (programs.cu:2318-2321)
                         deferred = h.mtype != 3 && s.analytic_count > 0;
@@ -677,6 +694,7 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
                             }
                         }
                     }
+                    deferred = deferred || emissive_restir;
                     if (!deferred && bsdf_avail) {
                         if constexpr (kSplit) {
                             to_scatter = true;
@@ -698,11 +716,14 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
         // the random walk scaled the throughput k_scatter starts from
         if (kSplit && to_scatter && thr_changed) P.thr[path] = f4(st.thr, st.prev_pdf);
         if (deferred) {
-            // slot 0 travels to k_restir, which adds slot 1 and queues the shadow rays
-            P.sh_c[0][path] = sh_c[0];
-            if (sh_c[0].w != 0.0f) {
-                P.sh_o[0][path] = sh_o[0];
-                P.sh_d[0][path] = sh_d[0];
+            // the NEE slot travels to k_restir, which adds the ReSTIR slot (1 for
+            // analytic lights, 0 for emissive geometry) and queues the shadow rays
+            const bool em = fp.restir_emissive != 0;
+            const float4 kc = em ? sh_c[1] : sh_c[0];
+            (em ? P.sh_c[1] : P.sh_c[0])[path] = kc;
+            if (kc.w != 0.0f) {
+                (em ? P.sh_o[1] : P.sh_o[0])[path] = em ? sh_o[1] : sh_o[0];
+                (em ? P.sh_d[1] : P.sh_d[0])[path] = em ? sh_d[1] : sh_d[0];
             }
         } else {
             const bool any_shadow = sh_c[0].w != 0.0f || sh_c[1].w != 0.0f;
@@ -764,14 +785,16 @@ struct RestirShared {
     int guide[kGuide + 1];
 };
 
-RTGB_D const float* stage_cdf(const DeviceScene& s, RestirShared& sh) {
-    const bool shared = s.analytic_count <= kSharedCdf;
+RTGB_D const float* stage_cdf(const FrameParams& fp, const DeviceScene& s, RestirShared& sh, int& count) {
+    const float* src = fp.restir_emissive != 0 ? s.light_cdf : s.analytic_cdf;
+    count = fp.restir_emissive != 0 ? s.light_count : s.analytic_count;
+    const bool shared = count <= kSharedCdf;
     if (shared) {
-        for (int k = threadIdx.x; k < s.analytic_count; k += blockDim.x) sh.cdf[k] = s.analytic_cdf[k];
+        for (int k = threadIdx.x; k < count; k += blockDim.x) sh.cdf[k] = src[k];
         __syncthreads();
     }
-    const float* cdf = shared ? sh.cdf : s.analytic_cdf;
-    build_guide(cdf, s.analytic_count, sh.guide);
+    const float* cdf = shared ? sh.cdf : src;
+    build_guide(cdf, count, sh.guide);
     return cdf;
 }
 
@@ -784,8 +807,9 @@ __global__ void __launch_bounds__(128, 6) k_restir_ris(const FrameParams* __rest
     const FrameBufs hist = fp.hist;
     const int count = counters->restir;
     if (count == 0) return;
-    const float* cdf = stage_cdf(s, sh);
-    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, cdf};
+    int cdf_count = 0;
+    const float* cdf = stage_cdf(fp, s, sh, cdf_count);
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, cdf, cdf_count};
     constexpr int bounce = 0;
     const bool bsdf_avail = bounce + 1 < fp.max_bounces;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
@@ -811,7 +835,7 @@ __global__ void __launch_bounds__(128, 6) k_restir_ris(const FrameParams* __rest
         store_reservoir(reservoir_slot(fp, P, fp.cur, c, path), r);
         P.rng[path] = rng;
         P.res_meta[path] = pack_meta(nsrc, selected_src, canonical);
-        for (int k = 0; k < nsrc; ++k) P.res_src[static_cast<long long>(path) * kMaxSources + k] = make_int2(src_index[k], mult[k]);
+        for (int k = 0; k < nsrc; ++k) P.res_src[k * P.src_stride + path] = make_int2(src_index[k], mult[k]);
         const bool bias = fp.restir_bias == 1 && r.valid != 0;
         for (int k = 0; k < kMaxSources; ++k) {
             queue_push(P.vis_queue, &counters->vis, (path << 4) | k, bias && k < nsrc);
@@ -825,7 +849,7 @@ __global__ void __launch_bounds__(128) k_restir_vis(const FrameParams* __restric
     const FrameParams& fp = *fpp;
     const FrameBufs hist = fp.hist;
     const int count = counters->vis;
-    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, s.analytic_cdf};
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, nullptr, 0};
     constexpr int bounce = 0;
     const bool bsdf_avail = bounce + 1 < fp.max_bounces;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
@@ -833,7 +857,7 @@ __global__ void __launch_bounds__(128) k_restir_vis(const FrameParams* __restric
         const int path = item >> 4;
         const int k = item & 15;
         const int c = camera_of_path(fp, path);
-        const long long slot = static_cast<long long>(path) * kMaxSources + k;
+        const long long slot = k * P.src_stride + path;
         const ReservoirRec* hres = hist.reservoirs + fp.cam[c].pixel_offset;
         const float4 sq = reservoir_slot(fp, P, fp.cur, c, path)->q[2];
         const Candidate sel{__float_as_int(sq.x), sq.y, sq.z};
@@ -849,7 +873,7 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
     const FrameParams& fp = *fpp;
     FrameBufs cur = fp.cur;
     const int count = counters->restir;
-    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, s.analytic_cdf};
+    ShadeCtx ctx{fp, s, 0, 0ull, 0ull, nullptr, 0};
     constexpr int bounce = 0;
     const int out = 1;
     unsigned long long runs = 0;
@@ -879,13 +903,16 @@ __global__ void __launch_bounds__(128) k_restir(const FrameParams* __restrict__ 
         }
         P.rng[path] = rng;
         if (keep) store_path(P, path, st);
-        const bool slot0 = P.sh_c[0][path].w != 0.0f;
-        const bool any_shadow = slot0 || sh_c1.w != 0.0f;
+        // the ReSTIR sample's slot: 1 beside the emissive NEE in slot 0 (the
+        // reference), or 0 when ReSTIR resamples the emissive geometry itself
+        const int rs = fp.restir_emissive != 0 ? 0 : 1;
+        const bool nee = P.sh_c[rs ^ 1][path].w != 0.0f;
+        const bool any_shadow = nee || sh_c1.w != 0.0f;
         if (sh_c1.w != 0.0f) {
-            P.sh_o[1][path] = sh_o1;
-            P.sh_d[1][path] = sh_d1;
+            P.sh_o[rs][path] = sh_o1;
+            P.sh_d[rs][path] = sh_d1;
         }
-        if (any_shadow) P.sh_c[1][path] = sh_c1;
+        if (any_shadow) P.sh_c[rs][path] = sh_c1;
         queue_push(P.shadow_queue, &counters->shadow, path, any_shadow);
         queue_push(P.queue[out], &counters->active[out], path, keep);
     }

@@ -847,6 +847,110 @@ RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t&
     return smp;
 }
 
+// A ReSTIR candidate over emissive geometry (no reference counterpart: the
+// reference's ReSTIR DI resamples analytic lights only, programs.cu:1915-1924).
+// Light `li` of the emissive list sampled with the given (u0, u1) the way
+// sample_direct samples it for a receiver that is not itself an emitter, so a
+// candidate re-evaluates to the same point at any surface: cone sampling
+// toward spheres, uniform area sampling on quads and triangles, and for the
+// environment the cosine distribution about the receiver normal built from
+// (u0, u1) (normal + a uniform sphere point), whose pdf the BSDF-side MIS
+// weight of emission_mis_weight assumes; isotropic receivers take the uniform
+// sphere point.
+template <bool kPbr>
+RTGB_D LightSample emissive_candidate(const DeviceScene& s, const float3& sp, const float3& sn, int rcv_mtype, int li,
+    float u0, float u1) {
+    LightSample smp = empty_sample();
+    if (li < 0 || li >= s.light_count) return smp;
+    const PackedLight light = s.lights[li];
+    const float sel = light.selection_pdf;
+    if (sel <= 0.0f) return smp;
+    smp.light_index = li;
+    if (light.type == 3) {
+        const float3 q = sphere_direction(u0, u1);
+        if (rcv_mtype == 4) {
+            smp.direction = q;
+            smp.pdf = sel * uniform_sphere_pdf();
+        } else {
+            smp.direction = add(sn, q);
+            if (near_zero(smp.direction)) smp.direction = sn;
+            smp.direction = normalize(smp.direction);
+            smp.pdf = sel * fmaxf(dot(sn, smp.direction), 0.0f) / kPi;
+        }
+        smp.emission = ld3(s.background);
+        smp.distance = kRayFar;
+        smp.infinite = true;
+        smp.valid = smp.pdf > 0.0f && max_comp(smp.emission) > 0.0f;
+        return smp;
+    }
+    float tu = 0.0f, tv = 0.0f, cond = 0.0f;
+    if (light.type == 0) {
+        if (light.primitive_index < 0 || light.primitive_index >= s.sphere_count) return empty_sample();
+        const rtgb_sphere sph = s.spheres[light.primitive_index];
+        const float3 center = ld3(sph.center);
+        const float3 tc = sub(center, sp);
+        const float d2 = len_sq(tc);
+        const float r2 = sph.radius * sph.radius;
+        if (d2 <= r2 * (1.0f + 1e-6f)) return empty_sample();
+        const float ctm = sqrtf(fmaxf(0.0f, 1.0f - r2 / d2));
+        smp.direction = cone_direction(normalize(tc), ctm, u0, u1);
+        const float3 oc = sub(sp, center);
+        const float hb = dot(oc, smp.direction);
+        const float disc = hb * hb - (len_sq(oc) - r2);
+        if (disc <= 0.0f) return empty_sample();
+        smp.distance = -hb - sqrtf(disc);
+        if (smp.distance <= kRayEpsilon) return empty_sample();
+        smp.position = add(sp, mul(smp.direction, smp.distance));
+        smp.normal = normalize(sub(smp.position, center));
+        sphere_uv(smp.normal, tu, tv);
+        smp.material_index = sph.material_index;
+        cond = uniform_cone_pdf(ctm);
+    } else {
+        float3 an;
+        if (light.type == 1) {
+            if (light.primitive_index < 0 || light.primitive_index >= s.quad_count) return empty_sample();
+            const rtgb_quad q = s.quads[light.primitive_index];
+            const float3 o = ld3(q.origin), eu = ld3(q.edge_u), ev = ld3(q.edge_v);
+            tu = u0;
+            tv = u1;
+            smp.position = add(o, add(mul(eu, tu), mul(ev, tv)));
+            an = cross(eu, ev);
+            smp.material_index = q.material_index;
+        } else {
+            if (light.primitive_index < 0 || light.primitive_index >= s.triangle_count) return empty_sample();
+            const rtgb_triangle t = s.triangles[light.primitive_index];
+            const float3 p0 = ld3(t.p0), p1 = ld3(t.p1), p2 = ld3(t.p2);
+            float w0 = 0.0f, w1 = 0.0f, w2 = 0.0f;
+            sample_uniform_triangle(u0, u1, w0, w1, w2);
+            smp.position = add(mul(p0, w0), add(mul(p1, w1), mul(p2, w2)));
+            if (t.has_texcoords != 0) {
+                tu = t.uv0[0] * w0 + t.uv1[0] * w1 + t.uv2[0] * w2;
+                tv = t.uv0[1] * w0 + t.uv1[1] * w1 + t.uv2[1] * w2;
+            } else {
+                tu = w1;
+                tv = w2;
+            }
+            an = cross(sub(p1, p0), sub(p2, p0));
+            smp.material_index = t.material_index;
+        }
+        const float alen = len(an);
+        if (alen <= 1e-12f) return empty_sample();
+        smp.normal = divs(an, alen);
+        const float3 tl = sub(smp.position, sp);
+        const float d2 = len_sq(tl);
+        if (d2 <= 1e-12f) return empty_sample();
+        smp.distance = sqrtf(d2);
+        smp.direction = divs(tl, smp.distance);
+        const float ac = dot(smp.normal, mul(smp.direction, -1.0f));
+        cond = area_pdf(light.type == 1 ? alen : 0.5f * alen, d2, ac);
+    }
+    if (cond <= 0.0f || smp.material_index < 0 || smp.material_index >= s.material_count) return empty_sample();
+    smp.emission = material_emission<kPbr>(s, s.materials[smp.material_index], tu, tv, smp.position);
+    smp.pdf = sel * cond;
+    smp.valid = smp.pdf > 0.0f && max_comp(smp.emission) > 0.0f;
+    return smp;
+}
+
 // sample_analytic_direct_light_candidate, programs.cu:1234-1346
 // Disk and rect lights (the common case) read only the light's hot record
 // (DeviceScene::analytic_hot); the other types read the full light.

@@ -271,7 +271,10 @@ __global__ void __launch_bounds__(256) k_resolve(const FrameParams* __restrict__
         const float blend = 1.0f / static_cast<float>(hl + 1);
         const float ccx = fminf(fmaxf(cb.x, 0.0f), 10.0f), ccy = fminf(fmaxf(cb.y, 0.0f), 10.0f),
                     ccz = fminf(fmaxf(cb.z, 0.0f), 10.0f);
-        if (fp.restir_enabled == 0) {
+        // the reference accumulates beauty only without its (analytic) ReSTIR;
+        // the emissive-geometry ReSTIR extension keeps the accumulation, so it
+        // changes the direct-light estimator and nothing else
+        if (fp.restir_enabled == 0 || fp.restir_emissive != 0) {
             cur.beauty[pix] = make_float4(hb.x + (ccx - hb.x) * blend, hb.y + (ccy - hb.y) * blend,
                 hb.z + (ccz - hb.z) * blend, 1.0f);
         }

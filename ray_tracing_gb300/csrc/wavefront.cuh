@@ -44,8 +44,9 @@ struct Paths {
     int* sss_mat;            // OpenPBR material whose random-walk medium the path is inside, -1 outside
     float4* sss_ext;         // that medium's extinction.xyz, w = Henyey-Greenstein anisotropy
     float4* sss_alb;         // its single-scattering albedo.xyz
-    int2* res_src;           // ReSTIR reuse sources [path][9]: history pixel, multiplicity
-    float* res_src_t;        // their bias-correction targets [path][9]
+    int2* res_src;           // ReSTIR reuse sources [source][path] (9 sources): history pixel, multiplicity
+    float* res_src_t;        // their bias-correction targets [source][path]
+    long long src_stride;    // paths per source row of res_src / res_src_t (the path capacity)
     int* res_meta;           // per path: source count, selected source + 1, canonical M
     int* vis_queue;          // (path << 4) | source of each bias-correction ray
     int* sort_key;           // material bucket of each shade-queue slot (shade_sort.cu)
@@ -93,6 +94,7 @@ struct FrameParams {
     int restir_spatial;
     int restir_max_spatial;
     int restir_bias;
+    int restir_emissive;   // 1: ReSTIR DI resamples the emissive-geometry lights (opt-in; no reference counterpart)
     int record_paths;
     int sort_from_bounce;  // shade in material-bucket order from this bounce on (INT_MAX: never)
     FrameBufs cur;      // this frame's buffers
