@@ -1105,10 +1105,12 @@ rtgb_status rtgb_default_rig(const char* scene_name, int32_t camera_count, int32
         return RTGB_OK;
     }
     if (n == "triangle_terrain" || n == "triangle_terrain_pbr") {
-        // mixed rig: 2x pinhole32 640x480 (hfov 90) + 2x equi62_lut1d 1280x1024 (180 deg)
+        // mixed rig: 2x pinhole32 640x480 (hfov 90) + 2x equi62_lut1d 1280x1024 (180 deg);
+        // a given width/height applies to every camera
         for (int i = 0; i < camera_count; ++i) {
             const bool equi = i >= 2;
-            rtgb_camera c = equi ? equi_camera(1280, 1024, 180.0) : pinhole_camera(640, 480, 90.0);
+            rtgb_camera c = equi ? equi_camera(width > 0 ? width : 1280, height > 0 ? height : 1024, 180.0)
+                                 : pinhole_camera(width > 0 ? width : 640, height > 0 ? height : 480, 90.0);
             const Vec3 eye {0.0, 4.0, 0.0};
             const Vec3 dir = rotate_about({0.0, -0.35, 1.0}, {0.0, 1.0, 0.0}, kYaw[i]);
             look_at(c, eye, {eye[0] + dir[0], eye[1] + dir[1], eye[2] + dir[2]}, {0.0, 1.0, 0.0});

@@ -37,6 +37,20 @@ TRAIN_SCENES = [
 ]
 VALID_SCENE = ("random_spheres", 7, 1024)
 
+# The learned-denoiser recipe of the benchmark protocol (seeded scenes of the
+# 1 M-triangle terrain generator with constant OpenPBR materials and 256
+# emissive triangles, 256 x 256 crops, 4096-spp targets, batch 16, Adam 1e-3,
+# log-space L1), scaled down to `--c4-scenes` scenes, plus seeds of the
+# textured-room generator (seeds other than the benchmark's 0) and the scenes
+# above so the other workloads' material and lighting stay covered.
+C4_SEED0 = 100
+ROOM_SEEDS = (1, 2, 3, 4)
+
+
+def c4_scenes(count: int):
+    return ([("triangle_terrain_pbr", C4_SEED0 + i, 0) for i in range(count)]
+            + [("textured_room", s, 0) for s in ROOM_SEEDS] + TRAIN_SCENES)
+
 
 def noisy_profile():
     return scenes.profile("balanced", samples_per_pixel=1, max_bounces=4, enable_denoise=0, enable_restir_di=1,
@@ -89,13 +103,23 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--native", action="store_true", help="train with the library's kernels (rtgb_trainer_*)")
+    ap.add_argument("--recipe", choices=["default", "c4"], default="default",
+                    help="c4: the protocol's recipe (terrain-generator scenes, 256 x 256 crops, 4096-spp targets, "
+                         "batch 16, Adam 1e-3), scaled down to --c4-scenes scenes")
+    ap.add_argument("--c4-scenes", type=int, default=48)
     args = ap.parse_args(argv)
+    scene_list = TRAIN_SCENES
+    if args.recipe == "c4":
+        scene_list = c4_scenes(args.c4_scenes)
+        for name, default in (("width", 640), ("height", 480), ("target_spp", 1024), ("crop", 128), ("lr", 2e-3)):
+            if getattr(args, name) == default:
+                setattr(args, name, {"width": 320, "height": 256, "target_spp": 4096, "crop": 256, "lr": 1e-3}[name])
 
     import torch
     dev = torch.device("cuda", 0)
     t0 = time.time()
     inputs, targets = [], []
-    for name, seed, detail in TRAIN_SCENES:
+    for name, seed, detail in scene_list:
         for x, y in render_pair(name, seed, detail, args.width, args.height, 4, (2, 3, 5), args.target_spp,
                                 args.spp_per_frame):
             inputs.append(torch.from_numpy(x).to(dev))
@@ -166,7 +190,8 @@ def main(argv=None):
     flat = denoiser.flatten(model)
     denoiser.save_weights(flat, args.out, {
         "trainer": "native (rtgb_trainer_*)" if args.native else "pytorch",
-        "train_scenes": [f"{n}/{s}/{d}" for n, s, d in TRAIN_SCENES], "valid_scene": "/".join(map(str, VALID_SCENE)),
+        "recipe": args.recipe, "train_scenes": [f"{n}/{s}/{d}" for n, s, d in scene_list],
+        "valid_scene": "/".join(map(str, VALID_SCENE)), "width": args.width, "height": args.height,
         "target_spp": args.target_spp, "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
         "valid_relmse": rel, "valid_noisy_relmse": noisy})
     print(f"saved {args.out} ({time.time() - t0:.1f} s)")
