@@ -781,6 +781,36 @@ def training_record(steps: int = 10, warmup: int = 3):
             "final_loss": float(loss.value)}
 
 
+def roofline_traversal(stage_ms, frames_stats):
+    """The traversal launches measured against L2 bandwidth: k_trace and k_shadow
+    at bounce 0. Their SoA stream bytes are small next to the acceleration
+    structure they walk, so `profiles/trace_l2.json` (one ncu capture of each
+    bounce-0 launch of the benchmark frame) gives the L1, L2 and DRAM bytes
+    per ray, BVH nodes and leaf records included; achieved = L2 bytes per ray x
+    this run's rays / this run's CUDA-event time of the launch, peak = the L2
+    byte rate at 100 % of lts__t_bytes in that capture."""
+    path = ROOT / "profiles" / "trace_l2.json"
+    if not path.exists():
+        return None
+    prof = json.loads(path.read_text())
+    out = {}
+    for name, idx, rays_of in (("k_trace@0", 1, lambda st: st["active"][0]),
+                               ("k_shadow@0", 3, lambda st: st["shadow_rays_per_bounce"][0])):
+        rec = prof.get(name)
+        if not rec:
+            continue
+        rays = float(np.mean([rays_of(st) for st in frames_stats]))
+        ms = float(np.mean([t[idx] for t in stage_ms]))
+        per_ray = {k: rec[k] / rec["rays"] for k in ("l1_bytes", "l2_bytes", "dram_bytes")}
+        peak = rec["l2_bytes"] / (rec["duration_ns"] * 1e-9) / (rec["l2_pct_of_peak"] / 100.0) / 1e9
+        achieved = per_ray["l2_bytes"] * rays / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+        out[name] = {"bound": "latency (traversal)", "unit": "GB/s", "achieved": achieved, "peak": peak,
+                     "frac": achieved / peak, "peak_source": "L2 byte rate at 100 % of lts__t_bytes (ncu capture)",
+                     "l1_bytes_per_ray": per_ray["l1_bytes"], "l2_bytes_per_ray": per_ray["l2_bytes"],
+                     "dram_bytes_per_ray": per_ray["dram_bytes"], "avg_launch_ms": ms, "rays_per_launch": rays}
+    return out
+
+
 def roofline(stage_ms, frames_stats, spatial):
     """Roofline record of the launch slot (kernel at a bounce) with the largest
     average time per frame; per-unit algorithmic bytes over its
@@ -828,6 +858,25 @@ def roofline(stage_ms, frames_stats, spatial):
             "avg_launch_ms": ms / max(launches, 1), "algorithmic_bytes_per_launch": nbytes / max(launches, 1),
             "share_of_frame": ms / frame_ms if frame_ms > 0 else None,
             "stage_ms_per_frame": by_kernel}
+
+
+def profile_frames(n: int) -> None:
+    """The benchmark frame rendered `n` times without the denoiser: scene
+    preparation, then per frame raygen, (trace, material bucketing, shade,
+    shadow) per bounce with the three ReSTIR passes at bounce 0, finalize and
+    resolve; frame n-1 has full reservoir history."""
+    from ray_tracing_gb300.renderer import Renderer
+    sc, rig, prof = make_inputs()
+    prof.enable_denoise = 0
+    with Renderer() as r:
+        r.prepare_scene(sc.view)
+        r.reset_sequence(SEED)
+        for _ in range(n):
+            v = r.render_frame(rig, prof, CAMERAS)
+        print(json.dumps({"frames": n, "restir_pixels": int(v.restir_pixels),
+                          "active": [int(v.active_paths[b]) for b in range(prof.max_bounces)],
+                          "shadow": [int(v.shadow_per_bounce[b]) for b in range(prof.max_bounces)]}))
+    sc.close()
 
 
 def replica_reduce(value: float, op: str, device="cpu") -> float:
@@ -945,6 +994,7 @@ def run_ours(args, rank, world, local_rank):
         "config": workload_config(world=world),
         "rays_per_frame": rays / args.steps / world,
         "roofline": roof,
+        "roofline_traversal": roofline_traversal(stage_ms, frame_stats),
         "e2e": e2e,
         "clocks": clocks,
         "gpu_launches": launches_per_frame * args.steps,
@@ -979,6 +1029,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the persistent launch shapes instead of rtgb_autotune_launches' choice")
     ap.add_argument("--c5-size", default=None, help="WxH of the C5 cameras (default 1920x1080; for profiling)")
+    ap.add_argument("--profile-frames", type=int, default=0,
+                    help="render the benchmark frame this many times (no denoiser, no autotuning, untimed) and exit: "
+                         "a fixed launch sequence for ncu captures")
     ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke", "c4"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
@@ -991,6 +1044,10 @@ def main():
         w, h = (int(v) for v in args.c5_size.lower().split("x"))
         C5_SIZE = (w, h)
     C5_RELMSE = not args.no_relmse
+    if args.profile_frames > 0:
+        if rank == 0:
+            profile_frames(args.profile_frames)
+        return 0
     if args.workload is not None:
         if rank == 0:
             print(json.dumps({"workloads": workload_records((args.workload,), args.steps, args.warmup)}), flush=True)

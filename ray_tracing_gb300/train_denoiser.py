@@ -44,12 +44,11 @@ VALID_SCENE = ("random_spheres", 7, 1024)
 # textured-room generator (seeds other than the benchmark's 0) and the scenes
 # above so the other workloads' material and lighting stay covered.
 C4_SEED0 = 100
-ROOM_SEEDS = (1, 2, 3, 4)
 
 
-def c4_scenes(count: int):
+def c4_scenes(count: int, rooms: int):
     return ([("triangle_terrain_pbr", C4_SEED0 + i, 0) for i in range(count)]
-            + [("textured_room", s, 0) for s in ROOM_SEEDS] + TRAIN_SCENES)
+            + [("textured_room", 1 + i, 0) for i in range(rooms)] + TRAIN_SCENES)
 
 
 def noisy_profile():
@@ -107,20 +106,28 @@ def main(argv=None):
                     help="c4: the protocol's recipe (terrain-generator scenes, 256 x 256 crops, 4096-spp targets, "
                          "batch 16, Adam 1e-3), scaled down to --c4-scenes scenes")
     ap.add_argument("--c4-scenes", type=int, default=48)
+    ap.add_argument("--c4-rooms", type=int, default=12, help="textured-room seeds 1..N added to the c4 recipe")
+    ap.add_argument("--noisy-frames", default=None,
+                    help="comma-separated frame indices of each scene's sequence used as noisy inputs (default 2,3,5; "
+                         "c4: 2,5,12,24, so inputs with temporal accumulation are covered)")
     args = ap.parse_args(argv)
     scene_list = TRAIN_SCENES
+    noisy_frames = (2, 3, 5)
     if args.recipe == "c4":
-        scene_list = c4_scenes(args.c4_scenes)
+        scene_list = c4_scenes(args.c4_scenes, args.c4_rooms)
+        noisy_frames = (2, 5, 12, 24)
         for name, default in (("width", 640), ("height", 480), ("target_spp", 1024), ("crop", 128), ("lr", 2e-3)):
             if getattr(args, name) == default:
                 setattr(args, name, {"width": 320, "height": 256, "target_spp": 4096, "crop": 256, "lr": 1e-3}[name])
+    if args.noisy_frames:
+        noisy_frames = tuple(int(v) for v in args.noisy_frames.split(","))
 
     import torch
     dev = torch.device("cuda", 0)
     t0 = time.time()
     inputs, targets = [], []
     for name, seed, detail in scene_list:
-        for x, y in render_pair(name, seed, detail, args.width, args.height, 4, (2, 3, 5), args.target_spp,
+        for x, y in render_pair(name, seed, detail, args.width, args.height, 4, noisy_frames, args.target_spp,
                                 args.spp_per_frame):
             inputs.append(torch.from_numpy(x).to(dev))
             targets.append(torch.from_numpy(y).to(dev))
@@ -190,7 +197,7 @@ def main(argv=None):
     flat = denoiser.flatten(model)
     denoiser.save_weights(flat, args.out, {
         "trainer": "native (rtgb_trainer_*)" if args.native else "pytorch",
-        "recipe": args.recipe, "train_scenes": [f"{n}/{s}/{d}" for n, s, d in scene_list],
+        "recipe": args.recipe, "noisy_frames": list(noisy_frames), "train_scenes": [f"{n}/{s}/{d}" for n, s, d in scene_list],
         "valid_scene": "/".join(map(str, VALID_SCENE)), "width": args.width, "height": args.height,
         "target_spp": args.target_spp, "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
         "valid_relmse": rel, "valid_noisy_relmse": noisy})
