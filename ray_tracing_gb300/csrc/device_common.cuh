@@ -143,6 +143,25 @@ RTGB_D int sample_cdf(const float* cdf, int count, float u) {
     }
     return lo < count ? lo : count - 1;
 }
+constexpr int kGuide = 1024;          // CDF guide-table buckets
+
+// First i with u < cdf[i] (else count-1), the same index as sample_cdf, found
+// from a guide table: guide[j] = first i with j/kGuide < cdf[i] bounds the
+// answer for u in [j/kGuide, (j+1)/kGuide) between guide[j] and guide[j+1]
+// (guide[kGuide] = count), so the bisection covers one bucket.
+RTGB_D int sample_cdf_guided(const float* cdf, const int* guide, int count, float u) {
+    if (count <= 0) return -1;
+    const float s = u < 0.0f ? 0.0f : (u < 1.0f ? u : 0.99999994f);
+    const int j = static_cast<int>(s * static_cast<float>(kGuide));
+    int lo = guide[j], hi = guide[j + 1];
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s < cdf[mid]) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo < count ? lo : count - 1;
+}
+
 RTGB_HD void sample_uniform_triangle(float u0, float u1, float& w0, float& w1, float& w2) {
     const float su = sqrtf(u0 < 0.0f ? 0.0f : (u0 < 1.0f ? u0 : 1.0f));
     w0 = 1.0f - su;
@@ -467,6 +486,7 @@ struct DeviceScene {
     int sphere_count, quad_count, triangle_count, medium_count, material_count, texture_count, texel_count;
     const PackedLight* lights;
     const float* light_cdf;
+    const int* light_guide;       // kGuide + 1 bucket starts over light_cdf (sample_cdf_guided)
     int light_count;
     int environment_light;        // index into lights or -1
     const int* sphere_light;       // primitive -> light index or -1
@@ -480,6 +500,7 @@ struct DeviceScene {
     // (radiance, world_area), (analytic_light_normal, type as int bits)
     const float4* analytic_hot;
     const float* analytic_cdf;
+    const int* analytic_guide;    // kGuide + 1 bucket starts over analytic_cdf
     int analytic_count;
     const BvhNode* analytic_nodes;  // BVH over finite, non-point analytic lights
     const int* analytic_leaf;       // sorted slot -> analytic light index

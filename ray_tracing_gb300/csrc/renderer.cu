@@ -214,6 +214,7 @@ struct rtgb_renderer {
     bool denoise_this_frame = false;
     float last_denoise_ms = 0.0f;
     cudaEvent_t ev_dn0 = nullptr, ev_dn1 = nullptr;
+    DevBuf light_guide, analytic_guide;  // CDF guide tables of the NEE searches (sample_cdf_guided)
     DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
         triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
         sorted_keys, sorted_vals;
@@ -319,7 +320,8 @@ struct rtgb_renderer {
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4};
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4,
+            &light_guide, &analytic_guide};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -506,6 +508,26 @@ struct rtgb_renderer {
         RTGB_CHECK(cudaStreamSynchronize(stream));
     }
 
+    // guide[j] = first i with j / kGuide < cdf[i], by the same bisection the
+    // kernels use, guide[kGuide] = the count: sample_cdf_guided then returns
+    // exactly sample_cdf's index from one bucket.
+    static std::vector<int> cdf_guide(const std::vector<float>& cdf) {
+        const int n = static_cast<int>(cdf.size());
+        std::vector<int> g(static_cast<size_t>(kGuide) + 1);
+        for (int j = 0; j < kGuide; ++j) {
+            const float t = static_cast<float>(j) * (1.0f / static_cast<float>(kGuide));
+            int lo = 0, hi = n;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (t < cdf[static_cast<size_t>(mid)]) hi = mid;
+                else lo = mid + 1;
+            }
+            g[static_cast<size_t>(j)] = lo;
+        }
+        g[static_cast<size_t>(kGuide)] = n;
+        return g;
+    }
+
     // Uploads the scene for update kind 1 (non-geometry data; the primitives,
     // records and hierarchy stay), 2 (refit) or 3 (rebuild).
     void upload_scene(const rtgb_scene& s, int kind) {
@@ -582,6 +604,8 @@ struct rtgb_renderer {
         }
         d.lights = upload(lights, L.data(), L.size(), stream);
         d.light_cdf = upload(light_cdf, lcdf.data(), lcdf.size(), stream);
+        const std::vector<int> lguide = cdf_guide(lcdf);
+        d.light_guide = upload(light_guide, lguide.data(), lguide.size(), stream);
         d.light_count = static_cast<int>(L.size());
         d.sphere_light = upload(sphere_light, sl.data(), sl.size(), stream);
         d.quad_light = upload(quad_light, ql.data(), ql.size(), stream);
@@ -605,6 +629,8 @@ struct rtgb_renderer {
             if ((l.type >= 0 && l.type <= 3) && l.treat_as_point == 0) finite.push_back(i);
         }
         d.analytic_cdf = upload(analytic_cdf, acdf.data(), acdf.size(), stream);
+        const std::vector<int> aguide = cdf_guide(acdf);
+        d.analytic_guide = upload(analytic_guide, aguide.data(), aguide.size(), stream);
         d.infinite_analytic = upload(infinite_analytic, inf.data(), inf.size(), stream);
         d.infinite_analytic_count = static_cast<int>(inf.size());
 

@@ -195,24 +195,6 @@ RTGB_D ReservoirRec* reservoir_slot(const FrameParams& fp, const Paths& P, const
 // own register budget and occupancy; no value or draw order changes.
 
 constexpr int kMaxSources = kMaxReuseSources;
-constexpr int kGuide = 1024;          // CDF guide-table buckets
-
-// First i with u < cdf[i] (else count-1), the same index as sample_cdf, found
-// from a guide table: guide[j] = first i with j/kGuide < cdf[i] bounds the
-// answer for u in [j/kGuide, (j+1)/kGuide) between guide[j] and guide[j+1].
-RTGB_D int sample_cdf_guided(const float* cdf, const int* guide, int count, float u) {
-    if (count <= 0) return -1;
-    const float s = u < 0.0f ? 0.0f : (u < 1.0f ? u : 0.99999994f);
-    const int j = static_cast<int>(s * static_cast<float>(kGuide));
-    int lo = guide[j], hi = guide[j + 1];
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (s < cdf[mid]) hi = mid;
-        else lo = mid + 1;
-    }
-    return lo < count ? lo : count - 1;
-}
-
 // Builds guide[0..kGuide] over cdf (all threads of the block; ends with a barrier).
 RTGB_D void build_guide(const float* cdf, int count, int* guide) {
     for (int j = threadIdx.x; j <= kGuide; j += blockDim.x) {
@@ -675,7 +657,7 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
                         deferred = h.mtype != 3 && s.analytic_count > 0;
                     } else if (h.mtype != 3 && s.analytic_count > 0) {
                         // accumulate_analytic_direct_light (programs.cu:2282-2313) -> shadow slot 1
-                        const int li = sample_cdf(s.analytic_cdf, s.analytic_count, rnd(rng));
+                        const int li = sample_cdf_guided(s.analytic_cdf, s.analytic_guide, s.analytic_count, rnd(rng));
                         const float u0 = rnd(rng);
                         const float u1 = rnd(rng);
                         const LightSample l = analytic_candidate(s, h.pos, li, u0, u1);

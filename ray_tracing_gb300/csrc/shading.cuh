@@ -723,7 +723,7 @@ RTGB_D LightSample sample_direct(const DeviceScene& s, const Hit& rcv, uint32_t&
     if (eligible <= 1e-8f) return smp;
     int li = -1;
     if (ex < 0) {
-        li = sample_cdf(s.light_cdf, s.light_count, rnd(rng));
+        li = sample_cdf_guided(s.light_cdf, s.light_guide, s.light_count, rnd(rng));
     } else {
         // Receiver is itself an emitter: sequential renormalised scan, as the
         // reference accumulates it (programs.cu:1073-1093).
