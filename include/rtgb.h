@@ -445,28 +445,31 @@ rtgb_status rtgb_stage_times(rtgb_handle handle, float* out_ms, int32_t capacity
  * stays usable. */
 rtgb_status rtgb_set_debug_limits(rtgb_handle handle, int32_t traversal_limit, int32_t rejection_limit);
 
-/* Grid size (blocks) of each wavefront launch slot the handle uses now
- * (persistent sizes, or the autotuner's choice). No reference counterpart
- * (OptiX picks its own launch shapes). Fills min(capacity, count) entries;
- * *count = number of slots. */
-rtgb_status rtgb_launch_grids(rtgb_handle handle, int32_t* grids, int32_t capacity, int32_t* count);
+/* Launch shape of each wavefront launch slot the handle uses now (persistent
+ * sizes, or the autotuner's choice): grid size in blocks and threads per
+ * block (`blocks` may be NULL). No reference counterpart (OptiX picks its own
+ * launch shapes). Fills min(capacity, count) entries; *count = number of slots. */
+rtgb_status rtgb_launch_grids(rtgb_handle handle, int32_t* grids, int32_t* blocks, int32_t capacity, int32_t* count);
 
 /* Launch-shape autotuner (no reference counterpart; the reference leaves
  * launch shapes to OptiX). Renders `frames` (1..64) frames of this rig and
- * profile with the wavefront grids at each of RTGB_TUNE_CANDIDATES scales of
- * the persistent size (0.5, 1, 2, 4 x SMs x resident blocks), times every
- * stage with events, and keeps per stage group (raygen, trace, shade with
- * ReSTIR and material bucketing, shadow, finalize + resolve) the fastest
- * scale for the handle's later frames. Results never depend on the grids
- * (the kernels loop grid-stride over their queues). The tuning frames are
- * discarded: accumulation and history restart. Call after prepare_scene. */
-#define RTGB_TUNE_CANDIDATES 4
+ * profile with every wavefront launch at each of RTGB_TUNE_CANDIDATES shapes:
+ * grid scales 0.5, 1, 2, 4 of the persistent size (SMs x resident blocks) with
+ * the kernels' own block size, then the same four with half-size blocks (and
+ * twice the blocks, so the same threads); times every stage with events, and
+ * keeps per stage group (raygen, trace, shade with ReSTIR and material
+ * bucketing, shadow, finalize + resolve) the fastest shape for the handle's
+ * later frames. Results never depend on the shapes (the kernels loop
+ * grid-stride over their queues). The tuning frames are discarded:
+ * accumulation and history restart. Call after prepare_scene. */
+#define RTGB_TUNE_CANDIDATES 8
 #define RTGB_TUNE_GROUPS 5
 typedef struct rtgb_launch_tuning {
-    float scales[RTGB_TUNE_CANDIDATES];                   /* grid scales tried */
+    float scales[RTGB_TUNE_CANDIDATES];                   /* grid scales tried (of the persistent grid at that block size) */
+    int32_t block_halved[RTGB_TUNE_CANDIDATES];           /* 1: the candidate uses half-size blocks */
     float group_ms[RTGB_TUNE_CANDIDATES][RTGB_TUNE_GROUPS];/* per frame: raygen, trace, shade, shadow, finalize+resolve */
-    float frame_ms[RTGB_TUNE_CANDIDATES];                 /* whole frame at each scale */
-    int32_t chosen[RTGB_TUNE_GROUPS];                     /* index into scales, per group */
+    float frame_ms[RTGB_TUNE_CANDIDATES];                 /* whole frame at each candidate */
+    int32_t chosen[RTGB_TUNE_GROUPS];                     /* index into the candidates, per group */
     float tuned_frame_ms;                                 /* whole frame with the chosen shapes */
 } rtgb_launch_tuning;
 rtgb_status rtgb_autotune_launches(rtgb_handle handle, const rtgb_camera_rig* rig,

@@ -186,13 +186,14 @@ class FrameViews(C.Structure):
                 ("shadow_per_bounce", C.c_uint64 * 64)]
 
 
-TUNE_CANDIDATES = 4
+TUNE_CANDIDATES = 8
 TUNE_GROUPS = 5
 TUNE_GROUP_NAMES = ("raygen", "trace", "shade", "shadow", "finalize+resolve")
 
 
 class LaunchTuning(C.Structure):
-    _fields_ = [("scales", C.c_float * TUNE_CANDIDATES), ("group_ms", (C.c_float * TUNE_GROUPS) * TUNE_CANDIDATES),
+    _fields_ = [("scales", C.c_float * TUNE_CANDIDATES), ("block_halved", C.c_int32 * TUNE_CANDIDATES),
+                ("group_ms", (C.c_float * TUNE_GROUPS) * TUNE_CANDIDATES),
                 ("frame_ms", C.c_float * TUNE_CANDIDATES), ("chosen", C.c_int32 * TUNE_GROUPS),
                 ("tuned_frame_ms", C.c_float)]
 
@@ -240,7 +241,7 @@ SIGNATURES = {
     "rtgb_ray_totals": (C.c_int, [Handle, P(C.c_uint64)]),
     "rtgb_stage_times": (C.c_int, [Handle, P(C.c_float), C.c_int32, P(C.c_int32)]),
     "rtgb_set_debug_limits": (C.c_int, [Handle, C.c_int32, C.c_int32]),
-    "rtgb_launch_grids": (C.c_int, [Handle, P(C.c_int32), C.c_int32, P(C.c_int32)]),
+    "rtgb_launch_grids": (C.c_int, [Handle, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
     "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       P(C.c_float)]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),

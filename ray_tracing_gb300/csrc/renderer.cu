@@ -1418,9 +1418,12 @@ rtgb_status rtgb_set_debug_limits(rtgb_handle h, int32_t traversal_limit, int32_
     });
 }
 
-rtgb_status rtgb_launch_grids(rtgb_handle h, int32_t* grids, int32_t capacity, int32_t* count) {
+rtgb_status rtgb_launch_grids(rtgb_handle h, int32_t* grids, int32_t* blocks, int32_t capacity, int32_t* count) {
     if (!h || !count || capacity < 0 || (capacity > 0 && !grids)) return RTGB_INVALID_ARGUMENT;
-    for (int i = 0; i < capacity && i < kLaunchShapes; ++i) grids[i] = h->shapes[i].grid;
+    for (int i = 0; i < capacity && i < kLaunchShapes; ++i) {
+        grids[i] = h->shapes[i].grid;
+        if (blocks) blocks[i] = h->shapes[i].block;
+    }
     *count = kLaunchShapes;
     return RTGB_OK;
 }
@@ -1437,7 +1440,9 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
     if (!h || !rig || !profile || !out || frames < 1 || frames > 64) return RTGB_INVALID_ARGUMENT;
     return guarded(h, [&] {
         constexpr int kCandidates = RTGB_TUNE_CANDIDATES;
-        constexpr float kScales[kCandidates] = {0.5f, 1.0f, 2.0f, 4.0f};
+        // four grid scales at the kernels' block size, then the same with half-size blocks
+        constexpr float kScales[kCandidates] = {0.5f, 1.0f, 2.0f, 4.0f, 0.5f, 1.0f, 2.0f, 4.0f};
+        constexpr int kHalved[kCandidates] = {0, 0, 0, 0, 1, 1, 1, 1};
         // shape slots of each stage group (rtgb_launch_tuning::group_ms order)
         static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1}, {2, 6, 7, 8, 9, 10, 11, 12, 13}, {3}, {4, 5}};
         *out = rtgb_launch_tuning {};
@@ -1463,11 +1468,16 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         std::memcpy(restore.shapes, h->shapes, sizeof restore.shapes);
         const bool had_timing = h->stage_timing;
         h->stage_timing = true;
-        auto apply = [&](const float* scale_of_group) {
+        // a half-size block keeps the threads in flight with twice the blocks
+        auto apply = [&](const int* candidate_of_group) {
             for (int g = 0; g < RTGB_TUNE_GROUPS; ++g) {
+                const int c = candidate_of_group[g];
                 for (int slot : kGroups[g]) {
                     h->shapes[slot] = base[slot];
-                    h->shapes[slot].grid = std::max(1, static_cast<int>(static_cast<float>(base[slot].grid) * scale_of_group[g]));
+                    const int half = kHalved[c] != 0 ? 2 : 1;
+                    h->shapes[slot].block = base[slot].block / half;
+                    h->shapes[slot].grid =
+                        std::max(1, static_cast<int>(static_cast<float>(base[slot].grid * half) * kScales[c]));
                 }
             }
             h->drop_graph();
@@ -1475,10 +1485,11 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         rtgb_frame_views views {};
         std::vector<float> st(256);
         for (int c = 0; c < kCandidates; ++c) {
-            float scale[RTGB_TUNE_GROUPS];
-            for (float& x : scale) x = kScales[c];
-            apply(scale);
+            int cand[RTGB_TUNE_GROUPS];
+            for (int& x : cand) x = c;
+            apply(cand);
             out->scales[c] = kScales[c];
+            out->block_halved[c] = kHalved[c];
             if (const int st0 = h->render(*rig, *profile, active, true, &views); st0 != RTGB_OK) return static_cast<rtgb_status>(st0);  // warm
             double frame = 0.0;
             for (int f = 0; f < frames; ++f) {
@@ -1503,14 +1514,14 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
             }
             out->frame_ms[c] = static_cast<float>(frame / frames);
         }
-        float best[RTGB_TUNE_GROUPS];
+        int best[RTGB_TUNE_GROUPS];
         for (int g = 0; g < RTGB_TUNE_GROUPS; ++g) {
-            int pick = 1;  // the persistent grid unless another is faster
+            int pick = 1;  // the persistent shape unless another is faster
             for (int c = 0; c < kCandidates; ++c) {
                 if (out->group_ms[c][g] < out->group_ms[pick][g]) pick = c;
             }
             out->chosen[g] = pick;
-            best[g] = kScales[pick];
+            best[g] = pick;
         }
         apply(best);
         if (const int st2 = h->render(*rig, *profile, active, true, &views); st2 != RTGB_OK) return static_cast<rtgb_status>(st2);

@@ -6,9 +6,9 @@ namespace rtgb {
 
 void launch_restir_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
     const LaunchShape* shapes, cudaStream_t stream) {
-    k_restir_ris<true><<<shapes[11].grid, 128, 0, stream>>>(fp, scene, paths, counters);
-    k_restir_vis<true><<<shapes[12].grid, 128, 0, stream>>>(fp, scene, paths, counters);
-    k_restir<true><<<shapes[8].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_ris<true><<<shapes[11].grid, shapes[11].block, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_vis<true><<<shapes[12].grid, shapes[12].block, 0, stream>>>(fp, scene, paths, counters);
+    k_restir<true><<<shapes[8].grid, shapes[8].block, 0, stream>>>(fp, scene, paths, counters);
 }
 
 // shapes[8], [11], [12]: the final, RIS and visibility passes.

@@ -10,8 +10,8 @@ namespace rtgb {
 // k_scatter<true> (BSDF sampling, Russian roulette).
 void launch_shade_pbr(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, LaunchShape scatter_shape, cudaStream_t stream) {
-    k_shade<true, true><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
-    k_scatter<true><<<scatter_shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_shade<true, true><<<shape.grid, shape.block, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_scatter<true><<<scatter_shape.grid, scatter_shape.block, 0, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 LaunchShape query_shade_pbr_shape(int sm_count) {

@@ -354,12 +354,12 @@ void launch_camera_dirs(const CameraDev& cam, float4* out, cudaStream_t stream) 
 }
 
 void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream) {
-    k_raygen<<<shape.grid, 256, 0, stream>>>(fp, paths, counters);
+    k_raygen<<<shape.grid, shape.block, 0, stream>>>(fp, paths, counters);
 }
 
 void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream) {
-    k_trace<<<shape.grid, 128, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    k_trace<<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
@@ -368,12 +368,12 @@ void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
         launch_shade_pbr(fp, scene, paths, counters, bounce, shape, scatter_shape, stream);
         return;
     }
-    k_shade<false><<<shape.grid, 128, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_shade<false><<<shape.grid, shape.block, 0, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream) {
-    k_shadow<<<shape.grid, 128, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    k_shadow<<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
 }
 
 void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
@@ -382,17 +382,17 @@ void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counte
         launch_restir_pbr(fp, scene, paths, counters, shapes, stream);
         return;
     }
-    k_restir_ris<false><<<shapes[9].grid, 128, 0, stream>>>(fp, scene, paths, counters);
-    k_restir_vis<false><<<shapes[10].grid, 128, 0, stream>>>(fp, scene, paths, counters);
-    k_restir<false><<<shapes[6].grid, 128, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_ris<false><<<shapes[9].grid, shapes[9].block, 0, stream>>>(fp, scene, paths, counters);
+    k_restir_vis<false><<<shapes[10].grid, shapes[10].block, 0, stream>>>(fp, scene, paths, counters);
+    k_restir<false><<<shapes[6].grid, shapes[6].block, 0, stream>>>(fp, scene, paths, counters);
 }
 
 void launch_finalize(const FrameParams* fp, Paths paths, Counters* counters, LaunchShape shape, cudaStream_t stream) {
-    k_finalize<<<shape.grid, 256, 0, stream>>>(fp, paths, counters);
+    k_finalize<<<shape.grid, shape.block, 0, stream>>>(fp, paths, counters);
 }
 
 void launch_resolve(const FrameParams* fp, LaunchShape shape, cudaStream_t stream) {
-    k_resolve<<<shape.grid, 256, 0, stream>>>(fp);
+    k_resolve<<<shape.grid, shape.block, 0, stream>>>(fp);
 }
 
 void query_launch_shapes(int sm_count, LaunchShape* shapes) {

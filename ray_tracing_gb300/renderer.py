@@ -117,12 +117,13 @@ class Renderer:
         """rtgb_set_debug_limits: loop bounds of later frames (0 = default)."""
         self._check(self.lib.rtgb_set_debug_limits(self.h, traversal_limit, rejection_limit), "set_debug_limits")
 
-    def launch_grids(self) -> list[int]:
-        """rtgb_launch_grids: the grid size of every wavefront launch slot in use."""
-        buf = (C.c_int32 * 64)()
+    def launch_grids(self) -> list[tuple[int, int]]:
+        """rtgb_launch_grids: (grid, block) of every wavefront launch slot in use."""
+        grids = (C.c_int32 * 64)()
+        blocks = (C.c_int32 * 64)()
         n = C.c_int32()
-        self._check(self.lib.rtgb_launch_grids(self.h, buf, 64, C.byref(n)), "launch_grids")
-        return list(buf)[: n.value]
+        self._check(self.lib.rtgb_launch_grids(self.h, grids, blocks, 64, C.byref(n)), "launch_grids")
+        return list(zip(list(grids)[: n.value], list(blocks)[: n.value]))
 
     def autotune_launches(self, rig: abi.CameraRig, profile: abi.RenderProfile, active: int,
                           frames: int = 4) -> dict:
@@ -131,12 +132,13 @@ class Renderer:
         t = abi.LaunchTuning()
         self._check(self.lib.rtgb_autotune_launches(self.h, C.byref(rig), C.byref(profile), active, frames,
                                                     C.byref(t)), "autotune_launches")
-        scales = list(t.scales)
-        return {"scales": scales,
+        cands = [{"grid_scale": float(t.scales[c]), "block": "half" if t.block_halved[c] else "kernel's"}
+                 for c in range(abi.TUNE_CANDIDATES)]
+        return {"candidates": cands,
                 "group_ms": {abi.TUNE_GROUP_NAMES[g]: [round(t.group_ms[c][g], 4) for c in range(abi.TUNE_CANDIDATES)]
                              for g in range(abi.TUNE_GROUPS)},
                 "frame_ms": [round(x, 4) for x in t.frame_ms],
-                "chosen": {abi.TUNE_GROUP_NAMES[g]: scales[t.chosen[g]] for g in range(abi.TUNE_GROUPS)},
+                "chosen": {abi.TUNE_GROUP_NAMES[g]: cands[t.chosen[g]] for g in range(abi.TUNE_GROUPS)},
                 "tuned_frame_ms": round(t.tuned_frame_ms, 4)}
 
     def stream_ptr(self) -> int:

@@ -27,9 +27,10 @@ def test_tuned_grids_trace_the_same_paths():
     for r in (plain, tuned):
         r.prepare_scene(sc.view)
     report = tuned.autotune_launches(rig, prof, 2, frames=2)
-    assert report["scales"] == [0.5, 1.0, 2.0, 4.0]
+    assert [c["grid_scale"] for c in report["candidates"]] == [0.5, 1.0, 2.0, 4.0] * 2
+    assert [c["block"] for c in report["candidates"]] == ["kernel's"] * 4 + ["half"] * 4
     assert set(report["chosen"]) == set(abi.TUNE_GROUP_NAMES)
-    assert all(v in report["scales"] for v in report["chosen"].values())
+    assert all(v in report["candidates"] for v in report["chosen"].values())
     assert all(x > 0.0 for x in report["frame_ms"]) and report["tuned_frame_ms"] > 0.0
     for name, row in report["group_ms"].items():
         assert all(np.isfinite(row)) and min(row) >= 0.0, name
@@ -59,7 +60,7 @@ def test_a_failed_tuning_leaves_the_handle_as_it_was():
     r = Renderer()
     r.prepare_scene(sc.view)
     before = r.launch_grids()
-    assert len(before) >= 13 and min(before) > 0
+    assert len(before) >= 13 and min(g for g, _ in before) > 0 and {b for _, b in before} <= {128, 256}
     with pytest.raises(abi.RtgbError):
         r.autotune_launches(rig, bad, 2, frames=1)
     assert r.launch_grids() == before
@@ -67,5 +68,6 @@ def test_a_failed_tuning_leaves_the_handle_as_it_was():
     with pytest.raises(abi.RtgbError):
         r.stage_times()
     tuned = r.autotune_launches(rig, good, 2, frames=1)
-    assert r.launch_grids() != before or all(v == 1.0 for v in tuned["chosen"].values())
+    persistent = {"grid_scale": 1.0, "block": "kernel's"}
+    assert r.launch_grids() != before or all(v == persistent for v in tuned["chosen"].values())
     r.close()
