@@ -219,8 +219,16 @@ __global__ void k_wgrad_reduce(const float* __restrict__ partial, int ctas, int 
 }
 
 // db[o] += sum over pixels of dY (blocked layout, `hw` pixels per image); a
-// block sums a run of pixels of one 8-channel block.
-__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, int n, long long hw, int cout, float* __restrict__ db) {
+// block sums a run of pixels of one 8-channel block: each thread a strided
+// slice of 16-byte loads, then warp shuffles and a shared-memory pass across
+// the block's warps, so each block adds one value per channel (atomics on the
+// few bias words used to come from every warp and serialised in L2).
+constexpr int kBiasThreads = 256;
+constexpr int kBiasLoadsPerThread = 16;
+
+__global__ void __launch_bounds__(kBiasThreads) k_bias_grad(const __nv_bfloat16* __restrict__ dy, int n, long long hw,
+    int cout, float* __restrict__ db) {
+    __shared__ float part[kBiasThreads / 32][8];
     const int blocks = cout >> 3;
     const int cb = blockIdx.y % blocks, img = blockIdx.y / blocks;
     const __nv_bfloat16* base = dy + (static_cast<long long>(img) * blocks + cb) * hw * 8;
@@ -232,11 +240,18 @@ __global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dy, int n, long lo
 #pragma unroll
         for (int k = 0; k < 8; ++k) acc[k] += __bfloat162float(v[k]);
     }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        float s = acc[k];
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-        if ((threadIdx.x & 31) == 0) atomicAdd(db + cb * 8 + k, s);
+        float v = acc[k];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) part[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        float v = 0.0f;
+        for (int w = 0; w < kBiasThreads / 32; ++w) v += part[w][threadIdx.x];
+        atomicAdd(db + cb * 8 + threadIdx.x, v);
     }
     (void)n;
 }
@@ -294,9 +309,10 @@ cudaError_t launch_conv3x3_wgrad(const void* x, int n, int h, int w, int cin, co
     if (dbias != nullptr) {
         if ((e = cudaMemsetAsync(dbias, 0, static_cast<size_t>(cout) * sizeof(float), stream)) != cudaSuccess) return e;
         const long long hw = static_cast<long long>(h) * w;
-        long long bx = (hw + 255) / 256;
+        constexpr long long kPerBlock = static_cast<long long>(kBiasThreads) * kBiasLoadsPerThread;
+        long long bx = (hw + kPerBlock - 1) / kPerBlock;
         bx = bx < 64 ? bx : 64;
-        k_bias_grad<<<dim3(static_cast<unsigned>(bx), static_cast<unsigned>(n * (cout >> 3))), 256, 0, stream>>>(
+        k_bias_grad<<<dim3(static_cast<unsigned>(bx), static_cast<unsigned>(n * (cout >> 3))), kBiasThreads, 0, stream>>>(
             static_cast<const __nv_bfloat16*>(dy), n, hw, cout, dbias);
         e = cudaGetLastError();
     }

@@ -24,6 +24,8 @@
 #include "denoiser.cuh"
 #include "rtgb.h"
 
+#include <initializer_list>
+
 namespace rtgb {
 namespace {
 
@@ -80,50 +82,98 @@ __global__ void k_relu_mask(const __nv_bfloat16* __restrict__ g, int g_cs, int g
     }
 }
 
+// Backward passes on whole 8-channel blocks (every channel count and offset of
+// the U-Net is a multiple of 8): a thread moves one pixel's 8 channels as one
+// 16-byte load per operand, and the index arithmetic is 32-bit on (image,
+// channel block, pixel). k_relu_mask8 computes each element as k_relu_mask.
+__device__ __forceinline__ void unpack8(const uint4& q, float f[8]) {
+    const __nv_bfloat16* v = reinterpret_cast<const __nv_bfloat16*>(&q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) f[k] = bf2f(v[k]);
+}
+__device__ __forceinline__ uint4 pack8(const float f[8]) {
+    uint4 q;
+    __nv_bfloat16* v = reinterpret_cast<__nv_bfloat16*>(&q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = __float2bfloat16_rn(f[k]);
+    return q;
+}
+// 16-byte unit of channel block `cb` (of `cbs`) at pixel p of image img, hw pixels
+__device__ __forceinline__ long long unit(int img, int cbs, int cb, int hw, int p) {
+    return (static_cast<long long>(img) * cbs + cb) * hw + p;
+}
+
+__global__ void k_relu_mask8(const uint4* __restrict__ g, int g_cbs, int g_cb0, const uint4* __restrict__ y, int y_cbs,
+    int y_cb0, uint4* __restrict__ out, int o_cbs, int o_cb0, int blocks, int n, int hw) {
+    const long long total = static_cast<long long>(n) * blocks * hw;
+    for (long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; j < total;
+         j += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = static_cast<int>(j % hw);
+        const int t = static_cast<int>(j / hw);
+        const int cb = t % blocks, img = t / blocks;
+        float gv[8], yv[8], o[8];
+        unpack8(g[unit(img, g_cbs, g_cb0 + cb, hw, p)], gv);
+        unpack8(y[unit(img, y_cbs, y_cb0 + cb, hw, p)], yv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = yv[k] > 0.0f ? gv[k] : 0.0f;
+        out[unit(img, o_cbs, o_cb0 + cb, hw, p)] = pack8(o);
+    }
+}
+
 // Backward of nearest 2x upsampling followed by the ReLU of the layer that
-// produced it: out (h x w, dense `channels`) = (sum of the 2 x 2 gradient
+// produced it: out (h x w, dense channel blocks) = (sum of the 2 x 2 gradient
 // block of g) * (y > 0), y being the upsampled output itself (any pixel of
 // its 2 x 2 block holds the value).
-__global__ void k_up_backward_mask(const __nv_bfloat16* __restrict__ g, int g_cs, int g_off,
-    const __nv_bfloat16* __restrict__ y, int y_cs, int y_off, __nv_bfloat16* __restrict__ out, int channels, int n,
-    int h, int w) {
-    const int h2 = 2 * h, w2 = 2 * w;
-    const long long total = static_cast<long long>(n) * h * w * channels;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int c = static_cast<int>(i % channels);
-        long long r = i / channels;
-        const int x = static_cast<int>(r % w);
-        r /= w;
-        const int yy = static_cast<int>(r % h);
-        const int img = static_cast<int>(r / h);
-        float s = 0.0f;
-        for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx) s += bf2f(g[blk(img, g_off + c, g_cs, h2, w2, 2 * yy + dy, 2 * x + dx)]);
-        const float yv = bf2f(y[blk(img, y_off + c, y_cs, h2, w2, 2 * yy, 2 * x)]);
-        out[blk(img, c, channels, h, w, yy, x)] = __float2bfloat16_rn(yv > 0.0f ? s : 0.0f);
+__global__ void k_up_backward_mask8(const uint4* __restrict__ g, int g_cbs, int g_cb0, const uint4* __restrict__ y,
+    int y_cbs, int y_cb0, uint4* __restrict__ out, int blocks, int n, int h, int w) {
+    const int hw = h * w, w2 = 2 * w, hw2 = 4 * hw;
+    const long long total = static_cast<long long>(n) * blocks * hw;
+    for (long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; j < total;
+         j += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = static_cast<int>(j % hw);
+        const int t = static_cast<int>(j / hw);
+        const int cb = t % blocks, img = t / blocks;
+        const int yy = p / w, x = p - yy * w;
+        float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int dy = 0; dy < 2; ++dy) {
+            for (int dx = 0; dx < 2; ++dx) {
+                float v[8];
+                unpack8(g[unit(img, g_cbs, g_cb0 + cb, hw2, (2 * yy + dy) * w2 + 2 * x + dx)], v);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s[k] += v[k];
+            }
+        }
+        float yv[8], o[8];
+        unpack8(y[unit(img, y_cbs, y_cb0 + cb, hw2, 2 * yy * w2 + 2 * x)], yv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) o[k] = yv[k] > 0.0f ? s[k] : 0.0f;
+        out[unit(img, blocks, cb, hw, p)] = pack8(o);
     }
 }
 
 // Gradient of a layer whose output feeds both a skip connection (gradient g)
 // and a 2 x 2 average pooling (gradient gp at half size): out = (g + gp / 4) *
-// (y > 0) into a dense `channels` tensor (h, w even).
-__global__ void k_pool_backward_mask(const __nv_bfloat16* __restrict__ g, int g_cs, int g_off,
-    const __nv_bfloat16* __restrict__ gp, const __nv_bfloat16* __restrict__ y, int y_cs, int y_off,
-    __nv_bfloat16* __restrict__ out, int channels, int n, int h, int w) {
-    const long long total = static_cast<long long>(n) * h * w * channels;
-    for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < total;
-         i += static_cast<long long>(gridDim.x) * blockDim.x) {
-        const int c = static_cast<int>(i % channels);
-        long long r = i / channels;
-        const int x = static_cast<int>(r % w);
-        r /= w;
-        const int yy = static_cast<int>(r % h);
-        const int img = static_cast<int>(r / h);
-        const float s = bf2f(g[blk(img, g_off + c, g_cs, h, w, yy, x)]) +
-                        0.25f * bf2f(gp[blk(img, c, channels, h / 2, w / 2, yy / 2, x / 2)]);
-        const float yv = bf2f(y[blk(img, y_off + c, y_cs, h, w, yy, x)]);
-        out[blk(img, c, channels, h, w, yy, x)] = __float2bfloat16_rn(yv > 0.0f ? s : 0.0f);
+// (y > 0) into a dense tensor (h, w even).
+__global__ void k_pool_backward_mask8(const uint4* __restrict__ g, int g_cbs, int g_cb0, const uint4* __restrict__ gp,
+    const uint4* __restrict__ y, int y_cbs, int y_cb0, uint4* __restrict__ out, int blocks, int n, int h, int w) {
+    const int hw = h * w, wh = w / 2, hwh = (h / 2) * wh;
+    const long long total = static_cast<long long>(n) * blocks * hw;
+    for (long long j = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; j < total;
+         j += static_cast<long long>(gridDim.x) * blockDim.x) {
+        const int p = static_cast<int>(j % hw);
+        const int t = static_cast<int>(j / hw);
+        const int cb = t % blocks, img = t / blocks;
+        const int yy = p / w, x = p - yy * w;
+        float gv[8], pv[8], yv[8], o[8];
+        unpack8(g[unit(img, g_cbs, g_cb0 + cb, hw, p)], gv);
+        unpack8(gp[unit(img, blocks, cb, hwh, (yy / 2) * wh + x / 2)], pv);
+        unpack8(y[unit(img, y_cbs, y_cb0 + cb, hw, p)], yv);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float sv = gv[k] + 0.25f * pv[k];
+            o[k] = yv[k] > 0.0f ? sv : 0.0f;
+        }
+        out[unit(img, blocks, cb, hw, p)] = pack8(o);
     }
 }
 
@@ -359,8 +409,22 @@ struct Trainer {
         }
     }
 
+    static bool by8(std::initializer_list<int> v) {
+        for (int x : v) {
+            if (x % 8 != 0) return false;
+        }
+        return true;
+    }
+
     void mask(const void* g, int gcs, int goff, const void* y, int ycs, int yoff, void* out, int ocs, int ooff, int ch,
         int hh, int ww) {
+        if (by8({gcs, goff, ycs, yoff, ocs, ooff, ch})) {
+            k_relu_mask8<<<grid_of(static_cast<long long>(n) * hh * ww * (ch / 8)), 256, 0, stream>>>(
+                static_cast<const uint4*>(g), gcs / 8, goff / 8, static_cast<const uint4*>(y), ycs / 8, yoff / 8,
+                static_cast<uint4*>(out), ocs / 8, ooff / 8, ch / 8, n, hh * ww);
+            check(cudaGetLastError(), "mask");
+            return;
+        }
         k_relu_mask<<<grid_of(static_cast<long long>(n) * hh * ww * ch), 256, 0, stream>>>(
             static_cast<const __nv_bfloat16*>(g), gcs, goff, static_cast<const __nv_bfloat16*>(y), ycs, yoff,
             static_cast<__nv_bfloat16*>(out), ocs, ooff, ch, n, hh, ww);
@@ -381,7 +445,8 @@ struct Trainer {
         wgrad(8, cat1, h, w, g_t5);
         dgrad(8, g_t5, h, w, g_cat1, 80, 0);
         // d2b: its output was upsampled into cat1[32:80]
-        k_up_backward_mask<<<grid_of(half * 48), 256, 0, stream>>>(g_cat1, 80, 32, cat1, 80, 32, g_u7, 48, n, h2, w2);
+        k_up_backward_mask8<<<grid_of(half * 6), 256, 0, stream>>>(reinterpret_cast<const uint4*>(g_cat1), 10, 4,
+            reinterpret_cast<const uint4*>(cat1), 10, 4, reinterpret_cast<uint4*>(g_u7), 6, n, h2, w2);
         check(cudaGetLastError(), "up backward");
         wgrad(7, t4, h2, w2, g_u7);
         dgrad(7, g_u7, h2, w2, g_t4, 48, 0);
@@ -390,7 +455,8 @@ struct Trainer {
         wgrad(6, cat2, h2, w2, g_t4);
         dgrad(6, g_t4, h2, w2, g_cat2, 112, 0);
         // e3b: its output was upsampled into cat2[48:112]
-        k_up_backward_mask<<<grid_of(quarter * 64), 256, 0, stream>>>(g_cat2, 112, 48, cat2, 112, 48, g_u5, 64, n, h4, w4);
+        k_up_backward_mask8<<<grid_of(quarter * 8), 256, 0, stream>>>(reinterpret_cast<const uint4*>(g_cat2), 14, 6,
+            reinterpret_cast<const uint4*>(cat2), 14, 6, reinterpret_cast<uint4*>(g_u5), 8, n, h4, w4);
         check(cudaGetLastError(), "up backward");
         wgrad(5, t3, h4, w4, g_u5);
         dgrad(5, g_u5, h4, w4, g_t3, 64, 0);
@@ -399,7 +465,9 @@ struct Trainer {
         wgrad(4, p2, h4, w4, g_t3);
         dgrad(4, g_t3, h4, w4, g_p2, 48, 0);
         // e2b: output in cat2[0:48] (skip) and pooled into p2
-        k_pool_backward_mask<<<grid_of(half * 48), 256, 0, stream>>>(g_cat2, 112, 0, g_p2, cat2, 112, 0, g3, 48, n, h2, w2);
+        k_pool_backward_mask8<<<grid_of(half * 6), 256, 0, stream>>>(reinterpret_cast<const uint4*>(g_cat2), 14, 0,
+            reinterpret_cast<const uint4*>(g_p2), reinterpret_cast<const uint4*>(cat2), 14, 0, reinterpret_cast<uint4*>(g3), 6, n, h2,
+            w2);
         check(cudaGetLastError(), "pool backward");
         wgrad(3, t2, h2, w2, g3);
         dgrad(3, g3, h2, w2, g_t2, 48, 0);
@@ -408,7 +476,9 @@ struct Trainer {
         wgrad(2, p1, h2, w2, g_t2);
         dgrad(2, g_t2, h2, w2, g_p1, 32, 0);
         // e1b: output in cat1[0:32] (skip) and pooled into p1
-        k_pool_backward_mask<<<grid_of(full * 32), 256, 0, stream>>>(g_cat1, 80, 0, g_p1, cat1, 80, 0, g1, 32, n, h, w);
+        k_pool_backward_mask8<<<grid_of(full * 4), 256, 0, stream>>>(reinterpret_cast<const uint4*>(g_cat1), 10, 0,
+            reinterpret_cast<const uint4*>(g_p1), reinterpret_cast<const uint4*>(cat1), 10, 0, reinterpret_cast<uint4*>(g1), 4, n, h,
+            w);
         check(cudaGetLastError(), "pool backward");
         wgrad(1, t1, h, w, g1);
         dgrad(1, g1, h, w, g_t1, 32, 0);

@@ -563,7 +563,7 @@ RTGB_D int subsurface_step(const Paths& P, int path, int sss, const Hit& h, uint
 // samples the BSDF from the same RNG state, so each kernel carries only half
 // of the OpenPBR code (evaluation here, sampling there) and fewer registers.
 template <bool kPbr, bool kSplit = false>
-__global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+__global__ void __launch_bounds__(128, kSplit ? 6 : 1) k_shade(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
     const FrameParams& fp = *fpp;
     const int in = bounce & 1;
@@ -728,7 +728,7 @@ __global__ void __launch_bounds__(128, kSplit ? 4 : 1) k_shade(const FrameParams
 // apply_russian_roulette, :1764-1771) of the paths k_shade<kPbr, true> queued,
 // continuing their RNG stream where the next-event estimation left it.
 template <bool kPbr>
-__global__ void __launch_bounds__(128, 4) k_scatter(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+__global__ void __launch_bounds__(128, 6) k_scatter(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
     const FrameParams& fp = *fpp;
     const int out = (bounce & 1) ^ 1;
