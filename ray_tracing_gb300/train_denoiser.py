@@ -46,9 +46,16 @@ VALID_SCENE = ("random_spheres", 7, 1024)
 C4_SEED0 = 100
 
 
-def c4_scenes(count: int, rooms: int):
-    return ([("triangle_terrain_pbr", C4_SEED0 + i, 0) for i in range(count)]
-            + [("textured_room", 1 + i, 0) for i in range(rooms)] + TRAIN_SCENES)
+ORBIT_DEG = 2.0            # degrees per frame of the orbiting room sequences
+ORBIT_FRAMES = (5, 30, 59)  # their captured frames (each with its own target)
+
+
+def c4_scenes(count: int, rooms: int, orbit_rooms: int):
+    """(name, seed, detail, orbit degrees per frame) of the c4 recipe."""
+    return ([("triangle_terrain_pbr", C4_SEED0 + i, 0, 0.0) for i in range(count)]
+            + [("textured_room", 1 + i, 0, 0.0) for i in range(rooms)]
+            + [("textured_room", 1 + rooms + i, 0, ORBIT_DEG) for i in range(orbit_rooms)]
+            + [(n, s, d, 0.0) for n, s, d in TRAIN_SCENES])
 
 
 def noisy_profile():
@@ -60,8 +67,10 @@ def plain_profile(spp: int):
     return scenes.profile("balanced", samples_per_pixel=spp, max_bounces=4, enable_denoise=0, enable_restir_di=0)
 
 
-def render_pair(name, seed, detail, width, height, cams, noisy_frames, target_spp, spp_per_frame):
-    """Per camera: (inputs (F, H, W, 10 source channels), target (H, W, 3)) of one scene."""
+def render_pair(name, seed, detail, width, height, cams, noisy_frames, target_spp, spp_per_frame, orbit_deg=0.0):
+    """Per camera: (inputs (F, H, W, 10 source channels), target (H, W, 3)) of one scene. With `orbit_deg`
+    the rig turns about the vertical axis by that many degrees per frame (the temporal accumulation then
+    reprojects), and every captured frame gets its own target at its pose: (inputs (1, ...), target) pairs."""
     sc = scenes.HostScene(name, seed=seed, detail=detail)
     rig = scenes.default_rig(name, cams, width, height)
     r = Renderer()
@@ -69,24 +78,40 @@ def render_pair(name, seed, detail, width, height, cams, noisy_frames, target_sp
     r.reset_sequence(1000 + seed)
     prof = noisy_profile()
     frames = [[] for _ in range(cams)]
+    poses = []
     for f in range(noisy_frames[-1] + 1):
-        r.render_frame(rig, prof, cams)
+        frig = scenes.orbit_rig(rig, orbit_deg * f) if orbit_deg else rig
+        r.render_frame(frig, prof, cams)
         if f in noisy_frames:
+            poses.append(frig)
             for c in range(cams):
                 frames[c].append(np.concatenate([r.buffer(c, "beauty")[..., :3], r.buffer(c, "albedo")[..., :3],
                                                  r.buffer(c, "denoiser_normal")[..., :3],
                                                  r.buffer(c, "depth")[..., None]], axis=-1))
     pprof = plain_profile(spp_per_frame)
-    acc = [None] * cams
     n = max(1, target_spp // spp_per_frame)
-    for _ in range(n):
-        r.reset_accumulation()
-        r.render_frame(rig, pprof, cams)
-        for c in range(cams):
-            cur = r.buffer(c, "beauty")[..., :3].astype(np.float64)
-            acc[c] = cur if acc[c] is None else acc[c] + cur
+
+    def target(trig):
+        acc = [None] * cams
+        for _ in range(n):
+            r.reset_accumulation()
+            r.render_frame(trig, pprof, cams)
+            for c in range(cams):
+                cur = r.buffer(c, "beauty")[..., :3].astype(np.float64)
+                acc[c] = cur if acc[c] is None else acc[c] + cur
+        return [(a / n).astype(np.float32) for a in acc]
+
+    if orbit_deg:
+        out = []
+        for k, trig in enumerate(poses):
+            ys = target(trig)
+            out += [(frames[c][k][None].astype(np.float32), ys[c]) for c in range(cams)]
+    else:
+        ys = target(rig)
+        out = [(np.stack(frames[c]).astype(np.float32), ys[c]) for c in range(cams)]
     r.close()
-    return [(np.stack(frames[c]).astype(np.float32), (acc[c] / n).astype(np.float32)) for c in range(cams)]
+    sc.close()
+    return out
 
 
 def main(argv=None):
@@ -106,15 +131,18 @@ def main(argv=None):
                     help="c4: the protocol's recipe (terrain-generator scenes, 256 x 256 crops, 4096-spp targets, "
                          "batch 16, Adam 1e-3), scaled down to --c4-scenes scenes")
     ap.add_argument("--c4-scenes", type=int, default=48)
-    ap.add_argument("--c4-rooms", type=int, default=12, help="textured-room seeds 1..N added to the c4 recipe")
+    ap.add_argument("--c4-rooms", type=int, default=6, help="textured-room seeds 1..N added to the c4 recipe")
+    ap.add_argument("--c4-orbit-rooms", type=int, default=6,
+                    help="further textured-room seeds rendered as orbiting sequences (the rig turning 2 degrees per "
+                         "frame, frames 5, 30 and 59 captured with a target each)")
     ap.add_argument("--noisy-frames", default=None,
                     help="comma-separated frame indices of each scene's sequence used as noisy inputs (default 2,3,5; "
                          "c4: 2,5,12,24, so inputs with temporal accumulation are covered)")
     args = ap.parse_args(argv)
-    scene_list = TRAIN_SCENES
+    scene_list = [(n, s, d, 0.0) for n, s, d in TRAIN_SCENES]
     noisy_frames = (2, 3, 5)
     if args.recipe == "c4":
-        scene_list = c4_scenes(args.c4_scenes, args.c4_rooms)
+        scene_list = c4_scenes(args.c4_scenes, args.c4_rooms, args.c4_orbit_rooms)
         noisy_frames = (2, 5, 12, 24)
         for name, default in (("width", 640), ("height", 480), ("target_spp", 1024), ("crop", 128), ("lr", 2e-3)):
             if getattr(args, name) == default:
@@ -126,9 +154,9 @@ def main(argv=None):
     dev = torch.device("cuda", 0)
     t0 = time.time()
     inputs, targets = [], []
-    for name, seed, detail in scene_list:
-        for x, y in render_pair(name, seed, detail, args.width, args.height, 4, noisy_frames, args.target_spp,
-                                args.spp_per_frame):
+    for name, seed, detail, orbit in scene_list:
+        for x, y in render_pair(name, seed, detail, args.width, args.height, 4, ORBIT_FRAMES if orbit else noisy_frames,
+                                args.target_spp, args.spp_per_frame, orbit):
             inputs.append(torch.from_numpy(x).to(dev))
             targets.append(torch.from_numpy(y).to(dev))
         print(f"rendered {name}/{seed}: {time.time() - t0:.1f} s", flush=True)
@@ -197,7 +225,7 @@ def main(argv=None):
     flat = denoiser.flatten(model)
     denoiser.save_weights(flat, args.out, {
         "trainer": "native (rtgb_trainer_*)" if args.native else "pytorch",
-        "recipe": args.recipe, "noisy_frames": list(noisy_frames), "train_scenes": [f"{n}/{s}/{d}" for n, s, d in scene_list],
+        "recipe": args.recipe, "noisy_frames": list(noisy_frames), "train_scenes": [f"{n}/{s}/{d}" + (f"/orbit{o}" if o else "") for n, s, d, o in scene_list],
         "valid_scene": "/".join(map(str, VALID_SCENE)), "width": args.width, "height": args.height,
         "target_spp": args.target_spp, "steps": args.steps, "batch": args.batch, "crop": args.crop, "lr": args.lr,
         "valid_relmse": rel, "valid_noisy_relmse": noisy})
