@@ -473,6 +473,8 @@ def workload_records(names=("c1", "c3", "c5", "smoke", "c4"), steps=None, warmup
                lambda: c5_record(frames=frames["steps"], warmup=frames["warmup"]) if frames else c5_record()),
         "smoke": ("published_protocol_smoke_realtime_4x640x480", smoke_record),
         "c4": ("C4_denoiser_inference_4x1280x720", c4_inference_record),
+        "training": ("C4_training_16x256x256",
+                     lambda: training_record(**({"steps": frames["steps"], "warmup": frames["warmup"]} if frames else {}))),
     }
     for key in names:
         name, fn = jobs[key]
@@ -1032,7 +1034,7 @@ def main():
     ap.add_argument("--profile-frames", type=int, default=0,
                     help="render the benchmark frame this many times (no denoiser, no autotuning, untimed) and exit: "
                          "a fixed launch sequence for ncu captures")
-    ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke", "c4"], default=None,
+    ap.add_argument("--workload", choices=["c1", "c3", "c5", "smoke", "c4", "training"], default=None,
                     help="measure only this protocol workload (steps / warmup frames) and print its record")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
