@@ -512,8 +512,6 @@ struct DeviceScene {
     int openpbr_count;
     float background[3];
     LoopBounds bounds;              // traversal / rejection bounds and the gave-up word
-    float cell_half;                // half-extent of the cube [-h, h]^3 holding the geometry (trace-order keys)
-    float cell_scale;               // 4 / (2 h): cells of a 4 x 4 x 4 grid over that cube
 };
 
 // ---- cameras: programs.cu:304-537 ------------------------------------------------

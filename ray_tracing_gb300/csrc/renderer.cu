@@ -269,7 +269,6 @@ struct rtgb_renderer {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     bool stage_timing = false;
     int shade_order = 0;  // rtgb_create_info::shade_order
-    int trace_order_from = INT_MAX;  // bounce from which the trace queue is ordered by ray key
     // device loop bounds (rtgb_create_info debug fields, rtgb_set_debug_limits)
     int traversal_limit = kDefaultTraversalLimit;
     int rejection_limit = kDefaultRejectionLimit;
@@ -661,8 +660,6 @@ struct rtgb_renderer {
             for (int k = 0; k < 3; ++k)
                 scale = std::max({scale, std::fabs(s.triangles[i].p0[k]), std::fabs(s.triangles[i].p1[k]), std::fabs(s.triangles[i].p2[k])});
         const float pad = 1e-5f + 1e-5f * scale;
-        d.cell_half = scale > 0.0f ? scale : 1.0f;
-        d.cell_scale = 2.0f / d.cell_half;
         d.prim_count = n;
         prim_count = n;
         ScopedBuf scratch, unsorted;
@@ -985,7 +982,6 @@ struct rtgb_renderer {
         launch_raygen(d_fp, paths, d_counters, sh[0], stream);
         mark(k);
         for (int b = 0; b < mb; ++b) {
-            if (b >= trace_order_from) launch_ray_sort(d_fp, scene, paths, d_counters, b, sh[1].grid, stream);
             launch_trace(d_fp, scene, paths, d_counters, b, sh[1], stream);
             mark(k);
             launch_reset_counters(d_counters, b, stream);
@@ -1124,7 +1120,6 @@ struct rtgb_renderer {
         const bool bucket = shade_order > 0 ||
             (shade_order == 0 && (scene.openpbr_count > 0 || scene.material_count > kBucketMaterials));
         fp.sort_from_bounce = !bucket ? INT_MAX : (shade_order == 1 ? 1 : 0);
-        fp.ray_sort_from_bounce = trace_order_from;
         fp.cur = frames[cur];
         fp.hist = frames[cur ^ 1];
         // Pageable source: the copy is staged before the call returns, so the

@@ -16,7 +16,6 @@
 // Only the order in which paths are shaded changes; every path's arithmetic
 // (and so every result) is the same as without the sort. Keys: 0 miss, 1
 // analytic-light hit or medium event, 2 + material (mod kSortBins - 2).
-// The same three launches order a bounce's trace queue by ray (ray_key).
 #include "wavefront.cuh"
 
 namespace rtgb {
@@ -43,19 +42,6 @@ __device__ __forceinline__ int shade_key(const DeviceScene& s, const float4& hr)
     return 2 + (mi < 0 ? 0 : mi % (kSortBins - 2));
 }
 
-// Ray key of the trace order: the direction octant (3 bits) and the origin's
-// cell in a 4 x 4 x 4 grid over the scene's bounding cube (6 bits), so a warp
-// traces rays that start in one region and head the same way (they walk the
-// same nodes near their origin and share cached node lines).
-__device__ __forceinline__ int ray_key(const DeviceScene& s, const float4& o, const float4& d) {
-    const int oct = (d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0);
-    const float inv = s.cell_scale;  // 4 / (2 * half-extent of the bounding cube)
-    const int cx = min(3, max(0, static_cast<int>((o.x + s.cell_half) * inv)));
-    const int cy = min(3, max(0, static_cast<int>((o.y + s.cell_half) * inv)));
-    const int cz = min(3, max(0, static_cast<int>((o.z + s.cell_half) * inv)));
-    return (oct << 6) | (cx << 4) | (cy << 2) | cz;
-}
-
 // the contiguous slice of [0, count) a block owns (same split in both passes)
 __device__ __forceinline__ void chunk_of(int count, int& begin, int& end) {
     const int per = (count + static_cast<int>(gridDim.x) - 1) / static_cast<int>(gridDim.x);
@@ -63,12 +49,9 @@ __device__ __forceinline__ void chunk_of(int count, int& begin, int& end) {
     end = min(count, begin + per);
 }
 
-// kRay: keys from the rays (trace order, from FrameParams::ray_sort_from_bounce)
-// instead of from the hits (shading order, from sort_from_bounce).
-template <bool kRay>
 __global__ void __launch_bounds__(kSortBlock) k_bucket_count(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     const Counters* __restrict__ counters, int bounce) {
-    if (bounce < (kRay ? fpp->ray_sort_from_bounce : fpp->sort_from_bounce)) return;
+    if (bounce < fpp->sort_from_bounce) return;
     __shared__ int bins[kSortBins];
     for (int b = threadIdx.x; b < kSortBins; b += blockDim.x) bins[b] = 0;
     __syncthreads();
@@ -77,8 +60,7 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_count(const FrameParams* 
     chunk_of(counters->active[in], begin, end);
     const int lane = static_cast<int>(threadIdx.x) & 31;
     for (int i = begin + static_cast<int>(threadIdx.x); i < end; i += blockDim.x) {
-        const int path = P.queue[in][i];
-        const int key = kRay ? ray_key(s, P.ray_o[path], P.ray_d[path]) : shade_key(s, P.hit[path]);
+        const int key = shade_key(s, P.hit[P.queue[in][i]]);
         P.sort_key[i] = key;
         // one shared atomic per distinct key in the warp (few materials would
         // otherwise serialise 32 lanes on one address)
@@ -93,9 +75,8 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_count(const FrameParams* 
 
 // one block of kSortBins threads: exclusive scan of the histogram into the
 // bucket cursors; the histogram is zeroed for the next bounce
-template <bool kRay>
 __global__ void __launch_bounds__(kSortBins) k_bucket_scan(const FrameParams* __restrict__ fpp, Paths P, int bounce) {
-    if (bounce < (kRay ? fpp->ray_sort_from_bounce : fpp->sort_from_bounce)) return;
+    if (bounce < fpp->sort_from_bounce) return;
     __shared__ int warp_sums[kSortBins / 32];
     const int b = threadIdx.x;
     const int v = P.sort_hist[b];
@@ -120,10 +101,9 @@ __global__ void __launch_bounds__(kSortBins) k_bucket_scan(const FrameParams* __
     P.sort_hist[b] = 0;
 }
 
-template <bool kRay>
 __global__ void __launch_bounds__(kSortBlock) k_bucket_scatter(const FrameParams* __restrict__ fpp, Paths P,
     const Counters* __restrict__ counters, int bounce) {
-    if (bounce < (kRay ? fpp->ray_sort_from_bounce : fpp->sort_from_bounce)) return;
+    if (bounce < fpp->sort_from_bounce) return;
     __shared__ int bins[kSortBins];
     __shared__ int base[kSortBins];
     for (int b = threadIdx.x; b < kSortBins; b += blockDim.x) bins[b] = 0;
@@ -160,16 +140,9 @@ __global__ void __launch_bounds__(kSortBlock) k_bucket_scatter(const FrameParams
 
 void launch_shade_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
     cudaStream_t stream) {
-    k_bucket_count<false><<<grid, kSortBlock, 0, stream>>>(fp, scene, paths, counters, bounce);
-    k_bucket_scan<false><<<1, kSortBins, 0, stream>>>(fp, paths, bounce);
-    k_bucket_scatter<false><<<grid, kSortBlock, 0, stream>>>(fp, paths, counters, bounce);
-}
-
-void launch_ray_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
-    cudaStream_t stream) {
-    k_bucket_count<true><<<grid, kSortBlock, 0, stream>>>(fp, scene, paths, counters, bounce);
-    k_bucket_scan<true><<<1, kSortBins, 0, stream>>>(fp, paths, bounce);
-    k_bucket_scatter<true><<<grid, kSortBlock, 0, stream>>>(fp, paths, counters, bounce);
+    k_bucket_count<<<grid, kSortBlock, 0, stream>>>(fp, scene, paths, counters, bounce);
+    k_bucket_scan<<<1, kSortBins, 0, stream>>>(fp, paths, bounce);
+    k_bucket_scatter<<<grid, kSortBlock, 0, stream>>>(fp, paths, counters, bounce);
 }
 
 }  // namespace rtgb

@@ -104,9 +104,8 @@ __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ f
     if (blockIdx.x == 0 && threadIdx.x == 0 && bounce < 64) counters->bounce_active[bounce] = count;
     int overflow = 0;
     unsigned long long traced = 0;
-    const int* __restrict__ order = bounce >= fpp->ray_sort_from_bounce ? P.sorted : P.queue[in];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const int path = order[i];
+        const int path = P.queue[in][i];
         const float3 o = xyz(P.ray_o[path]);
         const float3 d = xyz(P.ray_d[path]);
         float closest = kRayFar;

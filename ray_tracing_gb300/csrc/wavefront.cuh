@@ -97,7 +97,6 @@ struct FrameParams {
     int restir_emissive;   // 1: ReSTIR DI resamples the emissive-geometry lights (opt-in; no reference counterpart)
     int record_paths;
     int sort_from_bounce;  // shade in material-bucket order from this bounce on (INT_MAX: never)
-    int ray_sort_from_bounce;  // trace in ray-key order (origin cell, direction octant) from this bounce on
     FrameBufs cur;      // this frame's buffers
     FrameBufs hist;     // the previous frame's (ping-pong)
 };
@@ -119,10 +118,6 @@ void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
 // `scatter_shape`: the grid of k_scatter, which the OpenPBR instance runs after k_shade.
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, LaunchShape scatter_shape, cudaStream_t stream);
-// Orders the bounce's trace queue by ray key into Paths::sorted (a no-op below
-// FrameParams::ray_sort_from_bounce); shade_sort.cu.
-void launch_ray_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
-    cudaStream_t stream);
 // Buckets the bounce's shade queue by hit material into Paths::sorted (a no-op
 // below FrameParams::sort_from_bounce); shade_sort.cu.
 void launch_shade_sort(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, int grid,
