@@ -486,6 +486,25 @@ rtgb_status rtgb_ray_totals(rtgb_handle handle, uint64_t totals[4]);
 rtgb_status rtgb_download_frame(rtgb_handle handle, int32_t camera_index, float* beauty_rgba,
     float* normal_rgba, float* albedo_rgba, float* depth, float* download_ms);
 
+/* Pipelined form of rtgb_download_frame (no counterpart in the reference,
+ * whose download waits for its copies): enqueues the same copies of the last
+ * frame's buffers on the handle's copy stream, after that frame's kernels, and
+ * returns without waiting, so the copies overlap the next frame's rendering.
+ * Page-locked host memory (cudaHostAlloc / cudaHostRegister) is needed for the
+ * overlap; with other memory the copies are still correct but the call waits
+ * for them. The host buffers must stay valid and unread until
+ * rtgb_wait_downloads returns. The frame after next, which reuses the frame's
+ * device buffers, waits for these copies on the device. Any pointer may be
+ * NULL. */
+rtgb_status rtgb_download_frame_async(rtgb_handle handle, int32_t camera_index, float* beauty_rgba,
+    float* normal_rgba, float* albedo_rgba, float* depth);
+
+/* Waits until the copies of rtgb_download_frame_async have landed in host
+ * memory: all of them (keep_latest == 0), or all but those of the most
+ * recently downloaded frame (keep_latest != 0; the double-buffered loop
+ * render(i), download_async(i), wait_downloads(1) -> frame i-1 is on the host). */
+rtgb_status rtgb_wait_downloads(rtgb_handle handle, int32_t keep_latest);
+
 /* Copies any device frame buffer of one camera (flow, trust, denoiser normal)
  * to host: which = 0 beauty (the path tracer's, before denoising), 1 normal,
  * 2 denoiser_normal, 3 albedo, 4 depth, 5 flow, 6 flow_trustworthiness,

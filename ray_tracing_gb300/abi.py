@@ -244,6 +244,8 @@ SIGNATURES = {
     "rtgb_launch_grids": (C.c_int, [Handle, P(C.c_int32), P(C.c_int32), C.c_int32, P(C.c_int32)]),
     "rtgb_download_frame": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       P(C.c_float)]),
+    "rtgb_download_frame_async": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "rtgb_wait_downloads": (C.c_int, [Handle, C.c_int32]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),
     "rtgb_restir_diagnostics": (C.c_int, [Handle, C.c_int32, P(RestirDiagnostics)]),
     "rtgb_download_reservoirs": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_size_t]),

@@ -611,8 +611,11 @@ __global__ void k_dn_upsample(const __nv_bfloat16* __restrict__ in, int n, int h
 }
 
 // Network output (channels 0..2 of a 16-channel blocked tensor, log1p
-// radiance; `hw` pixels per image) to float4.
-__global__ void k_dn_unpack(const __nv_bfloat16* __restrict__ in, long long count, long long hw, float4* __restrict__ out) {
+// radiance; `hw` pixels per image) to float4, into the current frame's
+// denoised buffer from pixel `offset` on.
+__global__ void k_dn_unpack(const FrameParams* __restrict__ fpp, const __nv_bfloat16* __restrict__ in, long long offset,
+    long long count, long long hw) {
+    float4* __restrict__ out = fpp->cur.denoised + offset;
     for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < count;
          i += static_cast<long long>(gridDim.x) * blockDim.x) {
         const long long img = i / hw, px = i - img * hw;
@@ -874,8 +877,8 @@ bool unet_prepare(UNet* unet, int n, int h, int w) {
     return true;
 }
 
-cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, int n, int h, int w, float4* out,
-    int* err, int sms, cudaStream_t stream) {
+cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, int n, int h, int w, int* err, int sms,
+    cudaStream_t stream) {
     if (!unet->ready) return cudaErrorInvalidValue;
     Acts* net = unet_buffers(unet, n, h, w);
     if (net == nullptr) return cudaErrorMemoryAllocation;
@@ -912,7 +915,7 @@ cudaError_t unet_run(UNet* unet, const FrameParams* fp, long long pixel_offset, 
     if ((e = conv(8, h, w, net->t5, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(9, h, w, net->t6, 32, 0)) != cudaSuccess) return e;
     if ((e = conv(10, h, w, net->out16, 16, 0)) != cudaSuccess) return e;
-    k_dn_unpack<<<grid_for(full, sms), 256, 0, stream>>>(net->out16, full, hw, out + pixel_offset);
+    k_dn_unpack<<<grid_for(full, sms), 256, 0, stream>>>(fp, net->out16, pixel_offset, full, hw);
     return cudaGetLastError();
 }
 

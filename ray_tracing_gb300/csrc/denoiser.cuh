@@ -73,9 +73,9 @@ long long unet_param_count();
 bool unet_prepare(UNet* net, int n, int h, int w);
 // Denoises n cameras of equal size w x h whose pixels start at `pixel_offset`
 // in the frame-wide buffers of *fp (fp->cur); writes float4 radiance into
-// out[pixel_offset ...]. `err` (device int) receives a kernel's bounded-wait
-// failure code.
-cudaError_t unet_run(UNet* net, const FrameParams* fp, long long pixel_offset, int n, int h, int w, float4* out,
-    int* err, int sm_count, cudaStream_t stream);
+// fp->cur.denoised[pixel_offset ...]. `err` (device int) receives a kernel's
+// bounded-wait failure code.
+cudaError_t unet_run(UNet* net, const FrameParams* fp, long long pixel_offset, int n, int h, int w, int* err,
+    int sm_count, cudaStream_t stream);
 
 }  // namespace rtgb

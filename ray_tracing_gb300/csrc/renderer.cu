@@ -209,7 +209,6 @@ struct rtgb_renderer {
     DevBuf openpbr, analytic_hot;
     // learned denoiser (replaces OptixDenoiserWrapper, denoiser.cpp:111-185)
     UNet* unet = nullptr;
-    DevBuf denoised;          // float4 per pixel of the last denoised frame
     bool last_denoised = false;
     bool denoise_this_frame = false;
     float last_denoise_ms = 0.0f;
@@ -267,6 +266,17 @@ struct rtgb_renderer {
     FrameParams* d_fp = nullptr;
     FrameParams h_fp{};
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    // pipelined downloads (rtgb_download_frame_async): copies of a frame's
+    // buffers run on copy_stream while the next frame renders on `stream`;
+    // the frame that reuses a buffer set waits for that set's copies
+    // (copied[slot]) on the device
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_ready = nullptr;        // end of the frame being downloaded, on `stream`
+    cudaEvent_t ev_copied[2]{};            // last copy enqueued from frames[slot]
+    cudaEvent_t ev_older_copied = nullptr; // every copy of frames before the latest downloaded one
+    bool copy_pending[2] = {false, false};
+    uint64_t frame_serial = 0;             // frames rendered
+    uint64_t download_serial = 0;          // frame_serial of the frame last downloaded asynchronously
     bool stage_timing = false;
     int shade_order = 0;  // rtgb_create_info::shade_order
     // device loop bounds (rtgb_create_info debug fields, rtgb_set_debug_limits)
@@ -313,14 +323,19 @@ struct rtgb_renderer {
 
     ~rtgb_renderer() {
         if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         drop_graph();
         unet_destroy(unet);
         if (ev_dn0) cudaEventDestroy(ev_dn0);
         if (ev_dn1) cudaEventDestroy(ev_dn1);
+        for (cudaEvent_t e : {ev_ready, ev_copied[0], ev_copied[1], ev_older_copied}) {
+            if (e) cudaEventDestroy(e);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         DevBuf* bufs[] = {&spheres, &quads, &triangles, &media, &materials, &textures, &texels, &lights, &light_cdf,
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
-            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &denoised, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4,
+            &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4,
             &light_guide, &analytic_guide};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
@@ -804,12 +819,15 @@ struct rtgb_renderer {
     }
 
     void ensure_frames(long long pixels) {
-        // beauty, normal, dnormal, albedo float4; depth, trust float; flow float2; reservoir record 96 B
-        const size_t per = 4 * 16 + 4 + 4 + 8 + sizeof(ReservoirRec);
+        // beauty, normal, dnormal, albedo, denoised float4; depth, trust float; flow float2; reservoir record 96 B
+        const size_t per = 5 * 16 + 4 + 4 + 8 + sizeof(ReservoirRec);
         for (int f = 0; f < 2; ++f) {
-            if (frame_mem[f].bytes >= static_cast<size_t>(pixels) * per + 2048 && frame_mem[f].p) continue;
+            if (frame_mem[f].bytes >= static_cast<size_t>(pixels) * per + 2304 && frame_mem[f].p) continue;
             drop_graph();
-            char* p = static_cast<char*>(frame_mem[f].ensure(static_cast<size_t>(pixels) * per + 2048));
+            // asynchronous downloads may still read the old buffers
+            if (copy_stream) RTGB_CHECK(cudaStreamSynchronize(copy_stream));
+            copy_pending[f] = false;
+            char* p = static_cast<char*>(frame_mem[f].ensure(static_cast<size_t>(pixels) * per + 2304));
             auto take = [&](size_t bytes) {
                 char* r = p;
                 p += (bytes + 255) & ~size_t(255);
@@ -824,6 +842,7 @@ struct rtgb_renderer {
             b.flow = reinterpret_cast<float2*>(take(pixels * 8));
             b.trust = reinterpret_cast<float*>(take(pixels * 4));
             b.reservoirs = reinterpret_cast<ReservoirRec*>(take(pixels * sizeof(ReservoirRec)));
+            b.denoised = reinterpret_cast<float4*>(take(pixels * 16));
         }
     }
 
@@ -1002,7 +1021,7 @@ struct rtgb_renderer {
     }
 
     // Denoises every run of consecutive equal-size cameras as one batch into
-    // `denoised`, between two external events (denoise_ms).
+    // the frame's `denoised` buffer, between two external events (denoise_ms).
     void enqueue_denoise() {
         RTGB_CHECK(cudaEventRecordWithFlags(ev_dn0, stream, cudaEventRecordExternal));
         const FrameParams& fp = h_fp;
@@ -1011,7 +1030,7 @@ struct rtgb_renderer {
             int e = c + 1;
             while (e < fp.cam_count && fp.cam[e].width == fp.cam[c].width && fp.cam[e].height == fp.cam[c].height) ++e;
             RTGB_CHECK(unet_run(unet, d_fp, fp.cam[c].pixel_offset, e - c, fp.cam[c].height, fp.cam[c].width,
-                denoised.as<float4>(), &d_counters->denoise_error, sm_count, stream));
+                &d_counters->denoise_error, sm_count, stream));
             c = e;
         }
         RTGB_CHECK(cudaEventRecordWithFlags(ev_dn1, stream, cudaEventRecordExternal));
@@ -1055,15 +1074,17 @@ struct rtgb_renderer {
         total_paths = pixels * spp;
         ensure_frames(pixels);
         ensure_paths(total_paths, spp, mb);
+        // asynchronous downloads of the frame that last used frames[cur] finish
+        // before this frame's kernels overwrite it
+        if (copy_pending[cur]) {
+            RTGB_CHECK(cudaStreamWaitEvent(stream, ev_copied[cur], 0));
+            copy_pending[cur] = false;
+        }
         denoise_this_frame = profile.enable_denoise != 0 && unet_ready(unet);
         if (denoise_this_frame) {
             if (!ev_dn0) {
                 RTGB_CHECK(cudaEventCreate(&ev_dn0));
                 RTGB_CHECK(cudaEventCreate(&ev_dn1));
-            }
-            if (denoised.bytes < static_cast<size_t>(pixels) * 16) {
-                drop_graph();
-                denoised.ensure(static_cast<size_t>(pixels) * 16);
             }
             for (int c = 0; c < active;) {
                 int e = c + 1;
@@ -1167,6 +1188,7 @@ struct rtgb_renderer {
         last_bounces = mb;
         last = cur;
         cur ^= 1;
+        ++frame_serial;
         const uint32_t used_stream = sample_stream++;
         if (out) {
             std::memset(out, 0, sizeof *out);
@@ -1205,7 +1227,7 @@ struct rtgb_renderer {
         v.camera_index = c;
         v.width = last_w[c];
         v.height = last_h[c];
-        v.beauty = last_denoised ? denoised.as<float4>() + o : f.beauty + o;
+        v.beauty = last_denoised ? f.denoised + o : f.beauty + o;
         v.normal = f.normal + o;
         v.denoiser_normal = f.dnormal + o;
         v.albedo = f.albedo + o;
@@ -1249,14 +1271,54 @@ struct rtgb_renderer {
         const FrameBufs& f = frames[last];
         const long long o = last_pixel_offset[c];
         RTGB_CHECK(cudaEventRecord(ev_start, stream));
-        const void* bsrc = last_denoised ? static_cast<const void*>(denoised.as<float4>() + o) : static_cast<const void*>(f.beauty + o);
-        if (beauty) RTGB_CHECK(cudaMemcpyAsync(beauty, bsrc, n * 16, cudaMemcpyDeviceToHost, stream));
-        if (normal) RTGB_CHECK(cudaMemcpyAsync(normal, f.normal + o, n * 16, cudaMemcpyDeviceToHost, stream));
-        if (albedo) RTGB_CHECK(cudaMemcpyAsync(albedo, f.albedo + o, n * 16, cudaMemcpyDeviceToHost, stream));
-        if (depth) RTGB_CHECK(cudaMemcpyAsync(depth, f.depth + o, n * 4, cudaMemcpyDeviceToHost, stream));
+        enqueue_copies(f, o, n, beauty, normal, albedo, depth, stream);
         RTGB_CHECK(cudaEventRecord(ev_stop, stream));
         RTGB_CHECK(cudaStreamSynchronize(stream));
         if (ms) RTGB_CHECK(cudaEventElapsedTime(ms, ev_start, ev_stop));
+    }
+
+    // beauty (denoised when the frame was), normal, albedo and depth of one camera
+    void enqueue_copies(const FrameBufs& f, long long o, size_t n, float* beauty, float* normal, float* albedo,
+        float* depth, cudaStream_t s) const {
+        const float4* bsrc = last_denoised ? f.denoised + o : f.beauty + o;
+        if (beauty) RTGB_CHECK(cudaMemcpyAsync(beauty, bsrc, n * 16, cudaMemcpyDeviceToHost, s));
+        if (normal) RTGB_CHECK(cudaMemcpyAsync(normal, f.normal + o, n * 16, cudaMemcpyDeviceToHost, s));
+        if (albedo) RTGB_CHECK(cudaMemcpyAsync(albedo, f.albedo + o, n * 16, cudaMemcpyDeviceToHost, s));
+        if (depth) RTGB_CHECK(cudaMemcpyAsync(depth, f.depth + o, n * 4, cudaMemcpyDeviceToHost, s));
+    }
+
+    // rtgb_download_frame_async: the copies of the last frame's buffers go on
+    // copy_stream after that frame's kernels; the call does not wait for them.
+    void download_async(int c, float* beauty, float* normal, float* albedo, float* depth) {
+        check_camera(c);
+        if (!copy_stream) {
+            RTGB_CHECK(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&ev_ready, &ev_copied[0], &ev_copied[1], &ev_older_copied}) {
+                RTGB_CHECK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            }
+        }
+        if (download_serial != frame_serial) {
+            // first download of a newer frame: mark where the older frames' copies end
+            RTGB_CHECK(cudaEventRecord(ev_older_copied, copy_stream));
+            download_serial = frame_serial;
+        }
+        RTGB_CHECK(cudaEventRecord(ev_ready, stream));
+        RTGB_CHECK(cudaStreamWaitEvent(copy_stream, ev_ready, 0));
+        const size_t n = static_cast<size_t>(last_w[c]) * last_h[c];
+        enqueue_copies(frames[last], last_pixel_offset[c], n, beauty, normal, albedo, depth, copy_stream);
+        RTGB_CHECK(cudaEventRecord(ev_copied[last], copy_stream));
+        copy_pending[last] = true;
+    }
+
+    // rtgb_wait_downloads: every asynchronous download, or all but those of
+    // the most recently downloaded frame, has landed in host memory
+    void wait_downloads(bool keep_latest) {
+        if (!copy_stream) return;
+        if (keep_latest) {
+            RTGB_CHECK(cudaEventSynchronize(ev_older_copied));
+        } else {
+            RTGB_CHECK(cudaStreamSynchronize(copy_stream));
+        }
     }
 
     void download_buffer(int c, int which, void* host, size_t bytes) {
@@ -1288,7 +1350,7 @@ struct rtgb_renderer {
             }
             case 8:
                 if (!last_denoised) throw Invalid{"the last frame was not denoised"};
-                src = denoised.as<float4>() + o;
+                src = f.denoised + o;
                 need = n * 16;
                 break;
             default: throw Invalid{"unknown frame buffer"};
@@ -1559,6 +1621,23 @@ rtgb_status rtgb_download_frame(rtgb_handle h, int32_t c, float* beauty, float* 
     });
 }
 
+rtgb_status rtgb_download_frame_async(rtgb_handle h, int32_t c, float* beauty, float* normal, float* albedo,
+    float* depth) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->download_async(c, beauty, normal, albedo, depth);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_wait_downloads(rtgb_handle h, int32_t keep_latest) {
+    if (!h) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->wait_downloads(keep_latest != 0);
+        return RTGB_OK;
+    });
+}
+
 rtgb_status rtgb_download_buffer(rtgb_handle h, int32_t c, int32_t which, void* host, size_t bytes) {
     if (!h || !host) return RTGB_INVALID_ARGUMENT;
     if (which < 0 || which > 8 || which == 7) return RTGB_INVALID_ARGUMENT;
@@ -1689,7 +1768,8 @@ rtgb_status rtgb_tonemap_rgba8(rtgb_handle h, int32_t c, uint8_t* host) {
         h->check_camera(c);
         const size_t n = static_cast<size_t>(h->last_w[c]) * h->last_h[c];
         h->debug_rgba.ensure(n * 4);
-        const float4* src = h->last_denoised ? h->denoised.as<float4>() : h->frames[h->last].beauty;
+        const FrameBufs& f = h->frames[h->last];
+        const float4* src = h->last_denoised ? f.denoised : f.beauty;
         launch_tonemap(src + h->last_pixel_offset[c], h->debug_rgba.as<uint8_t>(), static_cast<long long>(n), h->stream);
         RTGB_CHECK(cudaGetLastError());
         RTGB_CHECK(cudaMemcpyAsync(host, h->debug_rgba.p, n * 4, cudaMemcpyDeviceToHost, h->stream));

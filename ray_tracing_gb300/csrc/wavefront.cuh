@@ -17,6 +17,7 @@ struct FrameBufs {
     float2* flow;
     float* trust;
     ReservoirRec* reservoirs;   // 96-byte sector-ordered records (device_common.cuh)
+    float4* denoised;           // denoiser output radiance (written when the frame is denoised)
 };
 
 // Structure-of-arrays path streams, one slot per path (pixel-major, sample-minor).

@@ -162,6 +162,29 @@ class Renderer:
         return CameraFrame(cam, w, h, beauty, normal, albedo, depth, self.last_views.cameras[cam].render_ms,
                            ms.value)
 
+    @staticmethod
+    def _host_ptr(buf):
+        if buf is None:
+            return None
+        if isinstance(buf, int):
+            return buf
+        if isinstance(buf, np.ndarray):
+            return buf.ctypes.data
+        return int(buf.data_ptr())  # a torch CPU tensor (pinned for overlap)
+
+    def download_async(self, cam: int, beauty=None, normal=None, albedo=None, depth=None) -> None:
+        """rtgb_download_frame_async: enqueues the last frame's copies into the
+        given host buffers (numpy arrays, torch CPU tensors or addresses) and
+        returns; the buffers are filled once wait_downloads returns."""
+        self._check(self.lib.rtgb_download_frame_async(self.h, cam, self._host_ptr(beauty), self._host_ptr(normal),
+                                                       self._host_ptr(albedo), self._host_ptr(depth)),
+                    "download_frame_async")
+
+    def wait_downloads(self, keep_latest: bool = False) -> None:
+        """rtgb_wait_downloads: all asynchronous downloads done, or all but the
+        latest frame's."""
+        self._check(self.lib.rtgb_wait_downloads(self.h, 1 if keep_latest else 0), "wait_downloads")
+
     BUFFERS = {"beauty": (0, 4), "normal": (1, 4), "denoiser_normal": (2, 4), "albedo": (3, 4), "depth": (4, 1),
                "flow": (5, 2), "flow_trustworthiness": (6, 1), "denoised": (8, 4)}
 
