@@ -237,6 +237,40 @@ typedef struct rtgb_scene {
     int32_t openpbr_material_count;
 } rtgb_scene;
 
+/* Instanced meshes flattened on the device (rtgb_prepare_scene_instanced): the
+ * mesh half of the SceneIR v2 lowering (add_v2_mesh,
+ * src/scene/realtime_scene_adapter.cpp:289-346), with each prototype
+ * triangulated and its primvars sampled once on the host and every instance's
+ * triangles (transformed points and normals, winding, materials) produced by
+ * a kernel. */
+#define RTGB_INSTANCE_MATERIAL (-2147483647 - 1)  /* triangle_materials entry: use the instance's material */
+
+typedef struct rtgb_mesh_prototype {
+    const double* points;              /* xyz per point */
+    int32_t point_count;
+    int32_t triangle_count;            /* fan triangles of the mesh's faces, in face order */
+    const int32_t* corner_points;      /* 3 point indices per triangle (fan order, before any winding flip) */
+    const double* corner_normals;      /* 9 per triangle: the normals primvar at the 3 corners, or NULL */
+    const double* corner_texcoords;    /* 6 per triangle: the st primvar at the 3 corners, or NULL */
+    const int32_t* triangle_materials; /* per triangle: a material index (subsets) or RTGB_INSTANCE_MATERIAL */
+} rtgb_mesh_prototype;
+
+typedef struct rtgb_mesh_instance {
+    int32_t prototype;
+    int32_t material;                  /* the surface's bound material */
+    int32_t flip_winding;              /* swap corners 1 and 2 (orientation against the transform's handedness) */
+    int32_t reserved;
+    double world[12];                  /* row-major 3 x 4 affine transform */
+    double normal_matrix[9];           /* inverse of the linear part; normals transform by its transpose */
+} rtgb_mesh_instance;
+
+typedef struct rtgb_mesh_set {
+    const rtgb_mesh_prototype* prototypes;
+    int32_t prototype_count;
+    const rtgb_mesh_instance* instances; /* flattened in this order after the scene's own triangles */
+    int32_t instance_count;
+} rtgb_mesh_set;
+
 /* ------------------------------------------------------------------------ */
 /* Cameras: PackedCamera / PackedCameraRig, src/realtime/camera_rig.h:15-30  */
 /* ------------------------------------------------------------------------ */
@@ -408,6 +442,20 @@ const char* rtgb_last_error(rtgb_handle handle);
  * sample stream to 0 and the temporal history, like use_prepared_scene. */
 rtgb_status rtgb_prepare_scene(rtgb_handle handle, const rtgb_scene* scene);
 
+/* rtgb_prepare_scene with instanced meshes: the scene's own primitives, then
+ * every instance of `meshes` flattened on the device into triangles appended
+ * after the scene's triangles, bit for bit the triangles the host lowering
+ * (add_v2_mesh, realtime_scene_adapter.cpp:289-346) appends. A normal whose
+ * transformed length is not finite or at most 1e-12 fails the call with the
+ * reference's message. Reuse / update / refit / rebuild as rtgb_prepare_scene,
+ * with the mesh set part of the geometry. */
+rtgb_status rtgb_prepare_scene_instanced(rtgb_handle handle, const rtgb_scene* scene, const rtgb_mesh_set* meshes);
+
+/* The device triangle array of the prepared scene (the scene's triangles, then
+ * the flattened instances): up to `capacity` records into `out` (may be NULL)
+ * and the total in *count. */
+rtgb_status rtgb_download_triangles(rtgb_handle handle, rtgb_triangle* out, int32_t capacity, int32_t* count);
+
 /* OptixRenderer::reset_sequence (optix_renderer.cpp:178-181). */
 rtgb_status rtgb_reset_sequence(rtgb_handle handle, uint32_t sample_stream);
 
@@ -504,6 +552,17 @@ rtgb_status rtgb_download_frame_async(rtgb_handle handle, int32_t camera_index, 
  * recently downloaded frame (keep_latest != 0; the double-buffered loop
  * render(i), download_async(i), wait_downloads(1) -> frame i-1 is on the host). */
 rtgb_status rtgb_wait_downloads(rtgb_handle handle, int32_t keep_latest);
+
+/* The emissive light table of the prepared scene, built on the device
+ * (build_light_distribution, packed_scene_preparation.cpp:265-302): `lights`
+ * receives up to `capacity` 16-byte records {int32 type (0 sphere, 1 quad,
+ * 2 triangle, 3 environment), int32 primitive_index, float selection_pdf,
+ * float cdf} (the reference's PackedLight, light_sampling.h:15-27) and
+ * *light_count the table's length; each non-NULL map receives one int32 per
+ * sphere / quad / triangle of the scene: the primitive's light index or -1.
+ * lights may be NULL to query the count. */
+rtgb_status rtgb_download_light_table(rtgb_handle handle, void* lights, int32_t capacity, int32_t* light_count,
+    int32_t* sphere_light, int32_t* quad_light, int32_t* triangle_light);
 
 /* Copies any device frame buffer of one camera (flow, trust, denoiser normal)
  * to host: which = 0 beauty (the path tracer's, before denoising), 1 normal,

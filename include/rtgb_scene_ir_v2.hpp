@@ -412,4 +412,34 @@ struct AccelerationIds {
 HostScenePtr adapt_scene_ir_v2_to_realtime(const SceneIRv2& scene, AccelerationIds& ids,
     const AdaptOptions& options = {});
 
+// The mesh half of the lowering left instanced, for the device flattening of
+// rtgb_prepare_scene_instanced: each mesh prototype fan-triangulated with its
+// primvars sampled once (corner order before any winding flip, subset
+// materials or RTGB_INSTANCE_MATERIAL), each visible mesh surface one
+// instance (world transform, inverse linear part, bound material, winding
+// flip), in the order the flat lowering appends their triangles.
+struct MeshInstances {
+    struct Prototype {
+        std::vector<double> points;             // xyz per point
+        std::vector<int32_t> corner_points;     // 3 per triangle
+        std::vector<double> corner_normals;     // 9 per triangle; empty without a normals primvar
+        std::vector<double> corner_texcoords;   // 6 per triangle; empty without an st primvar
+        std::vector<int32_t> triangle_materials;
+    };
+    std::vector<Prototype> prototypes;
+    std::vector<rtgb_mesh_instance> instances;
+
+    // A view of the arrays above, valid until this object changes.
+    rtgb_mesh_set view();
+
+private:
+    std::vector<rtgb_mesh_prototype> views_;
+};
+
+// adapt_scene_ir_v2_to_realtime with the meshes in `meshes` instead of the
+// host scene's triangles; rtgb_prepare_scene_instanced(handle, &scene view,
+// &meshes.view()) then prepares the same scene as the flat lowering.
+HostScenePtr adapt_scene_ir_v2_to_realtime_instanced(const SceneIRv2& scene, MeshInstances& meshes,
+    const AdaptOptions& options = {});
+
 }  // namespace rtgb::scene

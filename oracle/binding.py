@@ -24,6 +24,7 @@ _SIGS = {
     "orc_reset_accumulation": (None, [C.c_void_p]),
     "orc_set_path_records": (None, [C.c_void_p, C.c_int]),
     "orc_sample_stream": (C.c_uint32, [C.c_void_p]),
+    "orc_light_table": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "orc_render_frame": (C.c_int, [C.c_void_p, P(abi.CameraRig), P(abi.RenderProfile), C.c_int, C.c_int, C.c_int,
                                    C.c_int]),
     "orc_get_buffer": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
@@ -113,6 +114,13 @@ class OracleRenderer:
         st = self.lib.orc_get_buffer(self.h, cam, which, out.ctypes.data, out.nbytes)
         if st != 0:
             raise RuntimeError("orc_get_buffer failed")
+        return out
+
+    def light_table(self) -> np.ndarray:
+        """build_light_distribution's PackedLight records (abi.LIGHT_DTYPE)."""
+        n = self.lib.orc_light_table(self.h, None, 0)
+        out = np.zeros(n, dtype=abi.LIGHT_DTYPE)
+        self.lib.orc_light_table(self.h, out.ctypes.data if n else None, n)
         return out
 
     def reservoirs(self, cam: int) -> np.ndarray:

@@ -2149,6 +2149,17 @@ void orc_reset_accumulation(orc_renderer* h) { h->r->reset_accumulation(); }
 void orc_set_path_records(orc_renderer* h, int on) { h->r->set_record(on != 0); }
 uint32_t orc_sample_stream(orc_renderer* h) { return h->r->stream(); }
 
+// The emissive light table of build_light_distribution: up to `capacity`
+// 16-byte PackedLight records into `lights` (may be null); returns the count.
+int orc_light_table(orc_renderer* h, void* lights, int capacity) {
+    const std::vector<orc::PackedLight>& L = h->r->scene().lights;
+    const int n = static_cast<int>(L.size());
+    if (lights != nullptr && capacity > 0) {
+        std::memcpy(lights, L.data(), sizeof(orc::PackedLight) * static_cast<size_t>(std::min(n, capacity)));
+    }
+    return n;
+}
+
 int orc_render_frame(orc_renderer* h, const rtgb_camera_rig* rig, const rtgb_render_profile* profile,
     int active, int row_begin, int row_end, int row_stride) {
     if (!h || !rig || !profile) return RTGB_INVALID_ARGUMENT;

@@ -132,6 +132,25 @@ class Scene(C.Structure):
                 ("openpbr_materials", C.POINTER(OpenPbrMaterial)), ("openpbr_material_count", C.c_int32)]
 
 
+INSTANCE_MATERIAL = -2147483648  # RTGB_INSTANCE_MATERIAL
+
+
+class MeshPrototype(C.Structure):
+    _fields_ = [("points", C.POINTER(C.c_double)), ("point_count", C.c_int32), ("triangle_count", C.c_int32),
+                ("corner_points", C.POINTER(C.c_int32)), ("corner_normals", C.POINTER(C.c_double)),
+                ("corner_texcoords", C.POINTER(C.c_double)), ("triangle_materials", C.POINTER(C.c_int32))]
+
+
+class MeshInstance(C.Structure):
+    _fields_ = [("prototype", C.c_int32), ("material", C.c_int32), ("flip_winding", C.c_int32),
+                ("reserved", C.c_int32), ("world", C.c_double * 12), ("normal_matrix", C.c_double * 9)]
+
+
+class MeshSet(C.Structure):
+    _fields_ = [("prototypes", C.POINTER(MeshPrototype)), ("prototype_count", C.c_int32),
+                ("instances", C.POINTER(MeshInstance)), ("instance_count", C.c_int32)]
+
+
 class Pinhole32(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("fx", "fy", "cx", "cy", "k1", "k2", "k3", "p1", "p2")]
 
@@ -224,6 +243,11 @@ RESERVOIR_DTYPE = np.dtype([
 ])
 assert RESERVOIR_DTYPE.itemsize == 84
 
+# 16-byte PackedLight (src/common/light_sampling.h:15-27): type 0 sphere, 1 quad,
+# 2 triangle, 3 environment
+LIGHT_DTYPE = np.dtype([("type", "<i4"), ("primitive_index", "<i4"), ("selection_pdf", "<f4"), ("cdf", "<f4")])
+assert LIGHT_DTYPE.itemsize == 16
+
 Handle = C.c_void_p
 P = C.POINTER
 
@@ -233,6 +257,8 @@ SIGNATURES = {
     "rtgb_destroy": (None, [Handle]),
     "rtgb_last_error": (C.c_char_p, [Handle]),
     "rtgb_prepare_scene": (C.c_int, [Handle, P(Scene)]),
+    "rtgb_prepare_scene_instanced": (C.c_int, [Handle, P(Scene), P(MeshSet)]),
+    "rtgb_download_triangles": (C.c_int, [Handle, C.c_void_p, C.c_int32, P(C.c_int32)]),
     "rtgb_reset_sequence": (C.c_int, [Handle, C.c_uint32]),
     "rtgb_reset_accumulation": (C.c_int, [Handle]),
     "rtgb_render_frame": (C.c_int, [Handle, P(CameraRig), P(RenderProfile), C.c_int32, P(FrameViews)]),
@@ -246,6 +272,8 @@ SIGNATURES = {
                                       P(C.c_float)]),
     "rtgb_download_frame_async": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "rtgb_wait_downloads": (C.c_int, [Handle, C.c_int32]),
+    "rtgb_download_light_table": (C.c_int, [Handle, C.c_void_p, C.c_int32, P(C.c_int32), C.c_void_p, C.c_void_p,
+                                            C.c_void_p]),
     "rtgb_download_buffer": (C.c_int, [Handle, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]),
     "rtgb_restir_diagnostics": (C.c_int, [Handle, C.c_int32, P(RestirDiagnostics)]),
     "rtgb_download_reservoirs": (C.c_int, [Handle, C.c_int32, C.c_void_p, C.c_size_t]),

@@ -17,6 +17,8 @@
 
 #include "denoiser.cuh"
 #include "lbvh.cuh"
+#include "light_table.cuh"
+#include "mesh_flatten.cuh"
 #include "openpbr.h"
 #include "wavefront.cuh"
 
@@ -214,6 +216,9 @@ struct rtgb_renderer {
     float last_denoise_ms = 0.0f;
     cudaEvent_t ev_dn0 = nullptr, ev_dn1 = nullptr;
     DevBuf light_guide, analytic_guide;  // CDF guide tables of the NEE searches (sample_cdf_guided)
+    DevBuf material_lum, light_counts;   // light table inputs; its counts (+ the LBVH scale word)
+    // device copy of an instanced mesh set (rtgb_prepare_scene_instanced, mesh_flatten.cu)
+    DevBuf mesh_points, mesh_corners, mesh_normals, mesh_texcoords, mesh_materials, mesh_protos, mesh_insts;
     DevBuf spheres, quads, triangles, media, materials, textures, texels, lights, light_cdf, sphere_light, quad_light,
         triangle_light, analytic, analytic_cdf, analytic_nodes, analytic_leaf, infinite_analytic, prims, nodes,
         sorted_keys, sorted_vals;
@@ -336,7 +341,8 @@ struct rtgb_renderer {
             &sphere_light, &quad_light, &triangle_light, &analytic, &analytic_cdf, &analytic_nodes, &analytic_leaf,
             &infinite_analytic, &prims, &nodes, &sorted_keys, &sorted_vals, &frame_mem[0], &frame_mem[1], &path_mem,
             &counters_mem, &fp_mem, &debug_rgba, &openpbr, &analytic_hot, &bvh_children, &bvh_parent, &nodes4, &child4, &ref4,
-            &light_guide, &analytic_guide};
+            &light_guide, &analytic_guide, &material_lum, &light_counts, &mesh_points, &mesh_corners, &mesh_normals,
+            &mesh_texcoords, &mesh_materials, &mesh_protos, &mesh_insts};
         for (DevBuf* b : bufs) b->release();
         for (auto& slot : cam_res) {
             for (auto& r : slot) {
@@ -421,7 +427,7 @@ struct rtgb_renderer {
         return pbr::luminance(pbr::emission(params));
     }
 
-    void validate_scene(const rtgb_scene& s) {
+    void validate_scene(const rtgb_scene& s, long long mesh_triangles = 0) {
         auto check = [&](const void* p, int n, const char* what) {
             if (n < 0 || (n > 0 && p == nullptr)) throw Invalid{std::string("scene ") + what + " array is invalid"};
         };
@@ -434,7 +440,7 @@ struct rtgb_renderer {
         check(s.media, s.medium_count, "medium");
         check(s.analytic_lights, s.analytic_light_count, "analytic light");
         check(s.openpbr_materials, s.openpbr_material_count, "OpenPBR material");
-        const long long surfaces = static_cast<long long>(s.sphere_count) + s.quad_count + s.triangle_count;
+        const long long surfaces = static_cast<long long>(s.sphere_count) + s.quad_count + s.triangle_count + mesh_triangles;
         if (surfaces == 0) throw Invalid{"render_radiance requires at least one surface primitive"};
         if (surfaces >= (1ll << 28)) throw Invalid{"scene exceeds 2^28 surface primitives"};
     }
@@ -470,6 +476,107 @@ struct rtgb_renderer {
         return fnv_array(h, s.triangles, s.triangle_count);
     }
 
+    // The mesh set's contribution to the geometry signature: every prototype
+    // array and every instance record.
+    static uint64_t mesh_signature(uint64_t h, const rtgb_mesh_set& m) {
+        for (int i = 0; i < m.prototype_count; ++i) {
+            const rtgb_mesh_prototype& p = m.prototypes[i];
+            const long long t = p.triangle_count;
+            h = fnv_array(h, p.points, 3ll * p.point_count);
+            h = fnv_array(h, p.corner_points, 3 * t);
+            h = fnv_array(h, p.corner_normals, p.corner_normals ? 9 * t : 0);
+            h = fnv_array(h, p.corner_texcoords, p.corner_texcoords ? 6 * t : 0);
+            h = fnv_array(h, p.triangle_materials, t);
+        }
+        return fnv_array(h, m.instances, m.instance_count);
+    }
+
+    // Checks a mesh set as add_v2_mesh checks a mesh; returns the number of
+    // triangles its instances flatten to.
+    static long long validate_meshes(const rtgb_mesh_set& m) {
+        if (m.prototype_count < 0 || m.instance_count < 0 || (m.prototype_count > 0 && m.prototypes == nullptr)
+            || (m.instance_count > 0 && m.instances == nullptr)) {
+            throw Invalid{"mesh set arrays are invalid"};
+        }
+        for (int i = 0; i < m.prototype_count; ++i) {
+            const rtgb_mesh_prototype& p = m.prototypes[i];
+            if (p.point_count < 0 || p.triangle_count < 0 || (p.point_count > 0 && p.points == nullptr)
+                || (p.triangle_count > 0 && (p.corner_points == nullptr || p.triangle_materials == nullptr))) {
+                throw Invalid{"mesh prototype arrays are invalid"};
+            }
+            for (long long c = 0; c < 3ll * p.triangle_count; ++c) {
+                if (p.corner_points[c] < 0 || p.corner_points[c] >= p.point_count) {
+                    throw Invalid{"SceneIR v2 mesh point index is out of range"};
+                }
+            }
+        }
+        long long n = 0;
+        for (int i = 0; i < m.instance_count; ++i) {
+            const int proto = m.instances[i].prototype;
+            if (proto < 0 || proto >= m.prototype_count) throw Invalid{"mesh instance prototype is out of range"};
+            n += m.prototypes[proto].triangle_count;
+        }
+        return n;
+    }
+
+    // Appends the mesh set's instances to d's triangles (the buffer holds the
+    // scene's own d.triangle_count and room for the instances) on the device.
+    void flatten_meshes(const rtgb_mesh_set& m, DeviceScene& d) {
+        std::vector<double> points, normals, texcoords;
+        std::vector<int> corners, mats;
+        std::vector<MeshProtoDev> protos(static_cast<size_t>(m.prototype_count));
+        for (int i = 0; i < m.prototype_count; ++i) {
+            const rtgb_mesh_prototype& p = m.prototypes[i];
+            const size_t t = static_cast<size_t>(p.triangle_count);
+            MeshProtoDev& q = protos[static_cast<size_t>(i)];
+            q.point_offset = static_cast<long long>(points.size() / 3);
+            q.tri_offset = static_cast<long long>(mats.size());
+            q.tri_count = p.triangle_count;
+            q.has_normals = p.corner_normals != nullptr;
+            q.has_texcoords = p.corner_texcoords != nullptr;
+            points.insert(points.end(), p.points, p.points + 3 * static_cast<size_t>(p.point_count));
+            corners.insert(corners.end(), p.corner_points, p.corner_points + 3 * t);
+            mats.insert(mats.end(), p.triangle_materials, p.triangle_materials + t);
+            // per-triangle arrays stay aligned with mats: zeros where a prototype has none
+            if (p.corner_normals) normals.insert(normals.end(), p.corner_normals, p.corner_normals + 9 * t);
+            else normals.resize(normals.size() + 9 * t, 0.0);
+            if (p.corner_texcoords) texcoords.insert(texcoords.end(), p.corner_texcoords, p.corner_texcoords + 6 * t);
+            else texcoords.resize(texcoords.size() + 6 * t, 0.0);
+        }
+        std::vector<MeshInstDev> insts(static_cast<size_t>(m.instance_count));
+        long long out = d.triangle_count;
+        for (int i = 0; i < m.instance_count; ++i) {
+            const rtgb_mesh_instance& src = m.instances[i];
+            MeshInstDev& q = insts[static_cast<size_t>(i)];
+            q.out_offset = out;
+            q.prototype = src.prototype;
+            q.material = src.material;
+            q.flip = src.flip_winding != 0;
+            std::memcpy(q.world, src.world, sizeof q.world);
+            std::memcpy(q.normal_matrix, src.normal_matrix, sizeof q.normal_matrix);
+            out += m.prototypes[src.prototype].triangle_count;
+        }
+        MeshSetDev set{};
+        set.points = upload(mesh_points, points.data(), points.size(), stream);
+        set.corners = upload(mesh_corners, corners.data(), corners.size(), stream);
+        set.normals = upload(mesh_normals, normals.data(), normals.size(), stream);
+        set.texcoords = upload(mesh_texcoords, texcoords.data(), texcoords.size(), stream);
+        set.materials = upload(mesh_materials, mats.data(), mats.size(), stream);
+        set.prototypes = upload(mesh_protos, protos.data(), protos.size(), stream);
+        set.instances = upload(mesh_insts, insts.data(), insts.size(), stream);
+        set.instance_count = m.instance_count;
+        set.first_out = d.triangle_count;
+        set.end_out = out;
+        int* bad = static_cast<int*>(light_counts.ensure(4 * sizeof(int))) + 3;
+        RTGB_CHECK(cudaMemsetAsync(bad, 0, sizeof(int), stream));
+        RTGB_CHECK(launch_flatten_meshes(set, const_cast<rtgb_triangle*>(d.triangles), bad, sm_count, stream));
+        int h_bad = 0;
+        RTGB_CHECK(cudaMemcpyAsync(&h_bad, bad, sizeof h_bad, cudaMemcpyDeviceToHost, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        if (h_bad != 0) throw Invalid{"SceneIR v2 contains a singular or zero-length mesh normal"};
+        d.triangle_count = static_cast<int>(out);
+    }
+
     // Everything prepare uploads besides geometry (the packed light list is a
     // function of geometry and materials, so it needs no hash of its own).
     static uint64_t scene_signature(const rtgb_scene& s, uint64_t geometry) {
@@ -486,14 +593,16 @@ struct rtgb_renderer {
     // changed, update (re-upload, keep the hierarchy) when only non-geometry
     // data changed, refit when the primitive counts are unchanged, else
     // rebuild. Every kind restarts the sample stream and drops history.
-    void prepare(const rtgb_scene& s) {
-        validate_scene(s);
+    void prepare(const rtgb_scene& s, const rtgb_mesh_set* meshes = nullptr) {
+        const long long extra = meshes ? validate_meshes(*meshes) : 0;
+        validate_scene(s, extra);
         RTGB_CHECK(cudaSetDevice(device));
         RTGB_CHECK(cudaStreamSynchronize(stream));
-        const uint64_t geo = geometry_signature(s);
+        const uint64_t geo = meshes ? mesh_signature(geometry_signature(s), *meshes) : geometry_signature(s);
         const uint64_t sig = scene_signature(s, geo);
+        const long long tri_total = s.triangle_count + extra;
         const bool topology_changed = accel_counts[0] != s.sphere_count || accel_counts[1] != s.quad_count
-                                      || accel_counts[2] != s.triangle_count;
+                                      || accel_counts[2] != tri_total;
         int kind = 0;
         if (topology_changed || !accel_valid || !prepared) kind = 3;
         else if (geo != geometry_sig) kind = 2;
@@ -502,11 +611,11 @@ struct rtgb_renderer {
             drop_graph();
             prepared = false;
             accel_valid = false;
-            upload_scene(s, kind);
+            upload_scene(s, kind, meshes);
             accel_valid = true;
             accel_counts[0] = s.sphere_count;
             accel_counts[1] = s.quad_count;
-            accel_counts[2] = s.triangle_count;
+            accel_counts[2] = static_cast<int>(tri_total);
             geometry_sig = geo;
             scene_sig = sig;
             ++generation;
@@ -545,12 +654,25 @@ struct rtgb_renderer {
 
     // Uploads the scene for update kind 1 (non-geometry data; the primitives,
     // records and hierarchy stay), 2 (refit) or 3 (rebuild).
-    void upload_scene(const rtgb_scene& s, int kind) {
+    void upload_scene(const rtgb_scene& s, int kind, const rtgb_mesh_set* meshes) {
         DeviceScene d = kind == 1 ? scene : DeviceScene{};
         if (kind >= 2) {
             d.spheres = upload(spheres, s.spheres, static_cast<size_t>(s.sphere_count), stream);
             d.quads = upload(quads, s.quads, static_cast<size_t>(s.quad_count), stream);
-            d.triangles = upload(triangles, s.triangles, static_cast<size_t>(s.triangle_count), stream);
+            // the scene's triangles, then room for the flattened instances
+            long long extra = 0;
+            for (int i = 0; meshes && i < meshes->instance_count; ++i) {
+                extra += meshes->prototypes[meshes->instances[i].prototype].triangle_count;
+            }
+            rtgb_triangle* tris = static_cast<rtgb_triangle*>(
+                triangles.ensure(std::max<size_t>(static_cast<size_t>(s.triangle_count + extra), 1) * sizeof(rtgb_triangle)));
+            if (s.triangle_count > 0) {
+                RTGB_CHECK(cudaMemcpyAsync(tris, s.triangles, static_cast<size_t>(s.triangle_count) * sizeof(rtgb_triangle),
+                    cudaMemcpyHostToDevice, stream));
+            }
+            d.triangles = tris;
+            d.triangle_count = s.triangle_count;
+            if (meshes) flatten_meshes(*meshes, d);
         }
         d.media = upload(media, s.media, static_cast<size_t>(s.medium_count), stream);
         d.materials = upload(materials, s.materials, static_cast<size_t>(s.material_count), stream);
@@ -562,69 +684,45 @@ struct rtgb_renderer {
         d.texels = s.image_texel_count > 0 ? upload(texels, s.image_texels, 3 * static_cast<size_t>(s.image_texel_count), stream) : nullptr;
         d.sphere_count = s.sphere_count;
         d.quad_count = s.quad_count;
-        d.triangle_count = s.triangle_count;
         d.medium_count = s.medium_count;
         d.material_count = s.material_count;
         d.texture_count = s.texture_count;
         d.texel_count = s.image_texel_count;
         std::memcpy(d.background, s.background, sizeof d.background);
 
-        // build_light_distribution (packed_scene_preparation.cpp:265-302)
-        std::vector<PackedLight> L;
-        std::vector<int> sl(static_cast<size_t>(s.sphere_count), -1), ql(static_cast<size_t>(s.quad_count), -1),
-            tl(static_cast<size_t>(s.triangle_count), -1);
-        auto append = [&](int type, int index, float w) {
-            if (!std::isfinite(w) || w <= 1e-12f) return;
-            L.push_back(PackedLight{type, index, w, 0.0f});
-        };
-        constexpr float kPiF = 3.14159265358979323846f;
-        for (int i = 0; i < s.sphere_count; ++i) {
-            const rtgb_sphere& sp = s.spheres[i];
-            append(0, i, 4.0f * kPiF * sp.radius * sp.radius * emission_lum(s, sp.material_index));
+        // build_light_distribution (packed_scene_preparation.cpp:265-302) on
+        // the device (light_table.cu): the emission luminance once per material
+        // here; each primitive's weight, the order-keeping compaction, the
+        // sequential normalisation and the guide table there. A primitive is
+        // at most one light, so the maps answer find_packed_light.
+        {
+            std::vector<float> mat_lum(static_cast<size_t>(s.material_count));
+            for (int m = 0; m < s.material_count; ++m) mat_lum[static_cast<size_t>(m)] = emission_lum(s, m);
+            constexpr float kPiF = 3.14159265358979323846f;
+            const LightSources src{d.spheres, d.quads, d.triangles, d.sphere_count, d.quad_count, d.triangle_count,
+                upload(material_lum, mat_lum.data(), mat_lum.size(), stream), s.material_count,
+                4.0f * kPiF * luminance(s.background[0], s.background[1], s.background[2])};
+            const size_t prims = static_cast<size_t>(d.sphere_count) + d.quad_count + d.triangle_count;
+            auto ints = [](DevBuf& b, size_t n) { return static_cast<int*>(b.ensure(std::max<size_t>(n, 1) * sizeof(int))); };
+            const LightTable lt{static_cast<PackedLight*>(lights.ensure((prims + 1) * sizeof(PackedLight))),
+                static_cast<float*>(light_cdf.ensure((prims + 1) * sizeof(float))), ints(light_guide, kGuide + 1),
+                ints(sphere_light, static_cast<size_t>(d.sphere_count)), ints(quad_light, static_cast<size_t>(d.quad_count)),
+                ints(triangle_light, static_cast<size_t>(d.triangle_count)), ints(light_counts, 4)};
+            ScopedBuf scratch;
+            scratch.ensure(light_table_scratch_bytes(static_cast<long long>(prims)));
+            RTGB_CHECK(launch_light_table(src, lt, scratch.p, stream));
+            int counts[2] = {0, -1};
+            RTGB_CHECK(cudaMemcpyAsync(counts, lt.counts, sizeof counts, cudaMemcpyDeviceToHost, stream));
+            RTGB_CHECK(cudaStreamSynchronize(stream));
+            d.lights = lt.lights;
+            d.light_cdf = lt.cdf;
+            d.light_guide = lt.guide;
+            d.light_count = counts[0];
+            d.environment_light = counts[1];
+            d.sphere_light = lt.sphere_light;
+            d.quad_light = lt.quad_light;
+            d.triangle_light = lt.triangle_light;
         }
-        for (int i = 0; i < s.quad_count; ++i) {
-            const rtgb_quad& q = s.quads[i];
-            const float cx = q.edge_u[1] * q.edge_v[2] - q.edge_u[2] * q.edge_v[1];
-            const float cy = q.edge_u[2] * q.edge_v[0] - q.edge_u[0] * q.edge_v[2];
-            const float cz = q.edge_u[0] * q.edge_v[1] - q.edge_u[1] * q.edge_v[0];
-            append(1, i, std::sqrt(cx * cx + cy * cy + cz * cz) * emission_lum(s, q.material_index));
-        }
-        for (int i = 0; i < s.triangle_count; ++i) {
-            const rtgb_triangle& t = s.triangles[i];
-            const float ax = t.p1[0] - t.p0[0], ay = t.p1[1] - t.p0[1], az = t.p1[2] - t.p0[2];
-            const float bx = t.p2[0] - t.p0[0], by = t.p2[1] - t.p0[1], bz = t.p2[2] - t.p0[2];
-            const float cx = ay * bz - az * by, cy = az * bx - ax * bz, cz = ax * by - ay * bx;
-            append(2, i, 0.5f * std::sqrt(cx * cx + cy * cy + cz * cz) * emission_lum(s, t.material_index));
-        }
-        append(3, -1, 4.0f * kPiF * luminance(s.background[0], s.background[1], s.background[2]));
-        float total = 0.0f;
-        for (const PackedLight& l : L) total += l.selection_pdf;
-        float cdf = 0.0f;
-        for (PackedLight& l : L) {
-            l.selection_pdf /= total;
-            cdf += l.selection_pdf;
-            l.cdf = cdf;
-        }
-        if (!L.empty()) L.back().cdf = 1.0f;
-        std::vector<float> lcdf(L.size());
-        d.environment_light = -1;
-        for (size_t i = 0; i < L.size(); ++i) {
-            lcdf[i] = L[i].cdf;
-            const int idx = L[i].primitive_index;
-            // find_packed_light returns the first match; a primitive appears once.
-            if (L[i].type == 0) sl[static_cast<size_t>(idx)] = static_cast<int>(i);
-            else if (L[i].type == 1) ql[static_cast<size_t>(idx)] = static_cast<int>(i);
-            else if (L[i].type == 2) tl[static_cast<size_t>(idx)] = static_cast<int>(i);
-            else if (d.environment_light < 0) d.environment_light = static_cast<int>(i);
-        }
-        d.lights = upload(lights, L.data(), L.size(), stream);
-        d.light_cdf = upload(light_cdf, lcdf.data(), lcdf.size(), stream);
-        const std::vector<int> lguide = cdf_guide(lcdf);
-        d.light_guide = upload(light_guide, lguide.data(), lguide.size(), stream);
-        d.light_count = static_cast<int>(L.size());
-        d.sphere_light = upload(sphere_light, sl.data(), sl.size(), stream);
-        d.quad_light = upload(quad_light, ql.data(), ql.size(), stream);
-        d.triangle_light = upload(triangle_light, tl.data(), tl.size(), stream);
 
         // analytic lights: CDF array, infinite list and a BVH over finite ones
         const int na = s.analytic_light_count;
@@ -651,7 +749,7 @@ struct rtgb_renderer {
 
         EventPair ev;
         RTGB_CHECK(cudaEventRecord(ev.a, stream));
-        if (kind >= 2) build_scene_bvh(s, d, kind);
+        if (kind >= 2) build_scene_bvh(d, kind);
         build_analytic_bvh(s, finite, d);
         RTGB_CHECK(cudaEventRecord(ev.b, stream));
         RTGB_CHECK(cudaStreamSynchronize(stream));
@@ -663,17 +761,16 @@ struct rtgb_renderer {
 
     // Scene LBVH: a full device build (kind 3) that keeps children/parent, or
     // a refit (kind 2) of the kept hierarchy to the new primitive boxes.
-    void build_scene_bvh(const rtgb_scene& s, DeviceScene& d, int kind) {
-        const int n = s.sphere_count + s.quad_count + s.triangle_count;
-        float scale = 0.0f;
-        for (int i = 0; i < s.sphere_count; ++i)
-            for (int k = 0; k < 3; ++k) scale = std::max(scale, std::fabs(s.spheres[i].center[k]) + std::fabs(s.spheres[i].radius));
-        for (int i = 0; i < s.quad_count; ++i)
-            for (int k = 0; k < 3; ++k)
-                scale = std::max(scale, std::fabs(s.quads[i].origin[k]) + std::fabs(s.quads[i].edge_u[k]) + std::fabs(s.quads[i].edge_v[k]));
-        for (int i = 0; i < s.triangle_count; ++i)
-            for (int k = 0; k < 3; ++k)
-                scale = std::max({scale, std::fabs(s.triangles[i].p0[k]), std::fabs(s.triangles[i].p1[k]), std::fabs(s.triangles[i].p2[k])});
+    void build_scene_bvh(DeviceScene& d, int kind) {
+        const int n = d.sphere_count + d.quad_count + d.triangle_count;
+        // the largest coordinate magnitude of any primitive (launch_scene_scale)
+        unsigned* scale_bits = static_cast<unsigned*>(light_counts.ensure(4 * sizeof(int))) + 2;
+        RTGB_CHECK(launch_scene_scale(d, scale_bits, sm_count, stream));
+        unsigned bits = 0;
+        RTGB_CHECK(cudaMemcpyAsync(&bits, scale_bits, sizeof bits, cudaMemcpyDeviceToHost, stream));
+        RTGB_CHECK(cudaStreamSynchronize(stream));
+        float scale;
+        std::memcpy(&scale, &bits, sizeof scale);
         const float pad = 1e-5f + 1e-5f * scale;
         d.prim_count = n;
         prim_count = n;
@@ -1412,6 +1509,31 @@ rtgb_status rtgb_prepare_scene(rtgb_handle h, const rtgb_scene* scene) {
     });
 }
 
+rtgb_status rtgb_prepare_scene_instanced(rtgb_handle h, const rtgb_scene* scene, const rtgb_mesh_set* meshes) {
+    if (!h || !scene || !meshes) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        h->prepare(*scene, meshes);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_triangles(rtgb_handle h, rtgb_triangle* out, int32_t capacity, int32_t* count) {
+    if (!h || capacity < 0) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->prepared) {
+            h->error = "download_triangles requires prepare_scene() first";
+            return RTGB_NOT_PREPARED;
+        }
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        const int n = std::min(capacity, h->scene.triangle_count);
+        if (count) *count = h->scene.triangle_count;
+        if (out && n > 0) {
+            RTGB_CHECK(cudaMemcpy(out, h->scene.triangles, static_cast<size_t>(n) * sizeof(rtgb_triangle), cudaMemcpyDeviceToHost));
+        }
+        return RTGB_OK;
+    });
+}
+
 rtgb_status rtgb_reset_sequence(rtgb_handle h, uint32_t s) {
     if (!h) return RTGB_INVALID_ARGUMENT;
     h->sample_stream = s;
@@ -1634,6 +1756,29 @@ rtgb_status rtgb_wait_downloads(rtgb_handle h, int32_t keep_latest) {
     if (!h) return RTGB_INVALID_ARGUMENT;
     return guarded(h, [&] {
         h->wait_downloads(keep_latest != 0);
+        return RTGB_OK;
+    });
+}
+
+rtgb_status rtgb_download_light_table(rtgb_handle h, void* lights, int32_t capacity, int32_t* light_count,
+    int32_t* sphere_light, int32_t* quad_light, int32_t* triangle_light) {
+    if (!h || capacity < 0) return RTGB_INVALID_ARGUMENT;
+    return guarded(h, [&] {
+        if (!h->prepared) {
+            h->error = "download_light_table requires prepare_scene() first";
+            return RTGB_NOT_PREPARED;
+        }
+        const DeviceScene& d = h->scene;
+        RTGB_CHECK(cudaStreamSynchronize(h->stream));
+        if (light_count) *light_count = d.light_count;
+        const int n = std::min(capacity, d.light_count);
+        if (lights && n > 0) RTGB_CHECK(cudaMemcpy(lights, d.lights, static_cast<size_t>(n) * sizeof(PackedLight), cudaMemcpyDeviceToHost));
+        auto map = [](int32_t* dst, const int* src, int count) {
+            if (dst && count > 0) RTGB_CHECK(cudaMemcpy(dst, src, static_cast<size_t>(count) * sizeof(int), cudaMemcpyDeviceToHost));
+        };
+        map(sphere_light, d.sphere_light, d.sphere_count);
+        map(quad_light, d.quad_light, d.quad_count);
+        map(triangle_light, d.triangle_light, d.triangle_count);
         return RTGB_OK;
     });
 }

@@ -585,6 +585,68 @@ void add_mesh(rtgb_host_scene& out, AccelerationIds* ids, const SceneMeshGeometr
     }
 }
 
+// add_mesh's per-prototype half: the fan triangulation, point checks,
+// sampled primvars and subset materials, independent of the instance.
+MeshInstances::Prototype mesh_prototype(const SceneMeshGeometry& mesh, const std::unordered_map<std::string, int>& materials) {
+    MeshInstances::Prototype out;
+    const ScenePrimvar* normals = find_primvar(mesh, "normals", ScenePrimvarRole::normal);
+    const ScenePrimvar* uvs = find_primvar(mesh, "st", ScenePrimvarRole::texcoord);
+    std::vector<int> face_material(mesh.face_vertex_counts.size(), RTGB_INSTANCE_MATERIAL);
+    for (const SceneMaterialSubset& s : mesh.material_subsets) {
+        const int m = material_of(materials, s.material_path);
+        for (int32_t f : s.face_indices) {
+            if (f < 0 || static_cast<size_t>(f) >= face_material.size()) throw std::invalid_argument("SceneIR v2 material subset face is out of range");
+            face_material[static_cast<size_t>(f)] = m;
+        }
+    }
+    out.points.reserve(3 * mesh.points.size());
+    for (const Vec3& p : mesh.points) out.points.insert(out.points.end(), p.begin(), p.end());
+    size_t offset = 0;
+    for (size_t face = 0; face < mesh.face_vertex_counts.size(); ++face) {
+        const size_t count = static_cast<size_t>(mesh.face_vertex_counts[face]);
+        for (size_t c = 1; c + 1 < count; ++c) {
+            const std::array<size_t, 3> corner {offset, offset + c, offset + c + 1};
+            std::array<size_t, 3> pt {};
+            for (size_t k = 0; k < 3; ++k) {
+                const int32_t v = mesh.face_vertex_indices[corner[k]];
+                if (v < 0 || static_cast<size_t>(v) >= mesh.points.size()) throw std::invalid_argument("SceneIR v2 mesh point index is out of range");
+                pt[k] = static_cast<size_t>(v);
+                out.corner_points.push_back(v);
+            }
+            for (size_t k = 0; normals && k < 3; ++k) {
+                const Vec3 n = sample_primvar<3, Vec3f, Vec3>(*normals, face, corner[k], pt[k],
+                    "realtime normal primvar requires float3 or double3 values");
+                out.corner_normals.insert(out.corner_normals.end(), n.begin(), n.end());
+            }
+            for (size_t k = 0; uvs && k < 3; ++k) {
+                const Vec2 uv = sample_primvar<2, Vec2f, Vec2>(*uvs, face, corner[k], pt[k],
+                    "realtime texcoord primvar requires float2 or double2 values");
+                out.corner_texcoords.insert(out.corner_texcoords.end(), uv.begin(), uv.end());
+            }
+            out.triangle_materials.push_back(face_material[face]);
+        }
+        offset += count;
+    }
+    return out;
+}
+
+// add_mesh's per-instance half: the transform, its inverse linear part (for
+// normals), the bound material and the winding flip.
+rtgb_mesh_instance mesh_instance(const SceneMeshGeometry& mesh, const Mat4& world, int material, int prototype,
+    bool has_normals) {
+    rtgb_mesh_instance in {};
+    in.prototype = prototype;
+    in.material = material;
+    const M::Mat3 lin = M::linear(world);
+    in.flip_winding = (mesh.orientation == SceneMeshOrientation::left_handed) != (M::det(lin) < 0.0) ? 1 : 0;
+    for (int k = 0; k < 12; ++k) in.world[k] = world[static_cast<size_t>(k)];
+    if (has_normals) {
+        const M::Mat3 inv = M::inverse(lin);
+        for (int k = 0; k < 9; ++k) in.normal_matrix[k] = inv[static_cast<size_t>(k)];
+    }
+    return in;
+}
+
 void add_sphere(rtgb_host_scene& out, AccelerationIds* ids, const SceneSphereGeometry& g, const Mat4& world, int material,
     int prototype, int instance) {
     const M::Mat3 lin = M::linear(world);
@@ -605,7 +667,7 @@ void add_sphere(rtgb_host_scene& out, AccelerationIds* ids, const SceneSphereGeo
     }
 }
 
-HostScenePtr adapt(const SceneIRv2& scene, AccelerationIds* ids, const AdaptOptions& opt) {
+HostScenePtr adapt(const SceneIRv2& scene, AccelerationIds* ids, const AdaptOptions& opt, MeshInstances* meshes = nullptr) {
     require_valid_scene_ir_v2(scene);
     HostScenePtr result(new rtgb_host_scene);
     rtgb_host_scene& out = *result;
@@ -640,6 +702,7 @@ HostScenePtr adapt(const SceneIRv2& scene, AccelerationIds* ids, const AdaptOpti
 
     const double t = scene.stage_metadata().start_time_code.value_or(0.0);
     std::unordered_map<std::string, int> prototypes;
+    std::unordered_map<std::string, int> mesh_prototypes;  // instanced lowering: prototype path -> meshes->prototypes
     int next_instance = 0;
     for (const ScenePrim& p : scene.prims()) {
         if (p.kind != ScenePrimKind::surface || !compute_scene_visibility(scene, p.path)) continue;
@@ -653,6 +716,12 @@ HostScenePtr adapt(const SceneIRv2& scene, AccelerationIds* ids, const AdaptOpti
         const Mat4 world = compute_scene_world_transform(scene, p.path, t);
         if (const auto* s = std::get_if<SceneSphereGeometry>(&*proto->geometry)) {
             add_sphere(out, ids, *s, world, material, prototype, instance);
+        } else if (meshes) {
+            const SceneMeshGeometry& mesh = std::get<SceneMeshGeometry>(*proto->geometry);
+            auto [it, fresh] = mesh_prototypes.emplace(proto->path, static_cast<int>(meshes->prototypes.size()));
+            if (fresh) meshes->prototypes.push_back(mesh_prototype(mesh, materials));
+            const bool has_normals = !meshes->prototypes[static_cast<size_t>(it->second)].corner_normals.empty();
+            meshes->instances.push_back(mesh_instance(mesh, world, material, it->second, has_normals));
         } else {
             add_mesh(out, ids, std::get<SceneMeshGeometry>(*proto->geometry), world, material, materials, prototype, instance);
         }
@@ -671,6 +740,33 @@ HostScenePtr adapt_scene_ir_v2_to_realtime(const SceneIRv2& scene, const AdaptOp
 HostScenePtr adapt_scene_ir_v2_to_realtime(const SceneIRv2& scene, AccelerationIds& ids, const AdaptOptions& options) {
     ids = AccelerationIds {};
     return adapt(scene, &ids, options);
+}
+
+HostScenePtr adapt_scene_ir_v2_to_realtime_instanced(const SceneIRv2& scene, MeshInstances& meshes,
+    const AdaptOptions& options) {
+    meshes = MeshInstances {};
+    return adapt(scene, nullptr, options, &meshes);
+}
+
+rtgb_mesh_set MeshInstances::view() {
+    views_.assign(prototypes.size(), rtgb_mesh_prototype {});
+    for (size_t i = 0; i < prototypes.size(); ++i) {
+        const Prototype& p = prototypes[i];
+        rtgb_mesh_prototype& v = views_[i];
+        v.points = p.points.data();
+        v.point_count = static_cast<int32_t>(p.points.size() / 3);
+        v.triangle_count = static_cast<int32_t>(p.triangle_materials.size());
+        v.corner_points = p.corner_points.data();
+        v.corner_normals = p.corner_normals.empty() ? nullptr : p.corner_normals.data();
+        v.corner_texcoords = p.corner_texcoords.empty() ? nullptr : p.corner_texcoords.data();
+        v.triangle_materials = p.triangle_materials.data();
+    }
+    rtgb_mesh_set set {};
+    set.prototypes = views_.data();
+    set.prototype_count = static_cast<int32_t>(views_.size());
+    set.instances = instances.data();
+    set.instance_count = static_cast<int32_t>(instances.size());
+    return set;
 }
 
 }  // namespace rtgb::scene

@@ -78,6 +78,22 @@ class Renderer:
         self._check(self.lib.rtgb_prepare_scene(self.h, C.byref(scene)), "prepare_scene")
         self._scene_ref = scene
 
+    def prepare_scene_instanced(self, scene: abi.Scene, meshes: abi.MeshSet) -> None:
+        """rtgb_prepare_scene_instanced: the scene plus `meshes`' instances
+        flattened into triangles on the device."""
+        self._check(self.lib.rtgb_prepare_scene_instanced(self.h, C.byref(scene), C.byref(meshes)),
+                    "prepare_scene_instanced")
+        self._scene_ref = scene
+
+    def triangles(self) -> np.ndarray:
+        """rtgb_download_triangles: the device triangle array, one row of raw
+        rtgb_triangle bytes (abi.Triangle's layout) per triangle."""
+        n = C.c_int32()
+        self._check(self.lib.rtgb_download_triangles(self.h, None, 0, C.byref(n)), "download_triangles")
+        out = (abi.Triangle * max(1, n.value))()
+        self._check(self.lib.rtgb_download_triangles(self.h, out, n.value, C.byref(n)), "download_triangles")
+        return np.frombuffer(out, dtype=np.uint8, count=n.value * C.sizeof(abi.Triangle)).reshape(n.value, -1)
+
     def reset_sequence(self, sample_stream: int) -> None:
         self._check(self.lib.rtgb_reset_sequence(self.h, sample_stream), "reset_sequence")
 
@@ -184,6 +200,22 @@ class Renderer:
         """rtgb_wait_downloads: all asynchronous downloads done, or all but the
         latest frame's."""
         self._check(self.lib.rtgb_wait_downloads(self.h, 1 if keep_latest else 0), "wait_downloads")
+
+    def light_table(self) -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray]:
+        """rtgb_download_light_table: the device-built PackedLight records
+        (abi.LIGHT_DTYPE) and the sphere / quad / triangle -> light maps."""
+        n = C.c_int32()
+        self._check(self.lib.rtgb_download_light_table(self.h, None, 0, C.byref(n), None, None, None),
+                    "download_light_table")
+        sc = self._scene_ref
+        tris = C.c_int32()  # the scene's triangles and any flattened instances
+        self._check(self.lib.rtgb_download_triangles(self.h, None, 0, C.byref(tris)), "download_triangles")
+        lights = np.zeros(n.value, dtype=abi.LIGHT_DTYPE)
+        maps = [np.zeros(k, dtype=np.int32) for k in (sc.sphere_count, sc.quad_count, tris.value)]
+        ptr = [m.ctypes.data if m.size else None for m in maps]
+        self._check(self.lib.rtgb_download_light_table(self.h, lights.ctypes.data if n.value else None, n.value,
+                                                       C.byref(n), *ptr), "download_light_table")
+        return lights, maps[0], maps[1], maps[2]
 
     BUFFERS = {"beauty": (0, 4), "normal": (1, 4), "denoiser_normal": (2, 4), "albedo": (3, 4), "depth": (4, 1),
                "flow": (5, 2), "flow_trustworthiness": (6, 1), "denoised": (8, 4)}

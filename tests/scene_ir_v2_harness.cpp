@@ -13,7 +13,9 @@
 // `harness DIR` runs the cases; `harness DIR --write-scene FILE` also lowers
 // the parity scene (meshes, spheres, instances, subsets, checker / image /
 // constant textures bound to OpenPBR inputs, all analytic light types) and
-// writes it with rtgb_host_scene_save for the GPU parity test.
+// writes it with rtgb_host_scene_save for the GPU parity test;
+// `harness DIR --instanced-gpu` (needs a GPU) also prepares the scene through
+// rtgb_prepare_scene_instanced and compares it with the flat lowering.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -942,9 +944,81 @@ static void openpbr_compatibility_case() {
         "an OpenPBR surface cannot replace a volume");
 }
 
+// The instanced lowering on the CPU: the same scene with every mesh triangle
+// carried by a prototype / instance instead of the host scene's triangles.
+static void instanced_case(const std::string& img) {
+    const SceneIRv2 ir = parity_scene(img);
+    const HostScenePtr flat = adapt_scene_ir_v2_to_realtime(ir);
+    MeshInstances mi;
+    const HostScenePtr base = adapt_scene_ir_v2_to_realtime_instanced(ir, mi);
+    const rtgb_scene f = view_of(flat), b = view_of(base);
+    CHECK(b.triangle_count == 0 && b.sphere_count == f.sphere_count && b.material_count == f.material_count,
+        "instanced lowering keeps everything but the mesh triangles");
+    const rtgb_mesh_set set = mi.view();
+    long long tris = 0;
+    for (int i = 0; i < set.instance_count; ++i) tris += set.prototypes[set.instances[i].prototype].triangle_count;
+    CHECK(tris == f.triangle_count, "instances flatten to the flat lowering's triangle count");
+    CHECK(set.prototype_count < set.instance_count, "instanced cubes share one prototype");
+}
+
+// rtgb_prepare_scene_instanced against rtgb_prepare_scene on a GB300: the
+// device-flattened triangles, the light table and a rendered frame must be
+// identical bytes to the flat lowering's, for each variant of the scene.
+static void instanced_gpu_case(const std::string& img) {
+    const std::vector<SceneIRv2> variants = {parity_scene(img), parity_scene(img, 0x3f, true, false),
+        parity_scene(img, 0x3f, false)};
+    for (size_t k = 0; k < variants.size(); ++k) {
+        const HostScenePtr flat = adapt_scene_ir_v2_to_realtime(variants[k]);
+        MeshInstances mi;
+        const HostScenePtr base = adapt_scene_ir_v2_to_realtime_instanced(variants[k], mi);
+        const rtgb_scene fv = view_of(flat), bv = view_of(base);
+        const rtgb_mesh_set set = mi.view();
+        rtgb_create_info info {};
+        info.use_cuda_graph = 1;
+        rtgb_handle a = nullptr, c = nullptr;
+        CHECK(rtgb_create(&info, &a) == RTGB_OK && rtgb_create(&info, &c) == RTGB_OK, "create two renderers");
+        CHECK(rtgb_prepare_scene(a, &fv) == RTGB_OK, "prepare the flat lowering");
+        CHECK(rtgb_prepare_scene_instanced(c, &bv, &set) == RTGB_OK, "prepare the instanced lowering");
+        int32_t na = 0, nc = 0;
+        rtgb_download_triangles(a, nullptr, 0, &na);
+        rtgb_download_triangles(c, nullptr, 0, &nc);
+        std::vector<rtgb_triangle> ta(static_cast<size_t>(na)), tc(static_cast<size_t>(nc));
+        rtgb_download_triangles(a, ta.data(), na, &na);
+        rtgb_download_triangles(c, tc.data(), nc, &nc);
+        CHECK(na == fv.triangle_count && nc == na, "triangle counts");
+        CHECK(std::memcmp(ta.data(), tc.data(), ta.size() * sizeof(rtgb_triangle)) == 0,
+            "device-flattened triangles equal the host lowering's bit for bit");
+        int32_t la = 0, lc = 0;
+        rtgb_download_light_table(a, nullptr, 0, &la, nullptr, nullptr, nullptr);
+        rtgb_download_light_table(c, nullptr, 0, &lc, nullptr, nullptr, nullptr);
+        std::vector<uint8_t> lta(static_cast<size_t>(la) * 16), ltc(static_cast<size_t>(lc) * 16);
+        rtgb_download_light_table(a, lta.data(), la, &la, nullptr, nullptr, nullptr);
+        rtgb_download_light_table(c, ltc.data(), lc, &lc, nullptr, nullptr, nullptr);
+        CHECK(la == lc && lta == ltc, "light tables equal");
+        rtgb_camera_rig rig {};
+        rtgb_render_profile prof {};
+        CHECK(rtgb_default_rig("cornell_box", 1, 64, 48, &rig) == RTGB_OK && rtgb_profile_preset("balanced", &prof) == RTGB_OK,
+            "rig and profile");
+        prof.samples_per_pixel = 2;
+        prof.enable_denoise = 0;
+        std::vector<float> ba(64 * 48 * 4), bc(64 * 48 * 4);
+        for (rtgb_handle h : {a, c}) {
+            rtgb_frame_views views {};
+            CHECK(rtgb_render_frame(h, &rig, &prof, 1, &views) == RTGB_OK, "render a frame");
+        }
+        rtgb_download_frame(a, 0, ba.data(), nullptr, nullptr, nullptr, nullptr);
+        rtgb_download_frame(c, 0, bc.data(), nullptr, nullptr, nullptr, nullptr);
+        CHECK(ba == bc, "rendered frames equal");
+        rtgb_destroy(a);
+        rtgb_destroy(c);
+        std::printf("instanced variant %zu: %d triangles from %d prototypes / %d instances\n", k, nc,
+            set.prototype_count, set.instance_count);
+    }
+}
+
 int main(int argc, char** argv) {
     if (argc < 2) {
-        std::fprintf(stderr, "usage: %s DIR [--write-scene FILE]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s DIR [--write-scene FILE | --write-variants DIR | --instanced-gpu]\n", argv[0]);
         return 2;
     }
     const std::filesystem::path dir = argv[1];
@@ -968,6 +1042,8 @@ int main(int argc, char** argv) {
         transform_case();
         geometry_case();
         file_case(dir);
+        instanced_case((dir / "grid.png").string());
+        if (argc >= 3 && std::string(argv[2]) == "--instanced-gpu") instanced_gpu_case((dir / "grid.png").string());
         {
             const HostScenePtr h = adapt_scene_ir_v2_to_realtime(parity_scene((dir / "grid.png").string()));
             const rtgb_scene v = view_of(h);

@@ -36,7 +36,8 @@ STRUCTS = {
     "rtgb_camera_frame_view": abi.CameraFrameView, "rtgb_frame_views": abi.FrameViews,
     "rtgb_restir_stats": abi.RestirDiagnostics, "rtgb_acceleration_info": abi.AccelerationInfo,
     "rtgb_openpbr_material": abi.OpenPbrMaterial, "rtgb_device_info": abi.DeviceInfo,
-    "rtgb_launch_tuning": abi.LaunchTuning,
+    "rtgb_launch_tuning": abi.LaunchTuning, "rtgb_mesh_prototype": abi.MeshPrototype,
+    "rtgb_mesh_instance": abi.MeshInstance, "rtgb_mesh_set": abi.MeshSet,
 }
 
 

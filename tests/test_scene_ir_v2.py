@@ -48,6 +48,18 @@ def parity_scene_file(tmp_path_factory):
     return out
 
 
+@pytest.mark.gpu
+def test_instanced_lowering_flattens_on_the_device_like_the_host(parity_scene_file):
+    # rtgb_prepare_scene_instanced (mesh_flatten.cu) against rtgb_prepare_scene
+    # of the flat lowering: triangles, light table and a frame, bit for bit
+    exe = parity_scene_file.parent / "harness"
+    res = subprocess.run([str(exe), str(parity_scene_file.parent), "--instanced-gpu"], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "failures=0" in res.stdout
+    assert res.stdout.count("instanced variant") == 3
+
+
 def test_harness_cases_pass_and_the_scene_file_loads(parity_scene_file):
     sc = scenes.HostScene.load(parity_scene_file)
     c = sc.counts()
