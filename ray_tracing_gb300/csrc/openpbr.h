@@ -1020,7 +1020,10 @@ PBR_HD V3 reflection_fresnel(const Mat& m, float cm, float co, bool entering, co
 
 // ---- evaluate_openpbr_core (openpbr_core.h:1679-1860) ---------------------------------
 
-PBR_CALL Eval evaluate(const Mat& m, Frame f, const V3& wo_world, const V3& wi_world, const Context& ctx) {
+// The body, inlined where the call is hot (the shade kernel's next-event
+// estimation, the BSDF sampler's own evaluation); `evaluate` below is the
+// out-of-line copy the ReSTIR kernels' many call sites share.
+PBR_HD Eval evaluate_inline(const Mat& m, Frame f, const V3& wo_world, const V3& wi_world, const Context& ctx) {
     Eval res{zero3(), 0.0f};
     const V3 won = vnorm(wo_world);
     const V3 win = vnorm(wi_world);
@@ -1128,6 +1131,10 @@ PBR_CALL Eval evaluate(const Mat& m, Frame f, const V3& wo_world, const V3& wi_w
     return res;
 }
 
+PBR_CALL Eval evaluate(const Mat& m, Frame f, const V3& wo_world, const V3& wi_world, const Context& ctx) {
+    return evaluate_inline(m, f, wo_world, wi_world, ctx);
+}
+
 // emission_openpbr_core (openpbr_core.h:1868-1883)
 PBR_HD V3 emission(const Mat& m) {
     V3 e = vmul(nonneg(m.emission_color), mx(0.0f, m.emission_luminance) * sat(m.geometry_opacity));
@@ -1174,7 +1181,7 @@ PBR_HD Sample empty_sample() {
 PBR_HD Sample finish_from_eval(Sample s, const Mat& m, const Frame& authored, const Frame& f, const V3& won, const V3& wi,
     const Context& ctx) {
     s.wi = vnorm(to_world(f, wi));
-    const Eval e = evaluate(m, authored, won, s.wi, ctx);
+    const Eval e = evaluate_inline(m, authored, won, s.wi, ctx);
     if (e.pdf <= 1e-12f) return empty_sample();
     s.value = e.value;
     s.pdf = e.pdf;

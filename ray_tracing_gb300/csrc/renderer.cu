@@ -1098,7 +1098,7 @@ struct rtgb_renderer {
         launch_raygen(d_fp, paths, d_counters, sh[0], stream);
         mark(k);
         for (int b = 0; b < mb; ++b) {
-            launch_trace(d_fp, scene, paths, d_counters, b, sh[1], stream);
+            launch_trace(d_fp, scene, paths, d_counters, b, sh[deep_bvh(scene) ? 14 : 1], stream);
             mark(k);
             launch_reset_counters(d_counters, b, stream);
             const bool pbr_scene = scene.openpbr_count > 0;
@@ -1106,7 +1106,7 @@ struct rtgb_renderer {
             launch_shade(d_fp, scene, paths, d_counters, b, sh[pbr_scene ? 7 : 2], sh[13], stream);
             if (b == 0) launch_restir(d_fp, scene, paths, d_counters, sh, stream);
             mark(k);
-            launch_shadow(d_fp, scene, paths, d_counters, b, sh[3], stream);
+            launch_shadow(d_fp, scene, paths, d_counters, b, sh[deep_bvh(scene) ? 15 : 3], stream);
             mark(k);
         }
         launch_finalize(d_fp, paths, d_counters, sh[4], stream);
@@ -1628,7 +1628,7 @@ rtgb_status rtgb_autotune_launches(rtgb_handle h, const rtgb_camera_rig* rig, co
         constexpr float kScales[kCandidates] = {0.5f, 1.0f, 2.0f, 4.0f, 0.5f, 1.0f, 2.0f, 4.0f};
         constexpr int kHalved[kCandidates] = {0, 0, 0, 0, 1, 1, 1, 1};
         // shape slots of each stage group (rtgb_launch_tuning::group_ms order)
-        static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1}, {2, 6, 7, 8, 9, 10, 11, 12, 13}, {3}, {4, 5}};
+        static const std::vector<int> kGroups[RTGB_TUNE_GROUPS] = {{0}, {1, 14}, {2, 6, 7, 8, 9, 10, 11, 12, 13}, {3, 15}, {4, 5}};
         *out = rtgb_launch_tuning {};
         LaunchShape base[kLaunchShapes];
         query_launch_shapes(h->sm_count, base);

@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(128, kSplit ? 6 : 1) k_shade(const FrameParams
                         const LightSample l = sample_direct<kPbr>(s, h, rng);
                         if (l.valid) {
                             float bp = 0.0f;
-                            const float3 resp = direct_response<kPbr>(h, &pm, st.d, st.thr, l.direction, bp);
+                            const float3 resp = direct_response<kPbr, true>(h, &pm, st.d, st.thr, l.direction, bp);
                             if (max_comp(resp) > 0.0f) {
                                 const float max_t = l.infinite ? kRayFar : l.distance - kRayEpsilon * 3.0f;
                                 if (max_t > kRayEpsilon) {
@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(128, kSplit ? 6 : 1) k_shade(const FrameParams
                         const LightSample l = analytic_candidate(s, h.pos, li, u0, u1);
                         if (l.valid) {
                             float bp = 0.0f;
-                            const float3 resp = direct_response<kPbr>(h, &pm, st.d, st.thr, l.direction, bp);
+                            const float3 resp = direct_response<kPbr, true>(h, &pm, st.d, st.thr, l.direction, bp);
                             if (max_comp(resp) > 0.0f) {
                                 const float max_t = l.infinite ? kRayFar : l.distance - kRayEpsilon * 3.0f;
                                 if (max_t > kRayEpsilon) {

@@ -1079,10 +1079,19 @@ RTGB_D void openpbr_scattering(const DeviceScene& s, const Hit& h, pbr::Mat& m) 
 
 // OpenPBR branch of direct_material_response (programs.cu:1038-1054) with the
 // hit's scattering parameters already evaluated; `ray_d` is the incoming ray.
+// kInline: the BSDF evaluation inlined (the shade kernel) or the shared
+// out-of-line copy (the ReSTIR kernels' many call sites); same arithmetic.
+template <bool kInline>
 RTGB_D float3 openpbr_response(const pbr::Mat& m, const Hit& h, const float3& ray_d, const float3& thr,
     const float3& ldir, float& bsdf_pdf) {
     const pbr::Frame frame = pbr::make_frame(pv(h.gn), pbr::V3{0.0f, 0.0f, 0.0f});
-    const pbr::Eval e = pbr::evaluate(m, frame, pv(mul(normalize(ray_d), -1.0f)), pv(ldir), transport_context(thr));
+    const pbr::V3 wo = pv(mul(normalize(ray_d), -1.0f));
+    pbr::Eval e{};
+    if constexpr (kInline) {
+        e = pbr::evaluate_inline(m, frame, wo, pv(ldir), transport_context(thr));
+    } else {
+        e = pbr::evaluate(m, frame, wo, pv(ldir), transport_context(thr));
+    }
     const float cosine = fabsf(dot(h.sn, ldir));
     bsdf_pdf = e.pdf;
     return mul(fv(e.value), cosine);
@@ -1090,12 +1099,12 @@ RTGB_D float3 openpbr_response(const pbr::Mat& m, const Hit& h, const float3& ra
 
 // direct_material_response, programs.cu:1026-1055. `pm` holds the OpenPBR
 // scattering parameters when h.mtype == 5 (evaluated once per hit).
-template <bool kPbr>
+template <bool kPbr, bool kInline = false>
 RTGB_D float3 direct_response(const Hit& h, const pbr::Mat* pm, const float3& ray_d, const float3& thr,
     const float3& ldir, float& bsdf_pdf) {
     bsdf_pdf = 0.0f;
     if constexpr (kPbr) {
-        if (h.mtype == 5) return openpbr_response(*pm, h, ray_d, thr, ldir, bsdf_pdf);
+        if (h.mtype == 5) return openpbr_response<kInline>(*pm, h, ray_d, thr, ldir, bsdf_pdf);
     }
     if (h.mtype == 0) {
         const float c = fmaxf(dot(h.sn, ldir), 0.0f);

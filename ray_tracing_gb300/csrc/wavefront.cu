@@ -94,8 +94,11 @@ RTGB_D int stage_nodes4(const DeviceScene& s, float4* smem4) {
 
 constexpr int kStagedBytes = kStagedNodes4 * kNode4 * static_cast<int>(sizeof(float4));
 
-// intersect_scene (programs.cu:1654-1757) + intersect_analytic_lights (:795-813)
-__global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+// intersect_scene (programs.cu:1654-1757) + intersect_analytic_lights (:795-813).
+// kDeep: the instance for deep hierarchies (deep_bvh), held to 80 registers so
+// six blocks share an SM.
+template <bool kDeep>
+__global__ void __launch_bounds__(128, kDeep ? 6 : 1) k_trace(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
     extern __shared__ float4 smem4[];
     const int staged = stage_nodes4(s, smem4);
@@ -143,7 +146,8 @@ __global__ void __launch_bounds__(128) k_trace(const FrameParams* __restrict__ f
 
 // is_occluded (programs.cu:1759-1762) for the bounce's NEE samples; visible
 // contributions are added in slot order (emissive geometry, then analytic).
-__global__ void __launch_bounds__(128) k_shadow(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
+template <bool kDeep>
+__global__ void __launch_bounds__(128, kDeep ? 6 : 1) k_shadow(const FrameParams* __restrict__ fpp, DeviceScene s, Paths P,
     Counters* counters, int bounce) {
     extern __shared__ float4 smem4[];
     const int staged = stage_nodes4(s, smem4);
@@ -359,7 +363,11 @@ void launch_raygen(const FrameParams* fp, Paths paths, Counters* counters, Launc
 
 void launch_trace(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
     LaunchShape shape, cudaStream_t stream) {
-    k_trace<<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    if (deep_bvh(scene)) {
+        k_trace<true><<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    } else {
+        k_trace<false><<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    }
 }
 
 void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce,
@@ -373,7 +381,11 @@ void launch_shade(const FrameParams* fp, DeviceScene scene, Paths paths, Counter
 
 void launch_shadow(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters, int bounce, LaunchShape shape,
     cudaStream_t stream) {
-    k_shadow<<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    if (deep_bvh(scene)) {
+        k_shadow<true><<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    } else {
+        k_shadow<false><<<shape.grid, shape.block, kStagedBytes, stream>>>(fp, scene, paths, counters, bounce);
+    }
 }
 
 void launch_restir(const FrameParams* fp, DeviceScene scene, Paths paths, Counters* counters,
@@ -399,12 +411,16 @@ void query_launch_shapes(int sm_count, LaunchShape* shapes) {
     int blocks = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_raygen, 256, 0);
     shapes[0] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 256};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace, 128, kStagedBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace<false>, 128, kStagedBytes);
     shapes[1] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_trace<true>, 128, kStagedBytes);
+    shapes[14] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shade<false>, 128, 0);
     shapes[2] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shadow, 128, kStagedBytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shadow<false>, 128, kStagedBytes);
     shapes[3] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_shadow<true>, 128, kStagedBytes);
+    shapes[15] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 128};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_finalize, 256, 0);
     shapes[4] = LaunchShape{sm_count * (blocks > 0 ? blocks : 1), 256};
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_resolve, 256, 0);

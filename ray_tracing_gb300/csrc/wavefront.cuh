@@ -138,9 +138,20 @@ void launch_reset_counters(Counters* counters, int bounce, cudaStream_t stream);
 // shapes[0..6]: raygen, trace, shade, shadow, finalize, resolve, restir;
 // shapes[7..8]: the OpenPBR instances of shade and restir; [9..10]: restir RIS
 // and visibility passes; [11..12]: their OpenPBR instances; [13]: k_scatter
-// (OpenPBR BSDF sampling after k_shade).
+// (OpenPBR BSDF sampling after k_shade); [14..15]: the deep-hierarchy
+// instances of trace and shadow (deep_bvh).
 void query_launch_shapes(int sm_count, LaunchShape* shapes);
-constexpr int kLaunchShapes = 14;
+constexpr int kLaunchShapes = 16;
+
+// Scenes whose wide BVH has at least this many nodes (4 MB) trace with the
+// 80-register instances of k_trace / k_shadow, six blocks per SM: their node
+// fetches miss the L1 and wait on L2 / DRAM, and more warps in flight hide
+// that (the 4 M-triangle room: trace 27.8 against 30.3 ms, shadow 20.7 against
+// 22.5 ms per frame); shallow ones keep the 90-register instances, whose
+// traversal is cache-resident and slower with spills (the benchmark frame:
+// 0.588 against 0.600 ms of trace).
+constexpr int kDeepBvhNodes4 = 1 << 15;
+inline bool deep_bvh(const DeviceScene& s) { return s.node4_count >= kDeepBvhNodes4; }
 
 // Reuse sources kept per path by the ReSTIR passes: temporal + up to 8 spatial.
 constexpr int kMaxReuseSources = 9;
