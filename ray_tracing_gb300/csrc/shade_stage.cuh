@@ -617,7 +617,10 @@ __global__ void __launch_bounds__(128, kSplit ? 6 : 1) k_shade(const FrameParams
                     keep = bounce + 1 < fp.max_bounces;
                     if (fp.record_paths) record_decision(P, fp, path, bounce, kDecisionWalk << 2);
                 } else if (walk == 0) {
-                    pbr::Mat pm;
+                    // shared, not stack: as in k_scatter (one slot for the
+                    // legacy instances, which never touch it)
+                    __shared__ pbr::Mat shade_mats[kPbr ? 128 : 1];
+                    pbr::Mat& pm = shade_mats[kPbr ? threadIdx.x : 0];
                     if constexpr (kPbr) {
                         if (h.mtype == 5) openpbr_scattering(s, h, pm);
                     }
@@ -741,7 +744,12 @@ __global__ void __launch_bounds__(128, 6) k_scatter(const FrameParams* __restric
         uint32_t rng = P.rng[path];
         Hit h;
         rebuild_hit<kPbr>(s, hr, st, h);  // rebuilt in k_shade from the same record
-        pbr::Mat pm;
+        // The thread's OpenPBR parameters live in shared memory: the BSDF
+        // sampler is an out-of-line call that reads them by reference, and on
+        // the stack they would travel through L1 / L2 with every other
+        // thread's stack (204 B a thread, an odd word stride: no bank conflicts).
+        __shared__ pbr::Mat mats[128];
+        pbr::Mat& pm = mats[threadIdx.x];
         if constexpr (kPbr) {
             if (h.mtype == 5) openpbr_scattering(s, h, pm);
         }
