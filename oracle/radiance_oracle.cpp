@@ -189,8 +189,9 @@ V3 average_texture(const Scene& s, int index, int depth) {
         if (t.image_offset < 0 || t.image_offset + count > static_cast<int>(s.texels.size() / 3)) return {0, 0, 0};
         V3 sum{0, 0, 0};
         for (int i = 0; i < count; ++i) sum = add(sum, from3(&s.texels[3 * static_cast<size_t>(t.image_offset + i)]));
-        const V3 avg = mul(sum, 1.0f / static_cast<float>(count));
-        return {std::max(avg.x, 0.0f), std::max(avg.y, 0.0f), std::max(avg.z, 0.0f)};
+        // sum / count per component, as the reference divides (not a multiply by the reciprocal)
+        const float n = static_cast<float>(count);
+        return {std::max(sum.x / n, 0.0f), std::max(sum.y / n, 0.0f), std::max(sum.z / n, 0.0f)};
     }
     if (t.type == 3) return {0.5f, 0.5f, 0.5f};
     return {0, 0, 0};
