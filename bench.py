@@ -25,7 +25,9 @@ equal_relmse: the headline comparison. A 4096-spp plain render of the same
           The denoised pipeline's relMSE and ms/frame are measured, then the
           plain path (no ReSTIR, no denoiser) is run at doubling sample counts
           until its relMSE is no larger; its ms/frame there over the denoised
-          ms/frame is the speed-up at equal relMSE.
+          ms/frame is the speed-up at equal relMSE. The C5 record adds
+          trimmed_cross_check: both sides' relMSE without the largest 0.1 % of
+          per-value errors (fireflies), read off the same probes.
 roofline: the launch with the largest share of the frame, per-unit algorithmic
           bytes (SoA stream bytes per ray / path segment / pixel) over its CUDA-event durations, against the measured
           HBM copy bandwidth.
@@ -118,6 +120,29 @@ SPP_PER_FRAME = 16      # plain renders above this run as several frames, averag
 def relmse(x: np.ndarray, ref: np.ndarray) -> float:
     x = x.astype(np.float64)
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + RELMSE_EPS)))
+
+
+TRIM_FRACTION = 1e-3  # largest per-value errors left out of the firefly-trimmed relMSE
+
+
+def relmse_trimmed(x: np.ndarray, ref: np.ndarray, trim: float = TRIM_FRACTION) -> float:
+    """relMSE without the `trim` fraction of largest per-value errors: a
+    cross-check that rare bright paths (fireflies) do not decide an
+    equal-relMSE comparison on a small band sample."""
+    e = ((x.astype(np.float64) - ref) ** 2 / (ref ** 2 + RELMSE_EPS)).ravel()
+    keep = e.size - int(np.floor(e.size * trim))
+    if keep <= 0:
+        return 0.0
+    if keep < e.size:
+        e = np.partition(e, keep - 1)[:keep]
+    return float(np.mean(e))
+
+
+def first_spp_within(trail: list, key: str, target: float):
+    """The smallest probed spp of `trail` whose `key` is no larger than
+    `target` (None if none is)."""
+    hits = sorted((p["spp"] for p in trail if p.get(key) is not None and p[key] <= target))
+    return hits[0] if hits else None
 
 
 def plain_render(r, rig, spp: int, cameras: int = CAMERAS, max_bounces: int = 4, per_frame: int = SPP_PER_FRAME,
@@ -229,15 +254,30 @@ def banded_equal_relmse(sc, frame_rigs: dict, variants: dict, max_bounces: int, 
         def err(imgs, f):
             return float(np.mean([relmse(imgs[c], refs[f][c]) for c in range(cameras)]))
 
+        def err_trimmed(imgs, f):
+            return float(np.mean([relmse_trimmed(imgs[c], refs[f][c]) for c in range(cameras)]))
+
         probes = {}
 
         def probe(spp):
             if spp not in probes:
-                per = {f: err(plain_bands(r, frame_rigs[f], cameras, spp, max_bounces, per_frame=16)[0], f)
-                       for f in frame_rigs}
+                per, trimmed = {}, []
+                for f in frame_rigs:
+                    imgs = plain_bands(r, frame_rigs[f], cameras, spp, max_bounces, per_frame=16)[0]
+                    per[f] = err(imgs, f)
+                    trimmed.append(err_trimmed(imgs, f))
                 probes[spp] = {"spp": spp, "relmse": float(np.mean(list(per.values()))),
+                               "relmse_trimmed": float(np.mean(trimmed)),
                                "per_frame": {str(f): v for f, v in per.items()}}
             return probes[spp]
+
+        def plain_ms(spp):
+            first = next(iter(frame_rigs))
+            timed = min(spp, time_spp_cap)
+            if timed not in timed_ms:
+                timed_ms[timed] = plain_render(r, frame_rigs[first], timed, cameras=cameras,
+                                               max_bounces=max_bounces, per_frame=4, images=False)[1]
+            return timed_ms[timed] * spp / timed, timed
 
         timed_ms = {}
         for name, (denoised, den_ms) in variants.items():
@@ -261,12 +301,8 @@ def banded_equal_relmse(sc, frame_rigs: dict, variants: dict, max_bounces: int, 
                         lo = mid
             plain = None
             if found is not None:
-                first = next(iter(frame_rigs))
-                timed = min(found["spp"], time_spp_cap)
-                if timed not in timed_ms:
-                    timed_ms[timed] = plain_render(r, frame_rigs[first], timed, cameras=cameras,
-                                                   max_bounces=max_bounces, per_frame=4, images=False)[1]
-                plain = dict(found, ms=timed_ms[timed] * found["spp"] / timed, timed_spp=timed)
+                ms, timed = plain_ms(found["spp"])
+                plain = dict(found, ms=ms, timed_spp=timed)
             results[name] = {
                 "denoised": {"relmse": target, "per_frame": {str(f): v for f, v in d_err.items()},
                              "ms_per_frame": den_ms},
@@ -274,6 +310,21 @@ def banded_equal_relmse(sc, frame_rigs: dict, variants: dict, max_bounces: int, 
                 "plain_search": trail,
                 "speedup_at_equal_relmse": (plain["ms"] / den_ms) if plain is not None else None,
             }
+            # cross-check on the same renders: both sides' relMSE without the
+            # largest TRIM_FRACTION of per-value errors, the plain side read off
+            # the probes the search above already took (no new search)
+            try:
+                d_trim = float(np.mean([err_trimmed(denoised[f], f) for f in frame_rigs]))
+                t_spp = first_spp_within(list(probes.values()), "relmse_trimmed", d_trim)
+                t_ms = plain_ms(t_spp)[0] if t_spp is not None else None
+                results[name]["trimmed_cross_check"] = {
+                    "trim_fraction": TRIM_FRACTION, "denoised_relmse_trimmed": d_trim,
+                    "plain_spp": t_spp, "plain_ms": t_ms,
+                    "speedup": (t_ms / den_ms) if t_ms is not None else None,
+                    "note": "smallest probed spp within the trimmed target" if t_spp is not None
+                            else "no probed spp within the trimmed target"}
+            except Exception as e:  # the cross-check never costs the record
+                results[name]["trimmed_cross_check"] = {"error": f"{type(e).__name__}: {e}"}
     names = list(results)
     out = {"eps": RELMSE_EPS, "reference_spp": ref_spp, "frames": [int(f) for f in frame_rigs],
            "sample": f"{BAND_COUNT} bands of {BAND_ROWS} rows per camera (evenly spaced), rendered as cropped "

@@ -5,6 +5,7 @@ import json
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -62,3 +63,82 @@ def test_mixed_1080p_rig_for_the_relmse_target():
         e = rig.cameras[i].equi
         assert e.fx == pytest.approx(f) and e.cx == 960.0 and e.cy == 540.0
         assert all(e.lut[k] <= e.lut[k + 1] for k in range(len(e.lut) - 1))   # monotone theta(r) table
+
+
+def test_trimmed_relmse_drops_only_the_largest_errors():
+    rng = np.random.default_rng(3)
+    ref = rng.uniform(0.5, 1.5, (64, 100, 3))
+    x = ref * (1.0 + rng.normal(0.0, 0.05, ref.shape))
+    base = bench.relmse(x, ref)
+    assert bench.relmse_trimmed(x, ref, trim=0.0) == pytest.approx(base)
+    # one firefly dominates the plain relMSE but not the trimmed one
+    y = x.copy()
+    y[10, 20, 1] = 5000.0
+    assert bench.relmse(y, ref) > 100 * base
+    e = ((x - ref) ** 2 / (ref ** 2 + bench.RELMSE_EPS)).ravel()
+    keep = e.size - int(np.floor(e.size * bench.TRIM_FRACTION))
+    rest = np.delete(e, np.ravel_multi_index((10, 20, 1), ref.shape))  # the firefly is the largest error
+    assert bench.relmse_trimmed(y, ref) == pytest.approx(np.sort(rest)[:keep].mean())
+    assert bench.relmse_trimmed(y, ref) < 1.1 * base
+
+
+def test_first_spp_within_reads_the_smallest_probe():
+    trail = [{"spp": 1, "t": 9.0}, {"spp": 16, "t": 0.5}, {"spp": 8, "t": 0.7}, {"spp": 4, "t": 0.2},
+             {"spp": 2, "t": None}]
+    assert bench.first_spp_within(trail, "t", 0.6) == 4
+    assert bench.first_spp_within(trail, "t", 0.1) is None
+    assert bench.first_spp_within([], "t", 1.0) is None
+
+
+def test_banded_search_and_trimmed_cross_check_with_a_fake_renderer(monkeypatch):
+    # the search logic of the C5 equal-relMSE record on CPU: plain renders are
+    # the reference plus noise shrinking as 1/sqrt(spp), with a firefly at 16 spp
+    import types
+    import ray_tracing_gb300.renderer as rmod
+
+    class FakeRenderer:
+        def __init__(self, *a, **k):
+            pass
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            return False
+
+        def prepare_scene(self, view):
+            pass
+
+        def reset_sequence(self, s):
+            pass
+
+    rng0 = np.random.default_rng(11)
+    truth = [rng0.uniform(0.2, 2.0, (16, 40, 3)) for _ in range(2)]
+
+    def fake_bands(r, rig, cameras, spp, max_bounces, per_frame):
+        rng = np.random.default_rng(spp * 7 + rig)
+        bands = [t * (1.0 + rng.normal(0.0, 0.8 / np.sqrt(spp), t.shape)) for t in truth[:cameras]]
+        if spp == 16:
+            bands[0][3, 5, 0] = 1e4  # a firefly
+        return bands, 1.0
+
+    monkeypatch.setattr(rmod, "Renderer", FakeRenderer)
+    monkeypatch.setattr(bench, "plain_bands", fake_bands)
+    monkeypatch.setattr(bench, "plain_render", lambda r, rig, spp, **k: (None, float(spp)))
+    rng = np.random.default_rng(5)
+    denoised = {0: [t * (1.0 + rng.normal(0.0, 0.1, t.shape)) for t in truth],
+                1: [t * (1.0 + rng.normal(0.0, 0.1, t.shape)) for t in truth]}
+    out = bench.banded_equal_relmse(types.SimpleNamespace(view=None), {0: 0, 1: 1}, {"nee": (denoised, 2.0)},
+                                    max_bounces=6, cameras=2, ref_spp=4096, max_spp=1024, time_spp_cap=128)
+    spp = out["plain"]["spp"]
+    assert spp is not None and out["plain"]["relmse"] <= out["denoised"]["relmse"]
+    assert out["speedup_at_equal_relmse"] == pytest.approx(out["plain"]["ms"] / 2.0)
+    cc = out["trimmed_cross_check"]
+    assert "error" not in cc and cc["plain_spp"] is not None
+    assert cc["speedup"] == pytest.approx(cc["plain_ms"] / 2.0)
+    trail = out["plain_search"]
+    assert all("relmse_trimmed" in p for p in trail)
+    # the firefly inflates the 16-spp relMSE, not its trimmed value
+    p16 = next(p for p in trail if p["spp"] == 16)
+    p8 = next(p for p in trail if p["spp"] == 8)
+    assert p16["relmse"] > p8["relmse"] and p16["relmse_trimmed"] < p8["relmse_trimmed"]
