@@ -372,7 +372,7 @@ def equal_relmse(sc, rig, prof, frames: int = 8):
     r.reset_sequence(SEED)
     for _ in range(5):
         r.render_frame(rig, prof, CAMERAS)
-    d_err, d_ms, d_dn, n_err, p_err1 = [], [], [], [], []
+    d_err, d_ms, d_dn, n_err, d_trim = [], [], [], [], []
     for _ in range(frames):
         v = r.render_frame(rig, prof, CAMERAS)
         d_ms.append(v.frame_render_ms)
@@ -380,6 +380,7 @@ def equal_relmse(sc, rig, prof, frames: int = 8):
         den = np.stack([r.buffer(c, "denoised")[..., :3] for c in range(CAMERAS)])
         noisy = np.stack([r.buffer(c, "beauty")[..., :3] for c in range(CAMERAS)])
         d_err.append(relmse(den, ref))
+        d_trim.append(relmse_trimmed(den, ref))
         n_err.append(relmse(noisy, ref))
     target = float(np.mean(d_err))
     den_ms = float(np.median(d_ms))
@@ -389,7 +390,7 @@ def equal_relmse(sc, rig, prof, frames: int = 8):
     while spp <= 2048:
         img, ms = plain_render(r, rig, spp)
         e = relmse(img, ref)
-        trail.append({"spp": spp, "relmse": e, "ms": ms})
+        trail.append({"spp": spp, "relmse": e, "relmse_trimmed": relmse_trimmed(img, ref), "ms": ms})
         if e <= target:
             found = trail[-1]
             break
@@ -400,7 +401,7 @@ def equal_relmse(sc, rig, prof, frames: int = 8):
             mid = (lo + hi) // 2
             img, ms = plain_render(r, rig, mid)
             e = relmse(img, ref)
-            trail.append({"spp": mid, "relmse": e, "ms": ms})
+            trail.append({"spp": mid, "relmse": e, "relmse_trimmed": relmse_trimmed(img, ref), "ms": ms})
             if e <= target:
                 hi, found = mid, trail[-1]
             else:
@@ -412,6 +413,16 @@ def equal_relmse(sc, rig, prof, frames: int = 8):
         "plain_search": trail,
         "speedup_at_equal_relmse": (found["ms"] / den_ms) if found is not None else None,
     })
+    # the firefly-trimmed cross-check on the same renders (as the C5 record's)
+    try:
+        t_target = float(np.mean(d_trim))
+        t_spp = first_spp_within(trail, "relmse_trimmed", t_target)
+        t_ms = next((p["ms"] for p in trail if p["spp"] == t_spp), None)
+        out["trimmed_cross_check"] = {"trim_fraction": TRIM_FRACTION, "denoised_relmse_trimmed": t_target,
+                                      "plain_spp": t_spp, "plain_ms": t_ms,
+                                      "speedup": (t_ms / den_ms) if t_ms is not None else None}
+    except Exception as e:  # the cross-check never costs the record
+        out["trimmed_cross_check"] = {"error": f"{type(e).__name__}: {e}"}
     r.close()
     return out
 

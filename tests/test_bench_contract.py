@@ -142,3 +142,53 @@ def test_banded_search_and_trimmed_cross_check_with_a_fake_renderer(monkeypatch)
     p16 = next(p for p in trail if p["spp"] == 16)
     p8 = next(p for p in trail if p["spp"] == 8)
     assert p16["relmse"] > p8["relmse"] and p16["relmse_trimmed"] < p8["relmse_trimmed"]
+
+
+def test_headline_equal_relmse_with_a_fake_renderer(monkeypatch):
+    # the benchmark frame's search and its trimmed cross-check on CPU
+    import types
+    import ray_tracing_gb300.renderer as rmod
+
+    rng0 = np.random.default_rng(2)
+    truth = rng0.uniform(0.2, 2.0, (4, 12, 16, 3))
+
+    class FakeRenderer:
+        def __init__(self, *a, **k):
+            self.rng = np.random.default_rng(9)
+
+        def prepare_scene(self, view):
+            pass
+
+        def reset_sequence(self, s):
+            pass
+
+        def set_denoiser(self, w):
+            pass
+
+        def render_frame(self, rig, prof, n):
+            cam = types.SimpleNamespace(denoise_ms=0.5)
+            return types.SimpleNamespace(frame_render_ms=2.5, cameras=[cam])
+
+        def buffer(self, c, name):
+            noise = 0.1 if name == "denoised" else 1.0
+            img = truth[c] * (1.0 + self.rng.normal(0.0, noise, truth[c].shape))
+            return np.concatenate([img, np.ones(img.shape[:2] + (1,))], axis=-1)
+
+        def close(self):
+            pass
+
+    def fake_plain(r, rig, spp, **k):
+        rng = np.random.default_rng(spp)
+        img = truth * (1.0 + rng.normal(0.0, 1.0 / np.sqrt(spp), truth.shape))
+        return img, float(spp)
+
+    monkeypatch.setattr(rmod, "Renderer", FakeRenderer)
+    monkeypatch.setattr(bench, "plain_render", fake_plain)
+    monkeypatch.setattr(bench, "_weights", lambda: np.zeros(1))
+    out = bench.equal_relmse(types.SimpleNamespace(view=None), None, None, frames=3)
+    assert out["plain"]["spp"] is not None
+    assert out["speedup_at_equal_relmse"] == pytest.approx(out["plain"]["ms"] / 2.5)
+    cc = out["trimmed_cross_check"]
+    assert "error" not in cc and cc["plain_spp"] is not None
+    assert cc["speedup"] == pytest.approx(cc["plain_ms"] / 2.5)
+    assert all("relmse_trimmed" in p for p in out["plain_search"])
